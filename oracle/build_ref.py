@@ -1,0 +1,137 @@
+#!/usr/bin/env python3
+"""Build recipe for oracle/_ref — TEST INFRASTRUCTURE ONLY.
+
+Compiles the reference's own CPU FacetRT backend (StreamSim HiStream,
+models/histream/src/facetrt/facetrtcore.cpp) into oracle/_ref/libfacetrt_ref.so
+so that the C restatement in oracle/facet_oracle.c can be pinned against it.
+
+The reference file also holds a Vulkan driver, a GDAL texture loader and a
+JSON project loader that need libraries absent here, so the recipe takes the
+self-contained CPU span by line range (the same ranges on every run, checked
+against anchor lines first), wraps it in the reference header's POD types and
+appends the extern "C" wrappers of oracle/ref_shim.inc:
+
+    facetrt_vulkan.h   15-62     Vertex, Direction, SurfaceOptics, Config,
+                                 GraphDiagnostics, SolveResult
+    facetrtcore.cpp    39-53     Clock/Vec3 aliases
+    facetrtcore.cpp    74-630    constants, Scene, geometry, optics helpers
+    facetrtcore.cpp    703-1620  CpuRasterizer .. runCpu
+
+Everything generated goes to oracle/_ref/ (git-ignored).  The generated
+source travels with the repository snapshot, so on a machine without the
+reference tree `python oracle/build_ref.py` recompiles it from there.
+
+It is compiled with -ffp-contract=off: the shipped Windows build does not
+fuse multiply-adds, and GCC on aarch64 would otherwise fuse them.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+SRC = os.path.join(OUT, "facetrt_ref.cpp")
+LIB = os.path.join(OUT, "libfacetrt_ref.so")
+REFERENCE = os.environ.get("FACETRT_REFERENCE_ROOT", "/root/reference")
+FACETRT = os.path.join(REFERENCE, "models", "histream", "src", "facetrt")
+
+RANGES = [
+    ("facetrt_vulkan.h", 15, 62, "namespace facetvk {", "}"),
+    ("facetrtcore.cpp", 39, 53, "namespace {", None),
+    ("facetrtcore.cpp", 74, 630, None, None),
+    ("facetrtcore.cpp", 703, 1620, None, "}  // namespace"),
+]
+# (file, line, text the line must start with) — guards against a different
+# revision of the reference.
+ANCHORS = [
+    ("facetrt_vulkan.h", 15, "struct Vertex {"),
+    ("facetrt_vulkan.h", 62, "};"),
+    ("facetrtcore.cpp", 39, "using Clock"),
+    ("facetrtcore.cpp", 74, "constexpr float kPi"),
+    ("facetrtcore.cpp", 1212, "class CpuRasterizer"),
+    ("facetrtcore.cpp", 1348, "CpuGraph buildCpuGraph("),
+    ("facetrtcore.cpp", 1438, "std::vector<float> computeCpuSunlit("),
+    ("facetrtcore.cpp", 1476, "facetvk::SolveResult solveCpu("),
+    ("facetrtcore.cpp", 1585, "RunResult runCpu("),
+    ("facetrtcore.cpp", 1621, "RunResult runGpu("),
+    ("facetrtcore.cpp", 631, "std::shared_ptr<const ReflectanceVarianceTexture> loadReflectanceVarianceTexture("),
+]
+PRELUDE = """// GENERATED by oracle/build_ref.py from the reference tree. Not product
+// code and not committed: test infrastructure for parity checks only.
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <chrono>
+#include <cctype>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <filesystem>
+#include <fstream>
+#include <functional>
+#include <iomanip>
+#include <iostream>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+"""
+
+
+def _lines(name):
+    with open(os.path.join(FACETRT, name), encoding="utf-8") as f:
+        return f.read().split("\n")
+
+
+def generate():
+    cache = {}
+    for name, line, text in ANCHORS:
+        lines = cache.setdefault(name, _lines(name))
+        if not lines[line - 1].lstrip().startswith(text):
+            raise SystemExit(f"build_ref: {name}:{line} does not start with {text!r}; "
+                             "the reference revision differs from the one this recipe expects")
+    parts = [PRELUDE]
+    for name, lo, hi, before, after in RANGES:
+        lines = cache.setdefault(name, _lines(name))
+        if before:
+            parts.append(before)
+        parts.append(f"// ---- {name}:{lo}-{hi}")
+        parts.extend(lines[lo - 1:hi])
+        if after:
+            parts.append(after)
+    with open(os.path.join(HERE, "ref_shim.inc"), encoding="utf-8") as f:
+        parts.append(f.read())
+    os.makedirs(OUT, exist_ok=True)
+    with open(SRC, "w", encoding="utf-8") as f:
+        f.write("\n".join(parts) + "\n")
+
+
+def compile_lib():
+    cmd = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-fPIC", "-shared",
+           "-w", SRC, "-o", LIB]
+    subprocess.run(cmd, check=True)
+
+
+def main():
+    if os.path.isdir(FACETRT):
+        generate()
+    elif not os.path.exists(SRC):
+        print("build_ref: reference tree absent and no generated source; skipping",
+              file=sys.stderr)
+        return 0
+    compile_lib()
+    print(LIB)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

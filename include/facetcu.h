@@ -1,0 +1,208 @@
+/*
+ * facetcu.h — C ABI of the GB300 FacetRT facet-radiosity library.
+ *
+ * This is the library seam that replaces StreamSim HiStream's Vulkan backend
+ * class facetvk::FacetrtVulkan (models/histream/src/facetrt/facetrt_vulkan.h:70-104).
+ * Plain C types, plain pointers and sizes; every function returns an int
+ * status (FACETCU_OK = 0) and keeps a message for facetcu_last_error().
+ * One context = one GPU, one CUDA stream, one thread at a time (the
+ * reference object is single-threaded and non-reentrant, facetrt_vulkan.cpp:292-301).
+ * Every call is synchronous unless its name ends in _device or _async.
+ *
+ * Side convention (facetrt_vulkan.h:28-29): side 2f is the geometric-normal
+ * side of facet f, side 2f+1 the opposite side.
+ */
+#ifndef FACETCU_H
+#define FACETCU_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FACETCU_ABI_VERSION 1
+
+/* Status codes.  The first four map to the exception classes the reference
+ * throws (facetrt_vulkan.cpp), so a C++ wrapper can re-throw them. */
+enum {
+    FACETCU_OK = 0,
+    FACETCU_INVALID_ARGUMENT = 1, /* std::invalid_argument */
+    FACETCU_LOGIC_ERROR = 2,      /* std::logic_error: call-order violation */
+    FACETCU_RUNTIME_ERROR = 3,    /* std::runtime_error: overflow, no samples */
+    FACETCU_OVERFLOW_ERROR = 4,   /* std::overflow_error: capacity exceeded */
+    FACETCU_CUDA_ERROR = 5,       /* CUDA runtime failure */
+    FACETCU_NO_DEVICE = 6,        /* no usable GPU */
+    FACETCU_OUT_OF_MEMORY = 7,    /* device allocation failed */
+    FACETCU_DEVICE_CAPACITY = 8,  /* a device-side capacity flag was raised */
+    FACETCU_NOT_CONVERGED = 9     /* iteration budget spent; result still written */
+};
+
+typedef struct facetcu_context facetcu_context;
+
+/* facetvk::Vertex (facetrt_vulkan.h:15-18): 24 bytes. */
+typedef struct { float position[3]; float normal[3]; } facetcu_vertex;
+/* facetvk::Direction (facetrt_vulkan.h:22-26): towards the camera / sun. */
+typedef struct { float x, y, z; } facetcu_direction;
+/* facetvk::SurfaceOptics (facetrt_vulkan.h:30-35): 16 bytes per side. */
+typedef struct {
+    float reflectance, transmittance, emission, direct_irradiance;
+} facetcu_surface_optics;
+/* facetvk::Config (facetrt_vulkan.h:37-47), same field order and layout.
+ * max_fragments_per_pixel is the reference's A-buffer depth: a pixel chain
+ * longer than it is reported as fragment overflow and fails the build, as
+ * in the reference; the device lists themselves have no fixed depth.
+ * edge_hash_capacity is accepted and ignored (the graph is built by sorting,
+ * not hashing, so hash overflow cannot occur). */
+typedef struct {
+    uint32_t raster_width;
+    uint32_t raster_height;
+    uint32_t max_fragments_per_pixel;
+    uint32_t edge_hash_capacity;
+    bool enable_validation;
+    uint32_t gpu_index;
+    uint32_t periodic_neighbor_count;
+    float periodic_size_x;
+    float periodic_size_z;
+} facetcu_config;
+/* facetvk::GraphDiagnostics (facetrt_vulkan.h:49-56). */
+typedef struct {
+    uint32_t facet_count;
+    uint32_t surface_count;
+    uint32_t directed_edge_count;
+    uint32_t fragment_overflow;
+    uint32_t hash_overflow;
+    float max_closure_error;
+} facetcu_graph_diagnostics;
+/* FacetrtVulkan::CsrEdge (facetrt_vulkan.h:114-117). */
+typedef struct { uint32_t neighbor, count; } facetcu_csr_edge;
+
+/* ---- lifetime -------------------------------------------------------- */
+int facetcu_create(facetcu_context **out);
+void facetcu_release(facetcu_context *ctx);
+const char *facetcu_last_error(const facetcu_context *ctx);
+int facetcu_device_count(int *count);
+
+/* FacetrtVulkan::initialize (facetrt_vulkan.h:80, facetrt_vulkan.cpp:98). */
+int facetcu_initialize(facetcu_context *ctx, const facetcu_config *config);
+/* FacetrtVulkan::destroy (facetrt_vulkan.h:102): frees device resources;
+ * the context may be initialized again. */
+int facetcu_destroy(facetcu_context *ctx);
+/* The CUDA stream all of the context's work runs on (cudaStream_t). */
+int facetcu_get_stream(facetcu_context *ctx, void **stream);
+
+/* ---- geometry and visibility ----------------------------------------- */
+/* FacetrtVulkan::setGeometry (facetrt_vulkan.cpp:445-471): non-indexed
+ * triangle list, 3 consecutive vertices per facet with the same unit normal.
+ * The orthographic raster frame uses the vertex bounds, as the Vulkan
+ * backend does (facetrt_vulkan.cpp:455-464). */
+int facetcu_set_geometry(facetcu_context *ctx, const facetcu_vertex *vertices,
+                         uint64_t vertex_count);
+/* Use explicit scene bounds for the raster frame instead of the vertex
+ * bounds — what the reference's CPU backend does (Scene::minimum/maximum in
+ * CpuRasterizer, facetrtcore.cpp:1222-1242). */
+int facetcu_set_raster_bounds(facetcu_context *ctx, const float minimum[3],
+                              const float maximum[3]);
+/* FacetrtVulkan::buildVisibilityGraph (facetrt_vulkan.cpp:866-1062), with
+ * the raster and pixel-chain rules of buildCpuGraph (facetrtcore.cpp:1348-1436):
+ * integer counts equal to the reference CPU backend's. */
+int facetcu_build_visibility_graph(facetcu_context *ctx,
+                                   const facetcu_direction *directions,
+                                   uint32_t direction_count,
+                                   facetcu_graph_diagnostics *diagnostics);
+/* FacetrtVulkan::computeSunlitFraction (facetrt_vulkan.cpp:1064-1158) with
+ * the rules of computeCpuSunlit (facetrtcore.cpp:1438-1474). fraction: 2F. */
+int facetcu_compute_sunlit_fraction(facetcu_context *ctx,
+                                    const facetcu_direction *sun_direction,
+                                    float *fraction);
+
+/* Graph access (count form: F_sn = count_sn / denom_s, sky_s / denom_s). */
+int facetcu_graph_size(facetcu_context *ctx, uint32_t *surface_count,
+                       uint64_t *directed_edge_count);
+/* Rows are sorted by neighbour.  Any pointer may be NULL. */
+int facetcu_get_graph(facetcu_context *ctx, uint32_t *row_offsets,
+                      facetcu_csr_edge *edges, uint32_t *denominators,
+                      uint32_t *sky_counts);
+/* Load a graph built elsewhere (e.g. by the reference); needs set_geometry. */
+int facetcu_set_graph(facetcu_context *ctx, uint32_t surface_count,
+                      const uint32_t *row_offsets, const facetcu_csr_edge *edges,
+                      const uint32_t *denominators, const uint32_t *sky_counts);
+
+/* ---- solves (reference semantics) ------------------------------------ */
+/* FacetrtVulkan::solve (facetrt_vulkan.cpp:1177-1247): `iterations` Jacobi
+ * sweeps from B = 0 with the two-sided update of radiosity.comp:49-106;
+ * FP32 gather in CSR order.  radiosity: 2F. */
+int facetcu_solve(facetcu_context *ctx, const facetcu_surface_optics *optics,
+                  float sky_radiosity, uint32_t iterations, float relaxation,
+                  float *radiosity, uint32_t *iterations_done, float *max_delta);
+/* FacetrtVulkan::solveAccelerated (facetrt_vulkan.cpp:1249-1358): optional
+ * warm start, batches of batch_iterations sweeps, stop when the absolute
+ * max|dB| of the last sweep <= tolerance. initial may be NULL. */
+int facetcu_solve_accelerated(facetcu_context *ctx, const facetcu_surface_optics *optics,
+                              float sky_radiosity, const float *initial,
+                              uint32_t maximum_iterations, uint32_t batch_iterations,
+                              float tolerance, float relaxation, float *radiosity,
+                              uint32_t *iterations_done, float *max_delta);
+/* FacetrtVulkan::incidentIrradiance (facetrt_vulkan.cpp:1360-1399):
+ * H_s = max(0, diffuse_s + D_s) from a solution, FP64 gather. */
+int facetcu_incident_irradiance(facetcu_context *ctx, const float *radiosity,
+                                const facetcu_surface_optics *optics,
+                                float sky_radiosity, float *irradiance);
+
+/* ---- batched solves (no reference counterpart) ------------------------ */
+/* Many right-hand sides against the one graph: R = band_count * sun_count
+ * columns, column r = sun * band_count + band.  Per band b and side s:
+ * reflectance[b*S+s], transmittance[b*S+s], emission[b*S+s] (NULL = 0),
+ * sky[b] and beam[b]; per sun k: direct_geometry[k*S+s] (the sunlit
+ * fraction times max(0, n_s . sun_k); NULL = no direct light).  The source
+ * for column (k,b) is D = beam[b] * direct_geometry[k*S+s].
+ * Iterates the reference's two-sided Jacobi sweep (relaxation 1) until, for
+ * every column, max_s |B_new - B| <= tolerance * max_s |B_new|, or
+ * maximum_iterations.  radiosity: R * S floats, column-major by RHS
+ * (radiosity[r*S + s]). */
+enum {
+    FACETCU_PRECISION_FP32 = 0,     /* FP32 gather */
+    FACETCU_PRECISION_MIXED = 1,    /* BF16 defect gather + FP32 residual correction */
+    FACETCU_PRECISION_FP64 = 2      /* FP64 state and gather (reference truth) */
+};
+enum {
+    FACETCU_WARM_NONE = 0,          /* start from B = 0 */
+    FACETCU_WARM_GIVEN = 1          /* start from `initial` (R * S floats) */
+};
+typedef struct {
+    uint32_t band_count;
+    uint32_t sun_count;
+    uint32_t precision;         /* FACETCU_PRECISION_* */
+    uint32_t warm_start;        /* FACETCU_WARM_* */
+    uint32_t maximum_iterations;
+    float tolerance;            /* relative change per column */
+    uint32_t panel_width;       /* RHS columns per resident panel; 0 = autotuned */
+    uint32_t flags;             /* reserved, 0 */
+} facetcu_batch_config;
+typedef struct {
+    uint32_t iterations;        /* sweeps of the slowest panel */
+    uint32_t residual_corrections;
+    uint32_t converged;         /* 1 if every column met the tolerance */
+    float max_relative_change;  /* worst column at exit */
+    double seconds;             /* device time of the solve */
+} facetcu_batch_result;
+int facetcu_solve_batched(facetcu_context *ctx, const facetcu_batch_config *config,
+                          const float *reflectance, const float *transmittance,
+                          const float *emission, const float *sky, const float *beam,
+                          const float *direct_geometry, const float *initial,
+                          float *radiosity, facetcu_batch_result *result);
+/* Same with every array already in device memory (pointers from
+ * cudaMalloc or a framework allocator); runs on the context stream and
+ * returns after the solve has finished. */
+int facetcu_solve_batched_device(facetcu_context *ctx, const facetcu_batch_config *config,
+                                 const float *reflectance, const float *transmittance,
+                                 const float *emission, const float *sky, const float *beam,
+                                 const float *direct_geometry, const float *initial,
+                                 float *radiosity, facetcu_batch_result *result);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FACETCU_H */

@@ -1,0 +1,829 @@
+// api.cpp — the extern "C" entry points of include/facetcu.h.
+//
+// Each entry point mirrors a member of facetvk::FacetrtVulkan
+// (models/histream/src/facetrt/facetrt_vulkan.{h,cpp}): same preconditions,
+// same validation rules and messages, same outputs; exceptions become status
+// codes (see facetcu.h).  Host arithmetic that must round as the reference's
+// CPU rasterizer does (the orthographic frame) is compiled with
+// -ffp-contract=off.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <limits>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+using namespace facetcu;
+
+struct facetcu_context {
+    std::string last_error;
+    bool initialized = false;
+    facetcu_config config{};
+    int device = -1;
+    cudaStream_t stream = nullptr;
+
+    uint32_t facets = 0;
+    std::vector<facetcu_vertex> vertices_host;
+    DeviceBuffer vertices;
+    float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
+    bool bounds_override = false;
+    float omin[3] = {0, 0, 0}, omax[3] = {0, 0, 0};
+
+    DeviceGraph graph;
+    bool graph_ready = false;
+
+    RasterBuffers raster;
+    DeviceBuffer pairs, pair_count, denom_tmp;
+    Workspace ws;
+
+    DeviceBuffer optics, rad_a, rad_b, residual, host_io, scratch;
+    DeviceBuffer sun_total, sun_visible;
+    BatchState batch;
+    DeviceBuffer batch_inputs;
+};
+
+namespace {
+
+int fail(facetcu_context* ctx, int code, const std::string& msg)
+{
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+template <typename F>
+int guarded(facetcu_context* ctx, F&& body)
+{
+    if (!ctx) return FACETCU_INVALID_ARGUMENT;
+    try {
+        ctx->last_error.clear();
+        return body();
+    } catch (const Error& e) {
+        return fail(ctx, e.code, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(ctx, FACETCU_OUT_OF_MEMORY, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(ctx, FACETCU_RUNTIME_ERROR, e.what());
+    }
+}
+
+void require_initialized(facetcu_context* ctx, const char* what)
+{
+    if (!ctx->initialized)
+        throw Error(FACETCU_LOGIC_ERROR, std::string("initialize() must be called before ") + what);
+    FCU_CHECK(cudaSetDevice(ctx->device));
+}
+
+void require_graph(facetcu_context* ctx, const char* what)
+{
+    require_initialized(ctx, what);
+    if (!ctx->graph_ready)
+        throw Error(FACETCU_LOGIC_ERROR,
+                    std::string("buildVisibilityGraph() must be called before ") + what);
+}
+
+// ---- host frame arithmetic (facetrtcore.cpp:262-269, :1222-1255) ----------
+using V3 = std::array<float, 3>;
+float dot(const V3& a, const V3& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+V3 cross(const V3& a, const V3& b)
+{
+    return {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+}
+V3 normalized(const V3& v, const char* what)
+{
+    const float length = std::sqrt(dot(v, v));
+    if (!(length > 1.0e-8f)) throw Error(FACETCU_INVALID_ARGUMENT, what);
+    const float inv = 1.0f / length;
+    return {v[0] * inv, v[1] * inv, v[2] * inv};
+}
+const int kTileOffsets[20][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}, {-1, -1}, {-1, 1}, {1, -1},
+                                 {1, 1},  {-2, 0}, {2, 0}, {0, -2}, {0, 2}, {-2, -1}, {-2, 1},
+                                 {2, -1}, {2, 1},  {-1, -2}, {1, -2}, {-1, 2}, {1, 2}};
+
+RasterFrame make_frame(const facetcu_context* ctx)
+{
+    RasterFrame f{};
+    const float* mn = ctx->bounds_override ? ctx->omin : ctx->bmin;
+    const float* mx = ctx->bounds_override ? ctx->omax : ctx->bmax;
+    V3 emin{mn[0], mn[1], mn[2]}, emax{mx[0], mx[1], mx[2]};
+    const uint32_t neighbours = std::min(ctx->config.periodic_neighbor_count, 20u);
+    f.tiles = neighbours + 1u;
+    f.tile_dx[0] = 0.0f;
+    f.tile_dz[0] = 0.0f;
+    for (uint32_t t = 1; t <= neighbours; ++t) {
+        const int* o = kTileOffsets[t - 1];
+        const float ox = float(o[0]) * ctx->config.periodic_size_x;
+        const float oz = float(o[1]) * ctx->config.periodic_size_z;
+        f.tile_dx[t] = ox;
+        f.tile_dz[t] = oz;
+        emin[0] = std::min(emin[0], mn[0] + ox);
+        emax[0] = std::max(emax[0], mx[0] + ox);
+        emin[2] = std::min(emin[2], mn[2] + oz);
+        emax[2] = std::max(emax[2], mx[2] + oz);
+    }
+    const V3 diag{emax[0] - emin[0], emax[1] - emin[1], emax[2] - emin[2]};
+    f.center[0] = (emin[0] + emax[0]) * 0.5f;
+    f.center[1] = (emin[1] + emax[1]) * 0.5f;
+    f.center[2] = (emin[2] + emax[2]) * 0.5f;
+    f.radius = std::max(0.5f * std::sqrt(dot(diag, diag)) * 1.001f, 1.0e-4f);
+    f.width = ctx->config.raster_width;
+    f.height = ctx->config.raster_height;
+    f.facets = ctx->facets;
+    return f;
+}
+
+RasterView make_view(const facetcu_direction& d)
+{
+    const V3 view = normalized({d.x, d.y, d.z}, "A visibility direction has zero length");
+    const V3 ref = std::abs(view[2]) < 0.9f ? V3{0.0f, 0.0f, 1.0f} : V3{0.0f, 1.0f, 0.0f};
+    const V3 right = normalized(cross(ref, view), "A visibility direction has zero length");
+    const V3 up = cross(view, right);
+    RasterView v{};
+    for (int i = 0; i < 3; ++i) {
+        v.right[i] = right[i];
+        v.up[i] = up[i];
+        v.view[i] = view[i];
+    }
+    return v;
+}
+
+int side_bits_for(uint32_t surfaces)
+{
+    int b = 1;
+    while ((1ull << b) < surfaces) ++b;
+    return b;
+}
+
+uint32_t chain_cap(const facetcu_context* ctx) { return ctx->config.max_fragments_per_pixel; }
+
+// facetrt_vulkan.cpp:1160-1175
+void validate_optics(const facetcu_surface_optics* optics, size_t n)
+{
+    if (!optics) throw Error(FACETCU_INVALID_ARGUMENT, "Optics array must contain exactly two sides per facet");
+    for (size_t i = 0; i < n; ++i) {
+        const facetcu_surface_optics& v = optics[i];
+        if (!std::isfinite(v.reflectance) || !std::isfinite(v.transmittance) ||
+            !std::isfinite(v.emission) || !std::isfinite(v.direct_irradiance) ||
+            v.reflectance < 0.0f || v.transmittance < 0.0f || v.emission < 0.0f ||
+            v.direct_irradiance < 0.0f || v.reflectance + v.transmittance > 1.0001f) {
+            throw Error(FACETCU_INVALID_ARGUMENT,
+                        "Optical values must be finite, non-negative, and reflectance+transmittance<=1");
+        }
+    }
+}
+
+void validate_sky(float sky)
+{
+    if (!std::isfinite(sky) || sky < 0.0f)
+        throw Error(FACETCU_INVALID_ARGUMENT, "skyRadiosity must be finite and non-negative");
+}
+
+void validate_relax(float r)
+{
+    if (!(r > 0.0f && r <= 1.0f))
+        throw Error(FACETCU_INVALID_ARGUMENT, "GPU Jacobi relaxation must be in (0,1]");
+}
+
+void upload(DeviceBuffer& buf, const void* src, size_t bytes, cudaStream_t s)
+{
+    buf.reserve(bytes);
+    if (bytes) FCU_CHECK(cudaMemcpyAsync(buf.ptr, src, bytes, cudaMemcpyHostToDevice, s));
+}
+
+// The plain Jacobi loop shared by solve and solveAccelerated.  Runs `count`
+// sweeps starting from buffer `ping`; each sweep's max|dB| lands in
+// residual[sweep_index].  Returns the new ping.
+uint32_t run_sweeps(facetcu_context* ctx, float sky, float relax, uint32_t count, uint32_t ping,
+                    uint32_t first_slot)
+{
+    float* a = ctx->rad_a.as<float>();
+    float* b = ctx->rad_b.as<float>();
+    uint32_t* res = ctx->residual.as<uint32_t>();
+    for (uint32_t i = 0; i < count; ++i) {
+        const float* in = ping == 0 ? a : b;
+        float* out = ping == 0 ? b : a;
+        jacobi_plain_sweep(ctx->graph, ctx->optics.as<facetcu_surface_optics>(), sky, relax, in,
+                           out, res + first_slot + i, ctx->stream);
+        ping ^= 1u;
+    }
+    return ping;
+}
+
+}  // namespace
+
+extern "C" {
+
+int facetcu_create(facetcu_context** out)
+{
+    if (!out) return FACETCU_INVALID_ARGUMENT;
+    try {
+        *out = new facetcu_context();
+    } catch (...) {
+        return FACETCU_OUT_OF_MEMORY;
+    }
+    return FACETCU_OK;
+}
+
+void facetcu_release(facetcu_context* ctx)
+{
+    if (!ctx) return;
+    facetcu_destroy(ctx);
+    delete ctx;
+}
+
+const char* facetcu_last_error(const facetcu_context* ctx)
+{
+    return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+int facetcu_device_count(int* count)
+{
+    if (!count) return FACETCU_INVALID_ARGUMENT;
+    int n = 0;
+    const cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *count = 0;
+        return FACETCU_OK;
+    }
+    *count = n;
+    return FACETCU_OK;
+}
+
+// FacetrtVulkan::initialize (facetrt_vulkan.cpp:98-110)
+int facetcu_initialize(facetcu_context* ctx, const facetcu_config* config)
+{
+    return guarded(ctx, [&] {
+        facetcu_destroy(ctx);
+        if (!config) throw Error(FACETCU_INVALID_ARGUMENT, "config is null");
+        if (config->raster_width == 0 || config->raster_height == 0)
+            throw Error(FACETCU_INVALID_ARGUMENT, "Raster dimensions must be positive");
+        if (config->max_fragments_per_pixel == 0 || config->max_fragments_per_pixel > 1024)
+            throw Error(FACETCU_INVALID_ARGUMENT, "maxFragmentsPerPixel must be in [1, 1024]");
+        if (uint64_t(config->raster_width) * config->raster_height > (1ull << 26))
+            throw Error(FACETCU_INVALID_ARGUMENT, "Raster exceeds 8192 x 8192 pixels");
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+            cudaGetLastError();
+            throw Error(FACETCU_NO_DEVICE, "No CUDA device is available for FacetRT");
+        }
+        if (int(config->gpu_index) >= n)
+            throw Error(FACETCU_INVALID_ARGUMENT, "gpuIndex exceeds the number of CUDA devices");
+        ctx->device = int(config->gpu_index);
+        FCU_CHECK(cudaSetDevice(ctx->device));
+        FCU_CHECK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        ctx->config = *config;
+        ctx->initialized = true;
+        return FACETCU_OK;
+    });
+}
+
+// FacetrtVulkan::destroy (facetrt_vulkan.cpp:1486-1516)
+int facetcu_destroy(facetcu_context* ctx)
+{
+    if (!ctx) return FACETCU_INVALID_ARGUMENT;
+    if (!ctx->initialized) return FACETCU_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->vertices.release();
+    ctx->graph.row_offsets.release();
+    ctx->graph.edges.release();
+    ctx->graph.denominators.release();
+    ctx->graph.sky.release();
+    ctx->graph.packed.release();
+    ctx->graph.packed_valid = false;
+    ctx->graph_ready = false;
+    for (DeviceBuffer* b : {&ctx->raster.counts, &ctx->raster.offsets, &ctx->raster.records,
+                            &ctx->raster.big_list, &ctx->raster.deep_list, &ctx->raster.stats,
+                            &ctx->pairs, &ctx->pair_count, &ctx->denom_tmp, &ctx->ws.a, &ctx->ws.b,
+                            &ctx->ws.c, &ctx->ws.d, &ctx->ws.e, &ctx->optics, &ctx->rad_a,
+                            &ctx->rad_b, &ctx->residual, &ctx->host_io, &ctx->scratch,
+                            &ctx->sun_total, &ctx->sun_visible, &ctx->batch.x0, &ctx->batch.x1,
+                            &ctx->batch.half, &ctx->batch.colstats, &ctx->batch.q,
+                            &ctx->batch.corr, &ctx->batch_inputs})
+        b->release();
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    ctx->stream = nullptr;
+    ctx->facets = 0;
+    ctx->vertices_host.clear();
+    ctx->bounds_override = false;
+    ctx->initialized = false;
+    return FACETCU_OK;
+}
+
+int facetcu_get_stream(facetcu_context* ctx, void** stream)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "getStream()");
+        if (!stream) throw Error(FACETCU_INVALID_ARGUMENT, "stream is null");
+        *stream = ctx->stream;
+        return FACETCU_OK;
+    });
+}
+
+// FacetrtVulkan::setGeometry + validateGeometry (facetrt_vulkan.cpp:425-471)
+int facetcu_set_geometry(facetcu_context* ctx, const facetcu_vertex* vertices,
+                         uint64_t vertex_count)
+{
+    return guarded(ctx, [&] {
+        if (!ctx->initialized)
+            throw Error(FACETCU_LOGIC_ERROR, "initialize() must be called before setGeometry()");
+        FCU_CHECK(cudaSetDevice(ctx->device));
+        if (!vertices || vertex_count == 0 || vertex_count % 3 != 0)
+            throw Error(FACETCU_INVALID_ARGUMENT, "Geometry must be a non-empty triangle list");
+        if (vertex_count / 3 > (1ull << 30))
+            throw Error(FACETCU_OVERFLOW_ERROR, "Geometry exceeds 2^30 facets");
+        for (uint64_t i = 0; i < vertex_count; ++i) {
+            const facetcu_vertex& v = vertices[i];
+            for (float c : v.position)
+                if (!std::isfinite(c))
+                    throw Error(FACETCU_INVALID_ARGUMENT, "Geometry contains a non-finite position");
+            const float len = std::sqrt(v.normal[0] * v.normal[0] + v.normal[1] * v.normal[1] +
+                                        v.normal[2] * v.normal[2]);
+            if (!(len > 0.99f && len < 1.01f))
+                throw Error(FACETCU_INVALID_ARGUMENT, "Facet normals must be normalized");
+        }
+        FCU_CHECK(cudaStreamSynchronize(ctx->stream));
+        ctx->graph_ready = false;
+        ctx->graph.packed_valid = false;
+        ctx->facets = uint32_t(vertex_count / 3);
+        ctx->vertices_host.assign(vertices, vertices + vertex_count);
+        for (int a = 0; a < 3; ++a) {
+            ctx->bmin[a] = std::numeric_limits<float>::max();
+            ctx->bmax[a] = std::numeric_limits<float>::lowest();
+        }
+        for (uint64_t i = 0; i < vertex_count; ++i)
+            for (int a = 0; a < 3; ++a) {
+                ctx->bmin[a] = std::min(ctx->bmin[a], vertices[i].position[a]);
+                ctx->bmax[a] = std::max(ctx->bmax[a], vertices[i].position[a]);
+            }
+        upload(ctx->vertices, vertices, vertex_count * sizeof(facetcu_vertex), ctx->stream);
+        FCU_CHECK(cudaStreamSynchronize(ctx->stream));
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_set_raster_bounds(facetcu_context* ctx, const float minimum[3], const float maximum[3])
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "setRasterBounds()");
+        if (!minimum || !maximum) {
+            ctx->bounds_override = false;
+            return FACETCU_OK;
+        }
+        for (int a = 0; a < 3; ++a) {
+            if (!std::isfinite(minimum[a]) || !std::isfinite(maximum[a]) || maximum[a] < minimum[a])
+                throw Error(FACETCU_INVALID_ARGUMENT, "Raster bounds must be finite and ordered");
+            ctx->omin[a] = minimum[a];
+            ctx->omax[a] = maximum[a];
+        }
+        ctx->bounds_override = true;
+        return FACETCU_OK;
+    });
+}
+
+// FacetrtVulkan::buildVisibilityGraph (facetrt_vulkan.cpp:866-1062)
+int facetcu_build_visibility_graph(facetcu_context* ctx, const facetcu_direction* directions,
+                                   uint32_t direction_count,
+                                   facetcu_graph_diagnostics* diagnostics)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "buildVisibilityGraph()");
+        if (ctx->facets == 0)
+            throw Error(FACETCU_LOGIC_ERROR, "setGeometry() must be called before buildVisibilityGraph()");
+        if (!directions || direction_count == 0)
+            throw Error(FACETCU_INVALID_ARGUMENT, "At least one visibility direction is required");
+        ctx->graph_ready = false;
+        const uint32_t S = ctx->facets * 2u;
+        const int side_bits = side_bits_for(S);
+        std::vector<RasterView> views(direction_count);
+        for (uint32_t d = 0; d < direction_count; ++d) views[d] = make_view(directions[d]);
+        const RasterFrame frame = make_frame(ctx);
+        if (uint64_t(frame.tiles) * ctx->facets >= (1ull << 31))
+            throw Error(FACETCU_OVERFLOW_ERROR, "facets x periodic tiles exceeds 2^31");
+        cudaStream_t s = ctx->stream;
+        DeviceGraph& g = ctx->graph;
+        g.surfaces = S;
+        uint32_t* denom = static_cast<uint32_t*>(g.denominators.reserve(size_t(S) * 4));
+        uint32_t* sky = static_cast<uint32_t*>(g.sky.reserve(size_t(S) * 4));
+        FCU_CHECK(cudaMemsetAsync(denom, 0, size_t(S) * 4, s));
+        FCU_CHECK(cudaMemsetAsync(sky, 0, size_t(S) * 4, s));
+        unsigned long long* pair_count =
+            static_cast<unsigned long long*>(ctx->pair_count.reserve(16));
+        FCU_CHECK(cudaMemsetAsync(pair_count, 0, 8, s));
+        // directions per chunk: keep the per-pixel count/offset arrays near 1 GiB
+        const uint64_t pixels = uint64_t(frame.width) * frame.height;
+        uint32_t chunk = uint32_t(std::max<uint64_t>(1, (1ull << 30) / (8 * pixels)));
+        chunk = std::min<uint32_t>(std::min<uint32_t>(chunk, 64u), direction_count);
+        uint64_t overflow = 0, pairs_used = 0, pairs_cap = ctx->pairs.bytes / 8;
+        uint32_t capacity_error = 0, max_chain = 0;
+        for (uint32_t d0 = 0; d0 < direction_count; d0 += chunk) {
+            const uint32_t n = std::min(chunk, direction_count - d0);
+            RasterStats st{};
+            raster_fragments(ctx->vertices.as<facetcu_vertex>(), frame, views.data() + d0, n,
+                             ctx->raster, ctx->ws, st, s);
+            // pairs of this chunk are at most the fragments of it
+            const uint64_t need = pairs_used + st.fragments + 1;
+            if (need > pairs_cap) {
+                DeviceBuffer grown;
+                grown.reserve(std::max<uint64_t>(need, pairs_cap * 2) * 8);
+                if (pairs_used)
+                    FCU_CHECK(cudaMemcpyAsync(grown.ptr, ctx->pairs.ptr, pairs_used * 8,
+                                              cudaMemcpyDeviceToDevice, s));
+                FCU_CHECK(cudaStreamSynchronize(s));
+                std::swap(ctx->pairs.ptr, grown.ptr);
+                std::swap(ctx->pairs.bytes, grown.bytes);
+                pairs_cap = ctx->pairs.bytes / 8;
+            }
+            raster_resolve_graph(frame, n, chain_cap(ctx), ctx->raster, denom, sky,
+                                 ctx->pairs.as<uint64_t>(), pair_count, side_bits, st, s);
+            unsigned long long used = 0;
+            FCU_CHECK(cudaMemcpyAsync(&used, pair_count, 8, cudaMemcpyDeviceToHost, s));
+            FCU_CHECK(cudaStreamSynchronize(s));
+            pairs_used = used;
+            overflow += st.overflow;
+            capacity_error += st.capacity_error;
+            max_chain = std::max(max_chain, st.max_chain);
+        }
+        facetcu_graph_diagnostics diag{};
+        diag.facet_count = ctx->facets;
+        diag.surface_count = S;
+        diag.fragment_overflow = uint32_t(std::min<uint64_t>(overflow, 0xffffffffu));
+        diag.hash_overflow = 0;
+        if (diagnostics) *diagnostics = diag;
+        if (overflow)
+            throw Error(FACETCU_RUNTIME_ERROR,
+                        "Visibility A-buffer overflow; increase Config::maxFragmentsPerPixel");
+        if (capacity_error)
+            throw Error(FACETCU_DEVICE_CAPACITY, "a pixel chain exceeded the 1024-fragment device capacity");
+        graph_from_pairs(ctx->pairs.as<uint64_t>(), pairs_used, side_bits, g, ctx->ws, s);
+        float closure = 0.0f;
+        uint32_t sampled = 0;
+        graph_closure(g, &closure, &sampled, ctx->ws, s);
+        diag.directed_edge_count = uint32_t(g.nnz);
+        diag.max_closure_error = closure;
+        if (diagnostics) *diagnostics = diag;
+        if (sampled == 0)
+            throw Error(FACETCU_RUNTIME_ERROR,
+                        "Visibility raster has no surface samples; radiation results are invalid");
+        graph_pack(g, ctx->ws, s);
+        FCU_CHECK(cudaStreamSynchronize(s));
+        ctx->graph_ready = true;
+        return FACETCU_OK;
+    });
+}
+
+// FacetrtVulkan::computeSunlitFraction (facetrt_vulkan.cpp:1064-1158)
+int facetcu_compute_sunlit_fraction(facetcu_context* ctx, const facetcu_direction* sun,
+                                    float* fraction)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "computeSunlitFraction()");
+        if (ctx->facets == 0)
+            throw Error(FACETCU_LOGIC_ERROR, "setGeometry() must be called before computeSunlitFraction()");
+        if (!sun || !fraction) throw Error(FACETCU_INVALID_ARGUMENT, "sun direction and output are required");
+        const uint32_t S = ctx->facets * 2u;
+        const RasterView view = make_view(*sun);
+        const RasterFrame frame = make_frame(ctx);
+        cudaStream_t s = ctx->stream;
+        RasterStats st{};
+        raster_fragments(ctx->vertices.as<facetcu_vertex>(), frame, &view, 1, ctx->raster, ctx->ws,
+                         st, s);
+        uint32_t* total = static_cast<uint32_t*>(ctx->sun_total.reserve(size_t(S) * 4));
+        uint32_t* visible = static_cast<uint32_t*>(ctx->sun_visible.reserve(size_t(S) * 4));
+        FCU_CHECK(cudaMemsetAsync(total, 0, size_t(S) * 4, s));
+        FCU_CHECK(cudaMemsetAsync(visible, 0, size_t(S) * 4, s));
+        raster_resolve_sunlit(frame, chain_cap(ctx), ctx->raster, total, visible, st, s);
+        if (st.overflow)
+            throw Error(FACETCU_RUNTIME_ERROR,
+                        "Direct-light A-buffer overflow; increase Config::maxFragmentsPerPixel");
+        std::vector<uint32_t> t(S), v(S);
+        FCU_CHECK(cudaMemcpyAsync(t.data(), total, size_t(S) * 4, cudaMemcpyDeviceToHost, s));
+        FCU_CHECK(cudaMemcpyAsync(v.data(), visible, size_t(S) * 4, cudaMemcpyDeviceToHost, s));
+        FCU_CHECK(cudaStreamSynchronize(s));
+        for (uint32_t i = 0; i < S; ++i)
+            fraction[i] = t[i] ? float(v[i]) / float(t[i]) : 0.0f;
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_graph_size(facetcu_context* ctx, uint32_t* surface_count, uint64_t* edges)
+{
+    return guarded(ctx, [&] {
+        require_graph(ctx, "graphSize()");
+        if (surface_count) *surface_count = ctx->graph.surfaces;
+        if (edges) *edges = ctx->graph.nnz;
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_get_graph(facetcu_context* ctx, uint32_t* row_offsets, facetcu_csr_edge* edges,
+                      uint32_t* denominators, uint32_t* sky_counts)
+{
+    return guarded(ctx, [&] {
+        require_graph(ctx, "getGraph()");
+        const DeviceGraph& g = ctx->graph;
+        cudaStream_t s = ctx->stream;
+        if (row_offsets)
+            FCU_CHECK(cudaMemcpyAsync(row_offsets, g.row_offsets.ptr, (size_t(g.surfaces) + 1) * 4,
+                                      cudaMemcpyDeviceToHost, s));
+        if (edges && g.nnz)
+            FCU_CHECK(cudaMemcpyAsync(edges, g.edges.ptr, g.nnz * 8, cudaMemcpyDeviceToHost, s));
+        if (denominators)
+            FCU_CHECK(cudaMemcpyAsync(denominators, g.denominators.ptr, size_t(g.surfaces) * 4,
+                                      cudaMemcpyDeviceToHost, s));
+        if (sky_counts)
+            FCU_CHECK(cudaMemcpyAsync(sky_counts, g.sky.ptr, size_t(g.surfaces) * 4,
+                                      cudaMemcpyDeviceToHost, s));
+        FCU_CHECK(cudaStreamSynchronize(s));
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_set_graph(facetcu_context* ctx, uint32_t surface_count, const uint32_t* row_offsets,
+                      const facetcu_csr_edge* edges, const uint32_t* denominators,
+                      const uint32_t* sky_counts)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "setGraph()");
+        if (ctx->facets == 0)
+            throw Error(FACETCU_LOGIC_ERROR, "setGeometry() must be called before setGraph()");
+        if (surface_count != ctx->facets * 2u || !row_offsets || !denominators || !sky_counts)
+            throw Error(FACETCU_INVALID_ARGUMENT, "graph must have two rows per facet");
+        if (row_offsets[0] != 0)
+            throw Error(FACETCU_INVALID_ARGUMENT, "row offsets must start at 0");
+        for (uint32_t i = 0; i < surface_count; ++i)
+            if (row_offsets[i + 1] < row_offsets[i])
+                throw Error(FACETCU_INVALID_ARGUMENT, "row offsets must be non-decreasing");
+        const uint64_t nnz = row_offsets[surface_count];
+        if (nnz && !edges) throw Error(FACETCU_INVALID_ARGUMENT, "edges are required");
+        for (uint64_t e = 0; e < nnz; ++e)
+            if (edges[e].neighbor >= surface_count)
+                throw Error(FACETCU_INVALID_ARGUMENT, "graph contains an invalid surface index");
+        DeviceGraph& g = ctx->graph;
+        cudaStream_t s = ctx->stream;
+        g.surfaces = surface_count;
+        g.nnz = nnz;
+        upload(g.row_offsets, row_offsets, (size_t(surface_count) + 1) * 4, s);
+        upload(g.edges, edges, nnz * 8 + 8, s);
+        upload(g.denominators, denominators, size_t(surface_count) * 4, s);
+        upload(g.sky, sky_counts, size_t(surface_count) * 4, s);
+        g.packed_valid = false;
+        float closure;
+        uint32_t sampled;
+        graph_closure(g, &closure, &sampled, ctx->ws, s);
+        graph_pack(g, ctx->ws, s);
+        FCU_CHECK(cudaStreamSynchronize(s));
+        ctx->graph_ready = true;
+        return FACETCU_OK;
+    });
+}
+
+// FacetrtVulkan::solve (facetrt_vulkan.cpp:1177-1247)
+int facetcu_solve(facetcu_context* ctx, const facetcu_surface_optics* optics, float sky,
+                  uint32_t iterations, float relaxation, float* radiosity,
+                  uint32_t* iterations_done, float* max_delta)
+{
+    return guarded(ctx, [&] {
+        require_graph(ctx, "solve()");
+        const uint32_t S = ctx->graph.surfaces;
+        validate_optics(optics, S);
+        validate_sky(sky);
+        validate_relax(relaxation);
+        cudaStream_t s = ctx->stream;
+        upload(ctx->optics, optics, size_t(S) * 16, s);
+        ctx->rad_a.reserve(size_t(S) * 4);
+        ctx->rad_b.reserve(size_t(S) * 4);
+        ctx->residual.reserve((size_t(iterations) + 1) * 4);
+        FCU_CHECK(cudaMemsetAsync(ctx->rad_a.ptr, 0, size_t(S) * 4, s));
+        FCU_CHECK(cudaMemsetAsync(ctx->rad_b.ptr, 0, size_t(S) * 4, s));
+        FCU_CHECK(cudaMemsetAsync(ctx->residual.ptr, 0, (size_t(iterations) + 1) * 4, s));
+        const uint32_t ping = run_sweeps(ctx, sky, relaxation, iterations, 0, 0);
+        const float* final_buf = ping == 0 ? ctx->rad_a.as<float>() : ctx->rad_b.as<float>();
+        uint32_t bits = 0;
+        if (radiosity)
+            FCU_CHECK(cudaMemcpyAsync(radiosity, final_buf, size_t(S) * 4, cudaMemcpyDeviceToHost, s));
+        if (iterations)
+            FCU_CHECK(cudaMemcpyAsync(&bits, ctx->residual.as<uint32_t>() + iterations - 1, 4,
+                                      cudaMemcpyDeviceToHost, s));
+        FCU_CHECK(cudaStreamSynchronize(s));
+        if (iterations_done) *iterations_done = iterations;
+        if (max_delta) std::memcpy(max_delta, &bits, 4);
+        return FACETCU_OK;
+    });
+}
+
+// FacetrtVulkan::solveAccelerated (facetrt_vulkan.cpp:1249-1358)
+int facetcu_solve_accelerated(facetcu_context* ctx, const facetcu_surface_optics* optics,
+                              float sky, const float* initial, uint32_t maximum_iterations,
+                              uint32_t batch_iterations, float tolerance, float relaxation,
+                              float* radiosity, uint32_t* iterations_done, float* max_delta)
+{
+    return guarded(ctx, [&] {
+        require_graph(ctx, "solveAccelerated()");
+        const uint32_t S = ctx->graph.surfaces;
+        validate_optics(optics, S);
+        validate_sky(sky);
+        validate_relax(relaxation);
+        if (maximum_iterations == 0 || batch_iterations == 0 || !std::isfinite(tolerance) ||
+            tolerance < 0.0f)
+            throw Error(FACETCU_INVALID_ARGUMENT,
+                        "Accelerated solve iterations must be positive and tolerance non-negative");
+        if (initial) {
+            for (uint32_t i = 0; i < S; ++i)
+                if (!std::isfinite(initial[i]) || initial[i] < 0.0f)
+                    throw Error(FACETCU_INVALID_ARGUMENT,
+                                "Initial radiosity must contain one finite non-negative value per surface");
+        }
+        cudaStream_t s = ctx->stream;
+        upload(ctx->optics, optics, size_t(S) * 16, s);
+        ctx->rad_a.reserve(size_t(S) * 4);
+        ctx->rad_b.reserve(size_t(S) * 4);
+        ctx->residual.reserve((size_t(maximum_iterations) + 1) * 4);
+        FCU_CHECK(cudaMemsetAsync(ctx->residual.ptr, 0, (size_t(maximum_iterations) + 1) * 4, s));
+        if (initial) {
+            FCU_CHECK(cudaMemcpyAsync(ctx->rad_a.ptr, initial, size_t(S) * 4, cudaMemcpyHostToDevice, s));
+            FCU_CHECK(cudaMemcpyAsync(ctx->rad_b.ptr, initial, size_t(S) * 4, cudaMemcpyHostToDevice, s));
+        } else {
+            FCU_CHECK(cudaMemsetAsync(ctx->rad_a.ptr, 0, size_t(S) * 4, s));
+            FCU_CHECK(cudaMemsetAsync(ctx->rad_b.ptr, 0, size_t(S) * 4, s));
+        }
+        uint32_t done = 0, ping = 0;
+        float md = 0.0f;
+        while (done < maximum_iterations) {
+            const uint32_t count = std::min(batch_iterations, maximum_iterations - done);
+            ping = run_sweeps(ctx, sky, relaxation, count, ping, done);
+            done += count;
+            uint32_t bits = 0;
+            FCU_CHECK(cudaMemcpyAsync(&bits, ctx->residual.as<uint32_t>() + done - 1, 4,
+                                      cudaMemcpyDeviceToHost, s));
+            FCU_CHECK(cudaStreamSynchronize(s));
+            std::memcpy(&md, &bits, 4);
+            if (md <= tolerance) break;
+        }
+        const float* final_buf = ping == 0 ? ctx->rad_a.as<float>() : ctx->rad_b.as<float>();
+        if (radiosity)
+            FCU_CHECK(cudaMemcpyAsync(radiosity, final_buf, size_t(S) * 4, cudaMemcpyDeviceToHost, s));
+        FCU_CHECK(cudaStreamSynchronize(s));
+        if (iterations_done) *iterations_done = done;
+        if (max_delta) *max_delta = md;
+        return FACETCU_OK;
+    });
+}
+
+// FacetrtVulkan::incidentIrradiance (facetrt_vulkan.cpp:1360-1399)
+int facetcu_incident_irradiance(facetcu_context* ctx, const float* radiosity,
+                                const facetcu_surface_optics* optics, float sky, float* irradiance)
+{
+    return guarded(ctx, [&] {
+        if (!ctx->initialized || !ctx->graph_ready || !radiosity || !optics)
+            throw Error(FACETCU_INVALID_ARGUMENT,
+                        "Incident irradiance requires a completed solve and visibility graph");
+        FCU_CHECK(cudaSetDevice(ctx->device));
+        if (!std::isfinite(sky) || sky < 0.0f)
+            throw Error(FACETCU_INVALID_ARGUMENT, "Sky radiosity must be finite and non-negative");
+        const uint32_t S = ctx->graph.surfaces;
+        cudaStream_t s = ctx->stream;
+        upload(ctx->optics, optics, size_t(S) * 16, s);
+        float* rad = static_cast<float*>(ctx->scratch.reserve(size_t(S) * 8));
+        FCU_CHECK(cudaMemcpyAsync(rad, radiosity, size_t(S) * 4, cudaMemcpyHostToDevice, s));
+        incident_irradiance(ctx->graph, ctx->optics.as<facetcu_surface_optics>(), sky, rad, rad + S, s);
+        FCU_CHECK(cudaMemcpyAsync(irradiance, rad + S, size_t(S) * 4, cudaMemcpyDeviceToHost, s));
+        FCU_CHECK(cudaStreamSynchronize(s));
+        return FACETCU_OK;
+    });
+}
+
+}  // extern "C"
+
+namespace {
+
+void validate_batch(const facetcu_batch_config* cfg)
+{
+    if (!cfg) throw Error(FACETCU_INVALID_ARGUMENT, "batch config is null");
+    if (cfg->band_count == 0 || cfg->sun_count == 0)
+        throw Error(FACETCU_INVALID_ARGUMENT, "band_count and sun_count must be positive");
+    if (cfg->precision > 2u) throw Error(FACETCU_INVALID_ARGUMENT, "unknown precision");
+    if (cfg->warm_start > FACETCU_WARM_GIVEN) throw Error(FACETCU_INVALID_ARGUMENT, "unknown warm start");
+    if (!std::isfinite(cfg->tolerance) || cfg->tolerance < 0.0f)
+        throw Error(FACETCU_INVALID_ARGUMENT, "tolerance must be finite and non-negative");
+    if (uint64_t(cfg->band_count) * cfg->sun_count > (1ull << 31))
+        throw Error(FACETCU_OVERFLOW_ERROR, "band_count x sun_count exceeds 2^31");
+}
+
+int run_batched(facetcu_context* ctx, const facetcu_batch_config* cfg, const float* rho,
+                const float* tau, const float* emis, const float* sky, const float* beam,
+                const float* dgeo, const float* initial, float* out, facetcu_batch_result* result)
+{
+    BatchProblem p{};
+    p.S = ctx->graph.surfaces;
+    p.bands = cfg->band_count;
+    p.suns = cfg->sun_count;
+    p.rho = rho;
+    p.tau = tau;
+    p.emis = emis;
+    p.sky = sky;
+    p.beam = beam;
+    p.dgeo = dgeo;
+    cudaEvent_t e0, e1;
+    FCU_CHECK(cudaEventCreate(&e0));
+    FCU_CHECK(cudaEventCreate(&e1));
+    FCU_CHECK(cudaEventRecord(e0, ctx->stream));
+    const int rc = batched_solve(ctx->graph, p, *cfg, initial, out, ctx->batch, ctx->ws, ctx->stream,
+                                 result);
+    FCU_CHECK(cudaEventRecord(e1, ctx->stream));
+    FCU_CHECK(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (result) result->seconds = double(ms) * 1e-3;
+    if (rc == FACETCU_NOT_CONVERGED) {
+        ctx->last_error = "batched solve reached maximum_iterations before the tolerance";
+    }
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int facetcu_solve_batched_device(facetcu_context* ctx, const facetcu_batch_config* cfg,
+                                 const float* reflectance, const float* transmittance,
+                                 const float* emission, const float* sky, const float* beam,
+                                 const float* direct_geometry, const float* initial,
+                                 float* radiosity, facetcu_batch_result* result)
+{
+    return guarded(ctx, [&] {
+        require_graph(ctx, "solveBatched()");
+        validate_batch(cfg);
+        if (!reflectance || !transmittance || !sky || !beam || !radiosity)
+            throw Error(FACETCU_INVALID_ARGUMENT, "reflectance, transmittance, sky, beam and output are required");
+        if (cfg->warm_start == FACETCU_WARM_GIVEN && !initial)
+            throw Error(FACETCU_INVALID_ARGUMENT, "warm_start = GIVEN needs an initial radiosity");
+        return run_batched(ctx, cfg, reflectance, transmittance, emission, sky, beam,
+                           direct_geometry, initial, radiosity, result);
+    });
+}
+
+int facetcu_solve_batched(facetcu_context* ctx, const facetcu_batch_config* cfg,
+                          const float* reflectance, const float* transmittance,
+                          const float* emission, const float* sky, const float* beam,
+                          const float* direct_geometry, const float* initial, float* radiosity,
+                          facetcu_batch_result* result)
+{
+    return guarded(ctx, [&] {
+        require_graph(ctx, "solveBatched()");
+        validate_batch(cfg);
+        if (!reflectance || !transmittance || !sky || !beam || !radiosity)
+            throw Error(FACETCU_INVALID_ARGUMENT, "reflectance, transmittance, sky, beam and output are required");
+        if (cfg->warm_start == FACETCU_WARM_GIVEN && !initial)
+            throw Error(FACETCU_INVALID_ARGUMENT, "warm_start = GIVEN needs an initial radiosity");
+        const size_t S = ctx->graph.surfaces, B = cfg->band_count, K = cfg->sun_count;
+        const size_t R = B * K;
+        for (size_t i = 0; i < B * S; ++i) {
+            const float r = reflectance[i], t = transmittance[i];
+            const float e = emission ? emission[i] : 0.0f;
+            if (!std::isfinite(r) || !std::isfinite(t) || !std::isfinite(e) || r < 0.0f ||
+                t < 0.0f || e < 0.0f || r + t > 1.0001f)
+                throw Error(FACETCU_INVALID_ARGUMENT,
+                            "Optical values must be finite, non-negative, and reflectance+transmittance<=1");
+        }
+        for (size_t b = 0; b < B; ++b) {
+            validate_sky(sky[b]);
+            if (!std::isfinite(beam[b]) || beam[b] < 0.0f)
+                throw Error(FACETCU_INVALID_ARGUMENT, "beam irradiance must be finite and non-negative");
+        }
+        // one device block for all inputs: rho, tau, emis, dgeo, sky, beam, initial, out
+        const size_t n_bs = B * S, n_ks = direct_geometry ? K * S : 0, n_rs = R * S;
+        const size_t init_n = cfg->warm_start == FACETCU_WARM_GIVEN ? n_rs : 0;
+        const size_t total = 3 * n_bs + n_ks + 2 * B + init_n + n_rs + 64;
+        float* base = static_cast<float*>(ctx->batch_inputs.reserve(total * 4));
+        float* d_rho = base;
+        float* d_tau = d_rho + n_bs;
+        float* d_emis = d_tau + n_bs;
+        float* d_dgeo = d_emis + n_bs;
+        float* d_sky = d_dgeo + n_ks;
+        float* d_beam = d_sky + B;
+        float* d_init = d_beam + B;
+        float* d_out = d_init + init_n;
+        cudaStream_t s = ctx->stream;
+        FCU_CHECK(cudaMemcpyAsync(d_rho, reflectance, n_bs * 4, cudaMemcpyHostToDevice, s));
+        FCU_CHECK(cudaMemcpyAsync(d_tau, transmittance, n_bs * 4, cudaMemcpyHostToDevice, s));
+        if (emission) FCU_CHECK(cudaMemcpyAsync(d_emis, emission, n_bs * 4, cudaMemcpyHostToDevice, s));
+        if (n_ks) FCU_CHECK(cudaMemcpyAsync(d_dgeo, direct_geometry, n_ks * 4, cudaMemcpyHostToDevice, s));
+        FCU_CHECK(cudaMemcpyAsync(d_sky, sky, B * 4, cudaMemcpyHostToDevice, s));
+        FCU_CHECK(cudaMemcpyAsync(d_beam, beam, B * 4, cudaMemcpyHostToDevice, s));
+        if (init_n) FCU_CHECK(cudaMemcpyAsync(d_init, initial, init_n * 4, cudaMemcpyHostToDevice, s));
+        const int rc = run_batched(ctx, cfg, d_rho, d_tau, emission ? d_emis : nullptr, d_sky, d_beam,
+                                   n_ks ? d_dgeo : nullptr, init_n ? d_init : nullptr, d_out, result);
+        FCU_CHECK(cudaMemcpyAsync(radiosity, d_out, n_rs * 4, cudaMemcpyDeviceToHost, s));
+        FCU_CHECK(cudaStreamSynchronize(s));
+        return rc;
+    });
+}
+
+}  // extern "C"

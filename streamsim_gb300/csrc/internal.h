@@ -1,0 +1,204 @@
+// internal.h — shared declarations of the facetcu library (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/facetcu.h"
+
+namespace facetcu {
+
+// Error carrying one of the FACETCU_* status codes.
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void cuda_check(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return;
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        throw Error(FACETCU_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+    throw Error(FACETCU_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define FCU_CHECK(x) ::facetcu::cuda_check((x), #x)
+#define FCU_LAUNCH(what) ::facetcu::cuda_check(cudaGetLastError(), what)
+
+// Owning device buffer that only grows.
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    ~DeviceBuffer() { release(); }
+    void release()
+    {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    void* reserve(size_t n)
+    {
+        if (n <= bytes && ptr) return ptr;
+        release();
+        if (n == 0) n = 16;
+        cuda_check(cudaMalloc(&ptr, n), "cudaMalloc");
+        bytes = n;
+        return ptr;
+    }
+    template <typename T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+// Per-direction orthographic frame of the CPU rasterizer
+// (facetrtcore.cpp:1244-1282): right/up/view basis, centre and radius.
+struct RasterView {
+    float right[3];
+    float up[3];
+    float view[3];
+};
+
+struct RasterFrame {
+    float center[3];
+    float radius;
+    uint32_t width, height;
+    uint32_t facets;
+    uint32_t tiles;        // 1 + periodic neighbours (<= 21)
+    float tile_dx[21];
+    float tile_dz[21];
+};
+
+// Scratch used by the device sort and scan.
+struct Workspace {
+    DeviceBuffer a, b, c, d, e;
+};
+
+// ---- device utilities (sort.cu) ----------------------------------------
+// Exclusive scan of n uint32 values; out may alias in.  Returns nothing;
+// *total_dev (optional) receives the 64-bit sum on the device.
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n,
+                        unsigned long long* total_dev, Workspace& ws, cudaStream_t s);
+// LSD radix sort of 64-bit keys on bits [0, key_bits), with optional 32-bit
+// values; stable.  Result ends in keys/values (the buffers are swapped with
+// the alternates as needed).
+void radix_sort_u64(uint64_t*& keys, uint64_t*& keys_alt, uint32_t*& values,
+                    uint32_t*& values_alt, size_t n, int key_bits, Workspace& ws,
+                    cudaStream_t s);
+
+// ---- raster visibility (raster.cu) --------------------------------------
+struct RasterBuffers {
+    DeviceBuffer counts;    // dirs * pixels
+    DeviceBuffer offsets;   // dirs * pixels + 1
+    DeviceBuffer records;   // fragments (u64: depth bits << 32 | key)
+    DeviceBuffer big_list;  // large-triangle work items
+    DeviceBuffer deep_list; // pixels with more than the fast-path chain
+    DeviceBuffer stats;     // small counters
+};
+
+struct RasterStats {
+    unsigned long long fragments;
+    unsigned long long overflow;   // sum over pixels of max(0, count - cap)
+    unsigned long long pairs;
+    unsigned int big;
+    unsigned int deep;
+    unsigned int capacity_error;
+    unsigned int max_chain;
+};
+
+// Rasterise `dir_count` directions (views[0..dir_count)) into exact-size
+// per-pixel fragment lists.  Leaves counts/offsets/records filled.
+void raster_fragments(const facetcu_vertex* d_vertices, const RasterFrame& frame,
+                      const RasterView* views, uint32_t dir_count, RasterBuffers& rb,
+                      Workspace& ws, RasterStats& stats, cudaStream_t s);
+// Resolve the lists of a chunk into denominators, sky counts and pair keys
+// (lo << side_bits | hi), appended at pairs[pair_count..].
+// chain_cap = the reference's maxFragmentsPerPixel: longer chains count as
+// fragment overflow (UINT32_MAX = no limit).
+void raster_resolve_graph(const RasterFrame& frame, uint32_t dir_count, uint32_t chain_cap,
+                          RasterBuffers& rb, uint32_t* d_denominators, uint32_t* d_sky,
+                          uint64_t* d_pairs, unsigned long long* d_pair_count, int side_bits,
+                          RasterStats& stats, cudaStream_t s);
+// Resolve one direction's lists into sunlit total/visible counts.
+void raster_resolve_sunlit(const RasterFrame& frame, uint32_t chain_cap, RasterBuffers& rb,
+                           uint32_t* d_total, uint32_t* d_visible, RasterStats& stats,
+                           cudaStream_t s);
+
+// ---- graph assembly (graph.cu) ------------------------------------------
+struct DeviceGraph {
+    uint32_t surfaces = 0;
+    uint64_t nnz = 0;
+    DeviceBuffer row_offsets;   // S + 1 (u32)
+    DeviceBuffer edges;         // nnz * {neighbor, count}
+    DeviceBuffer denominators;  // S
+    DeviceBuffer sky;           // S
+    DeviceBuffer packed;        // nnz u32: neighbor | count << 22 (batched solver)
+    bool packed_valid = false;
+    uint32_t max_count = 0;
+};
+// Sort undirected pair keys, count runs, emit the symmetric CSR.
+void graph_from_pairs(uint64_t* d_pairs, size_t pair_count, int side_bits, DeviceGraph& g,
+                      Workspace& ws, cudaStream_t s);
+// max |(sky + sum counts) / denom - 1| over sides with denom > 0, and the
+// number of sides with denom > 0.
+void graph_closure(const DeviceGraph& g, float* closure, uint32_t* sampled, Workspace& ws,
+                   cudaStream_t s);
+// Build the 4-byte packed edge array (neighbor in 22 bits, count in 10 bits)
+// when the graph fits it.
+bool graph_pack(DeviceGraph& g, Workspace& ws, cudaStream_t s);
+
+// ---- solves (solve.cu) ---------------------------------------------------
+void jacobi_plain_sweep(const DeviceGraph& g, const facetcu_surface_optics* d_optics,
+                        float sky, float relaxation, const float* d_in, float* d_out,
+                        uint32_t* d_max_delta_bits, cudaStream_t s);
+void incident_irradiance(const DeviceGraph& g, const facetcu_surface_optics* d_optics,
+                         float sky, const float* d_radiosity, float* d_out, cudaStream_t s);
+
+// ---- batched solver (batched.cu) ---------------------------------------
+struct BatchProblem {
+    uint32_t S;            // sides
+    uint32_t bands, suns;  // R = bands * suns
+    const float* rho;      // bands * S
+    const float* tau;      // bands * S
+    const float* emis;     // bands * S or null
+    const float* sky;      // bands
+    const float* beam;     // bands
+    const float* dgeo;     // suns * S or null
+};
+struct BatchState {
+    DeviceBuffer x0, x1;        // panels, side-major [S][P]
+    DeviceBuffer half;          // BF16 copy for mixed precision
+    DeviceBuffer colstats;      // per-column max|dB|, max|B| bits
+    DeviceBuffer q;             // source term per panel
+    DeviceBuffer corr;          // residual / correction panel
+};
+int batched_solve(const DeviceGraph& g, const BatchProblem& p, const facetcu_batch_config& cfg,
+                  const float* d_initial, float* d_out, BatchState& st, Workspace& ws,
+                  cudaStream_t s, facetcu_batch_result* result);
+
+// ---- hemisphere ray casting (lbvh.cu, hemi.cu) ----------------------------
+struct Lbvh {
+    uint32_t leaves = 0;
+    DeviceBuffer nodes;      // internal nodes: 2 children (u32, leaf bit 31) + aabb
+    DeviceBuffer tri;        // per sorted leaf: a, e1, e2 (9 floats) + facet id
+    DeviceBuffer parent;     // build scratch
+    DeviceBuffer flags;      // build scratch
+    float scene_min[3], scene_max[3];
+};
+void lbvh_build(const facetcu_vertex* d_vertices, uint32_t facets, Lbvh& bvh, Workspace& ws,
+                cudaStream_t s);
+void hemisphere_graph(const facetcu_vertex* d_vertices, uint32_t facets, const Lbvh& bvh,
+                      const float* d_uv, const float* d_dir, uint32_t rays, uint32_t sets,
+                      uint32_t top_k, DeviceGraph& g, unsigned long long* dropped,
+                      Workspace& ws, cudaStream_t s);
+void hemisphere_sunlit(const facetcu_vertex* d_vertices, uint32_t facets, const Lbvh& bvh,
+                       const float* d_uv, uint32_t samples, uint32_t sets, float3 sun,
+                       float* d_fraction, cudaStream_t s);
+
+}  // namespace facetcu

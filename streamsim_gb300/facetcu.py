@@ -1,0 +1,394 @@
+"""ctypes binding of libfacetcu.so (include/facetcu.h) and a host-side class
+with the method names of the reference's facetvk::FacetrtVulkan
+(models/histream/src/facetrt/facetrt_vulkan.h:70-104).
+
+Errors come back as the reference's exception types: FACETCU_INVALID_ARGUMENT
+-> ValueError (std::invalid_argument), FACETCU_LOGIC_ERROR -> LogicError
+(std::logic_error), FACETCU_RUNTIME_ERROR -> RuntimeError, FACETCU_OVERFLOW_ERROR
+-> OverflowError, anything else -> FacetcuError.  There is no CPU fallback:
+if the library is missing, load() raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfacetcu.so")
+
+OK = 0
+INVALID_ARGUMENT = 1
+LOGIC_ERROR = 2
+RUNTIME_ERROR = 3
+OVERFLOW_ERROR = 4
+CUDA_ERROR = 5
+NO_DEVICE = 6
+OUT_OF_MEMORY = 7
+DEVICE_CAPACITY = 8
+NOT_CONVERGED = 9
+
+PRECISION_FP32 = 0
+PRECISION_MIXED = 1
+PRECISION_FP64 = 2
+WARM_NONE = 0
+WARM_GIVEN = 1
+
+
+class FacetcuError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class LogicError(FacetcuError):
+    pass
+
+
+class NotConverged(FacetcuError):
+    pass
+
+
+class Vertex(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("normal", C.c_float * 3)]
+
+
+class Direction(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float)]
+
+
+class SurfaceOptics(C.Structure):
+    _fields_ = [("reflectance", C.c_float), ("transmittance", C.c_float),
+                ("emission", C.c_float), ("direct_irradiance", C.c_float)]
+
+
+class Config(C.Structure):
+    _fields_ = [("raster_width", C.c_uint32), ("raster_height", C.c_uint32),
+                ("max_fragments_per_pixel", C.c_uint32), ("edge_hash_capacity", C.c_uint32),
+                ("enable_validation", C.c_bool), ("gpu_index", C.c_uint32),
+                ("periodic_neighbor_count", C.c_uint32), ("periodic_size_x", C.c_float),
+                ("periodic_size_z", C.c_float)]
+
+
+class GraphDiagnostics(C.Structure):
+    _fields_ = [("facet_count", C.c_uint32), ("surface_count", C.c_uint32),
+                ("directed_edge_count", C.c_uint32), ("fragment_overflow", C.c_uint32),
+                ("hash_overflow", C.c_uint32), ("max_closure_error", C.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class HemisphereConfig(C.Structure):
+    _fields_ = [("rays_per_side", C.c_uint32), ("top_k", C.c_uint32),
+                ("sample_sets", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("band_count", C.c_uint32), ("sun_count", C.c_uint32),
+                ("precision", C.c_uint32), ("warm_start", C.c_uint32),
+                ("maximum_iterations", C.c_uint32), ("tolerance", C.c_float),
+                ("panel_width", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("residual_corrections", C.c_uint32),
+                ("converged", C.c_uint32), ("max_relative_change", C.c_float),
+                ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_vp = C.c_void_p
+_u32 = C.c_uint32
+_ctx = C.c_void_p
+
+# name -> (restype, argtypes) for every symbol of include/facetcu.h
+SIGNATURES = {
+    "facetcu_create": (C.c_int, [C.POINTER(_vp)]),
+    "facetcu_release": (None, [_ctx]),
+    "facetcu_last_error": (C.c_char_p, [_ctx]),
+    "facetcu_device_count": (C.c_int, [C.POINTER(C.c_int)]),
+    "facetcu_initialize": (C.c_int, [_ctx, C.POINTER(Config)]),
+    "facetcu_destroy": (C.c_int, [_ctx]),
+    "facetcu_get_stream": (C.c_int, [_ctx, C.POINTER(_vp)]),
+    "facetcu_set_geometry": (C.c_int, [_ctx, _vp, C.c_uint64]),
+    "facetcu_set_raster_bounds": (C.c_int, [_ctx, _vp, _vp]),
+    "facetcu_build_visibility_graph": (C.c_int, [_ctx, _vp, _u32, C.POINTER(GraphDiagnostics)]),
+    "facetcu_compute_sunlit_fraction": (C.c_int, [_ctx, C.POINTER(Direction), _vp]),
+    "facetcu_graph_size": (C.c_int, [_ctx, C.POINTER(_u32), C.POINTER(C.c_uint64)]),
+    "facetcu_get_graph": (C.c_int, [_ctx, _vp, _vp, _vp, _vp]),
+    "facetcu_set_graph": (C.c_int, [_ctx, _u32, _vp, _vp, _vp, _vp]),
+    "facetcu_solve": (C.c_int, [_ctx, _vp, C.c_float, _u32, C.c_float, _vp, C.POINTER(_u32),
+                                C.POINTER(C.c_float)]),
+    "facetcu_solve_accelerated": (C.c_int, [_ctx, _vp, C.c_float, _vp, _u32, _u32, C.c_float,
+                                            C.c_float, _vp, C.POINTER(_u32), C.POINTER(C.c_float)]),
+    "facetcu_incident_irradiance": (C.c_int, [_ctx, _vp, _vp, C.c_float, _vp]),
+    "facetcu_solve_batched": (C.c_int, [_ctx, C.POINTER(BatchConfig)] + [_vp] * 8 +
+                              [C.POINTER(BatchResult)]),
+    "facetcu_solve_batched_device": (C.c_int, [_ctx, C.POINTER(BatchConfig)] + [_vp] * 8 +
+                                     [C.POINTER(BatchResult)]),
+}
+OPTIONAL_SIGNATURES = {
+    "facetcu_build_hemisphere_graph": (C.c_int, [_ctx, C.POINTER(HemisphereConfig), _vp, _vp,
+                                                 C.POINTER(GraphDiagnostics),
+                                                 C.POINTER(C.c_uint64)]),
+    "facetcu_hemisphere_sunlit": (C.c_int, [_ctx, C.POINTER(Direction), _u32, _u32, _vp, _vp]),
+}
+
+_LIB = None
+
+
+def load(path=LIB_PATH):
+    """Load libfacetcu.so; raises if it has not been built (no fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise FacetcuError(NO_DEVICE, f"libfacetcu.so not built at {path}; run "
+                                      "`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(path)
+    for name, (res, args) in {**SIGNATURES, **OPTIONAL_SIGNATURES}.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def header_symbols(header=None):
+    """Function names declared in include/facetcu.h."""
+    import re
+    header = header or os.path.join(HERE, "..", "include", "facetcu.h")
+    text = open(header).read()
+    return sorted(set(re.findall(r"\b(facetcu_[a-z0-9_]+)\s*\(", text)))
+
+
+def device_count():
+    lib = load()
+    n = C.c_int(0)
+    lib.facetcu_device_count(C.byref(n))
+    return n.value
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class FacetrtCuda:
+    """Host object with the interface of facetvk::FacetrtVulkan.
+
+    Vertices are an (n, 6) float32 array [px, py, pz, nx, ny, nz] (or
+    (F, 3, 6)); optics an (S, 4) float32 array [rho, tau, emission, direct].
+    """
+
+    def __init__(self):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.facetcu_create(C.byref(h))
+        if rc != OK:
+            raise FacetcuError(rc, "facetcu_create failed")
+        self.h = h
+        self.diagnostics = None
+
+    def close(self):
+        if self.h:
+            self.lib.facetcu_release(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        if rc == OK:
+            return
+        msg = (self.lib.facetcu_last_error(self.h) or b"").decode()
+        if rc == INVALID_ARGUMENT:
+            raise ValueError(msg)
+        if rc == LOGIC_ERROR:
+            raise LogicError(rc, msg)
+        if rc == RUNTIME_ERROR:
+            raise RuntimeError(msg)
+        if rc == OVERFLOW_ERROR:
+            raise OverflowError(msg)
+        if rc == NOT_CONVERGED:
+            raise NotConverged(rc, msg)
+        raise FacetcuError(rc, msg)
+
+    # -- facetvk::FacetrtVulkan -------------------------------------------
+    def initialize(self, raster_width=1024, raster_height=None, max_fragments_per_pixel=64,
+                   gpu_index=0, periodic_neighbor_count=0, periodic_size_x=1.0,
+                   periodic_size_z=1.0):
+        cfg = Config()
+        cfg.raster_width = raster_width
+        cfg.raster_height = raster_height if raster_height is not None else raster_width
+        cfg.max_fragments_per_pixel = max_fragments_per_pixel
+        cfg.edge_hash_capacity = 0
+        cfg.enable_validation = False
+        cfg.gpu_index = gpu_index
+        cfg.periodic_neighbor_count = periodic_neighbor_count
+        cfg.periodic_size_x = periodic_size_x
+        cfg.periodic_size_z = periodic_size_z
+        self._check(self.lib.facetcu_initialize(self.h, C.byref(cfg)))
+        return self
+
+    def destroy(self):
+        self._check(self.lib.facetcu_destroy(self.h))
+
+    def stream(self):
+        s = C.c_void_p()
+        self._check(self.lib.facetcu_get_stream(self.h, C.byref(s)))
+        return s.value
+
+    def setGeometry(self, vertices):
+        v = _f32(vertices).reshape(-1, 6)
+        self.facet_count = len(v) // 3
+        self._check(self.lib.facetcu_set_geometry(self.h, _ptr(v), len(v)))
+
+    def setRasterBounds(self, minimum, maximum):
+        mn = _f32(minimum, (3,))
+        mx = _f32(maximum, (3,))
+        self._check(self.lib.facetcu_set_raster_bounds(self.h, _ptr(mn), _ptr(mx)))
+
+    def buildVisibilityGraph(self, directions):
+        d = _f32(directions).reshape(-1, 3)
+        diag = GraphDiagnostics()
+        rc = self.lib.facetcu_build_visibility_graph(self.h, _ptr(d), len(d), C.byref(diag))
+        self.diagnostics = diag.as_dict()
+        self._check(rc)
+        return self.diagnostics
+
+    def computeSunlitFraction(self, sun):
+        sun = _f32(sun, (3,))
+        out = np.zeros(2 * self.facet_count, np.float32)
+        d = Direction(*[float(x) for x in sun])
+        self._check(self.lib.facetcu_compute_sunlit_fraction(self.h, C.byref(d), _ptr(out)))
+        return out
+
+    def buildHemisphereGraph(self, sample_uv, sample_dir, rays_per_side, top_k, sample_sets):
+        cfg = HemisphereConfig(rays_per_side, top_k, sample_sets, 0)
+        uv = _f32(sample_uv)
+        dr = _f32(sample_dir)
+        diag = GraphDiagnostics()
+        dropped = C.c_uint64()
+        rc = self.lib.facetcu_build_hemisphere_graph(self.h, C.byref(cfg), _ptr(uv), _ptr(dr),
+                                                     C.byref(diag), C.byref(dropped))
+        self.diagnostics = diag.as_dict()
+        self._check(rc)
+        return self.diagnostics, dropped.value
+
+    def hemisphereSunlit(self, sun, sample_uv, samples, sample_sets):
+        sun = _f32(sun, (3,))
+        uv = _f32(sample_uv)
+        out = np.zeros(2 * self.facet_count, np.float32)
+        d = Direction(*[float(x) for x in sun])
+        self._check(self.lib.facetcu_hemisphere_sunlit(self.h, C.byref(d), samples, sample_sets,
+                                                       _ptr(uv), _ptr(out)))
+        return out
+
+    def graph(self):
+        """(row_offsets, neighbors, counts, denominators, sky_counts) as numpy arrays."""
+        S = C.c_uint32()
+        n = C.c_uint64()
+        self._check(self.lib.facetcu_graph_size(self.h, C.byref(S), C.byref(n)))
+        rows = np.zeros(S.value + 1, np.uint32)
+        edges = np.zeros(2 * max(n.value, 1), np.uint32)
+        den = np.zeros(S.value, np.uint32)
+        sky = np.zeros(S.value, np.uint32)
+        self._check(self.lib.facetcu_get_graph(self.h, _ptr(rows), _ptr(edges), _ptr(den), _ptr(sky)))
+        e = edges[:2 * n.value]
+        return rows, e[0::2].copy(), e[1::2].copy(), den, sky
+
+    def setGraph(self, row_offsets, neighbors, counts, denominators, sky_counts):
+        rows = np.ascontiguousarray(row_offsets, np.uint32)
+        e = np.empty(2 * max(len(neighbors), 1), np.uint32)
+        e[0:2 * len(neighbors):2] = neighbors
+        e[1:2 * len(neighbors):2] = counts
+        den = np.ascontiguousarray(denominators, np.uint32)
+        sky = np.ascontiguousarray(sky_counts, np.uint32)
+        self._check(self.lib.facetcu_set_graph(self.h, len(den), _ptr(rows), _ptr(e), _ptr(den),
+                                               _ptr(sky)))
+
+    def solve(self, optics, sky_radiosity, iterations=64, relaxation=1.0):
+        o = _f32(optics).reshape(-1, 4)
+        out = np.zeros(len(o), np.float32)
+        it = C.c_uint32()
+        md = C.c_float()
+        self._check(self.lib.facetcu_solve(self.h, _ptr(o), sky_radiosity, iterations, relaxation,
+                                           _ptr(out), C.byref(it), C.byref(md)))
+        return {"radiosity": out, "iterations": it.value, "maxDelta": md.value}
+
+    def solveAccelerated(self, optics, sky_radiosity, initial=None, maximum_iterations=64,
+                         batch_iterations=8, tolerance=1.0e-4, relaxation=1.0):
+        o = _f32(optics).reshape(-1, 4)
+        init = None if initial is None else _f32(initial)
+        out = np.zeros(len(o), np.float32)
+        it = C.c_uint32()
+        md = C.c_float()
+        self._check(self.lib.facetcu_solve_accelerated(
+            self.h, _ptr(o), sky_radiosity, _ptr(init), maximum_iterations, batch_iterations,
+            tolerance, relaxation, _ptr(out), C.byref(it), C.byref(md)))
+        return {"radiosity": out, "iterations": it.value, "maxDelta": md.value}
+
+    def incidentIrradiance(self, radiosity, optics, sky_radiosity):
+        o = _f32(optics).reshape(-1, 4)
+        r = _f32(radiosity)
+        out = np.zeros(len(o), np.float32)
+        self._check(self.lib.facetcu_incident_irradiance(self.h, _ptr(r), _ptr(o), sky_radiosity,
+                                                         _ptr(out)))
+        return out
+
+    # -- batched extension ------------------------------------------------
+    def solveBatched(self, reflectance, transmittance, sky, beam, direct_geometry=None,
+                     emission=None, precision=PRECISION_FP32, tolerance=1e-6,
+                     maximum_iterations=1000, initial=None, panel_width=0, raise_on_nonconvergence=True):
+        """reflectance/transmittance/emission: (bands, S); sky, beam: (bands,);
+        direct_geometry: (suns, S).  Returns radiosity (suns*bands, S) and the result dict."""
+        rho = _f32(reflectance)
+        tau = _f32(transmittance)
+        bands = rho.shape[0]
+        S = rho.shape[1]
+        emis = None if emission is None else _f32(emission)
+        dgeo = None if direct_geometry is None else _f32(direct_geometry).reshape(-1, S)
+        suns = 1 if dgeo is None else dgeo.shape[0]
+        cfg = BatchConfig(bands, suns, precision, WARM_GIVEN if initial is not None else WARM_NONE,
+                          maximum_iterations, tolerance, panel_width, 0)
+        init = None if initial is None else _f32(initial)
+        out = np.zeros((suns * bands, S), np.float32)
+        res = BatchResult()
+        rc = self.lib.facetcu_solve_batched(self.h, C.byref(cfg), _ptr(rho), _ptr(tau), _ptr(emis),
+                                            _ptr(_f32(sky)), _ptr(_f32(beam)), _ptr(dgeo),
+                                            _ptr(init), _ptr(out), C.byref(res))
+        if rc == NOT_CONVERGED and not raise_on_nonconvergence:
+            return out, res.as_dict()
+        self._check(rc)
+        return out, res.as_dict()
+
+    def solveBatchedDevice(self, cfg, rho_ptr, tau_ptr, emis_ptr, sky_ptr, beam_ptr, dgeo_ptr,
+                           init_ptr, out_ptr):
+        """Device-pointer variant; all pointers are integers (or None)."""
+        res = BatchResult()
+        rc = self.lib.facetcu_solve_batched_device(
+            self.h, C.byref(cfg), rho_ptr, tau_ptr, emis_ptr, sky_ptr, beam_ptr, dgeo_ptr,
+            init_ptr, out_ptr, C.byref(res))
+        if rc not in (OK, NOT_CONVERGED):
+            self._check(rc)
+        return res.as_dict()

@@ -1,0 +1,263 @@
+"""Synthetic FacetRT scenes, band optics and hemisphere sample tables.
+
+Every scene is seeded (numpy default_rng) and Y-up like the reference
+(facetrtcore.cpp:485-486, :496).  Vertex arrays are (3F, 6) float32
+[px, py, pz, nx, ny, nz] with the three vertices of a facet consecutive and
+sharing the unit normal normalize((b-a) x (c-a)) (appendTriangle,
+facetrtcore.cpp:287-306).  Object facets come first, ground facets last
+(facetrtcore.cpp:2998-3004), and `leaf_count` is the number of object facets.
+
+Named workloads:
+  config1  10 x 10 m soil (32 x 32 quads = 2,048 triangles) + 2,048 leaf
+           triangles (edge 0.05 m, centres in [-5,5]^2 x [0.2,1.5], normals on
+           the upper hemisphere): 4,096 facets.
+  config2  60 trees (64-triangle trunk cylinder r = 0.15 m, h ~ U(4,8); crown
+           sphere r ~ U(1.5,3) of 3,000 leaves, edge 0.08 m, normals on the
+           sphere) on a 50 x 50 m soil of 20,000 triangles: 203,840 facets.
+  config3  the same forest with 150 trees on 80 x 80 m: 479,600 facets.
+"""
+import math
+
+import numpy as np
+
+
+class Scene:
+    def __init__(self, vertices, leaf_count, name, trunk_count=0):
+        self.vertices = np.ascontiguousarray(vertices, np.float32)
+        self.leaf_count = int(leaf_count)
+        self.trunk_count = int(trunk_count)
+        self.name = name
+
+    @property
+    def facet_count(self):
+        return len(self.vertices) // 3
+
+    @property
+    def surface_count(self):
+        return 2 * self.facet_count
+
+    def bounds(self):
+        p = self.vertices[:, :3]
+        return p.min(0), p.max(0)
+
+    def normals(self):
+        return self.vertices[0::3, 3:6]
+
+
+def _triangles_to_vertices(a, b, c):
+    """(F,3) corner arrays -> (3F,6) vertex array with facet normals."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    c = np.asarray(c, np.float64)
+    n = np.cross(b - a, c - a)
+    ln = np.linalg.norm(n, axis=1, keepdims=True)
+    keep = ln[:, 0] > 1e-12
+    n = n[keep] / ln[keep]
+    F = int(keep.sum())
+    v = np.empty((F, 3, 6), np.float64)
+    v[:, 0, :3] = a[keep]
+    v[:, 1, :3] = b[keep]
+    v[:, 2, :3] = c[keep]
+    v[:, :, 3:] = n[:, None, :]
+    return v.reshape(-1, 6).astype(np.float32)
+
+
+def _orthonormal(n):
+    helper = np.where(np.abs(n[:, 1:2]) < 0.9, [[0.0, 1.0, 0.0]], [[1.0, 0.0, 0.0]])
+    t = np.cross(helper, n)
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    b = np.cross(n, t)
+    return t, b
+
+
+def equilateral(centres, normals, edge, rng):
+    """Equilateral triangles (counter-clockwise around `normals`)."""
+    centres = np.asarray(centres, np.float64)
+    normals = np.asarray(normals, np.float64)
+    normals = normals / np.linalg.norm(normals, axis=1, keepdims=True)
+    t, b = _orthonormal(normals)
+    theta = rng.uniform(0, 2 * np.pi, len(centres))[:, None]
+    R = edge / math.sqrt(3.0)
+    corners = []
+    for k in range(3):
+        ang = theta + 2 * np.pi * k / 3
+        corners.append(centres + R * (np.cos(ang) * t + np.sin(ang) * b))
+    return corners
+
+
+def uniform_sphere(n, rng):
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def soil_grid(x0, x1, z0, z1, nx, nz, y=0.0):
+    xs = np.linspace(x0, x1, nx + 1)
+    zs = np.linspace(z0, z1, nz + 1)
+    X0, Z0 = np.meshgrid(xs[:-1], zs[:-1], indexing="ij")
+    X1, Z1 = np.meshgrid(xs[1:], zs[1:], indexing="ij")
+    X0, Z0, X1, Z1 = (q.ravel() for q in (X0, Z0, X1, Z1))
+    Y = np.full_like(X0, y)
+    a = np.stack([X0, Y, Z0], 1)
+    b1 = np.stack([X0, Y, Z1], 1)
+    c1 = np.stack([X1, Y, Z1], 1)
+    d1 = np.stack([X1, Y, Z0], 1)
+    # both triangles face +Y: (a, b1, c1) and (a, c1, d1)
+    A = np.concatenate([a, a])
+    B = np.concatenate([b1, c1])
+    C = np.concatenate([c1, d1])
+    return A, B, C
+
+
+def cylinder(base, radius, height, segments=32):
+    ang = np.linspace(0, 2 * np.pi, segments + 1)[:-1]
+    ang2 = np.roll(ang, -1)
+    p0 = np.stack([np.cos(ang), np.zeros_like(ang), np.sin(ang)], 1) * radius
+    p1 = np.stack([np.cos(ang2), np.zeros_like(ang2), np.sin(ang2)], 1) * radius
+    up = np.array([0.0, height, 0.0])
+    base = np.asarray(base, np.float64)
+    # outward normals: (p0, p0+up, p1) and (p1, p0+up, p1+up)
+    A = np.concatenate([base + p0, base + p1])
+    B = np.concatenate([base + p0 + up, base + p0 + up])
+    C = np.concatenate([base + p1, base + p1 + up])
+    return A, B, C
+
+
+def config1(seed=0, leaves=2048, grid=32):
+    rng = np.random.default_rng(seed)
+    centres = np.stack([rng.uniform(-5, 5, leaves), rng.uniform(0.2, 1.5, leaves),
+                        rng.uniform(-5, 5, leaves)], 1)
+    n = uniform_sphere(leaves, rng)
+    n[:, 1] = np.abs(n[:, 1])
+    leaf = _triangles_to_vertices(*equilateral(centres, n, 0.05, rng))
+    soil = _triangles_to_vertices(*soil_grid(-5, 5, -5, 5, grid, grid))
+    return Scene(np.concatenate([leaf, soil]), len(leaf) // 3, f"config1(seed={seed})")
+
+
+def forest(trees, extent, soil_quads, seed=0, leaves_per_crown=3000, leaf_edge=0.08,
+           name="forest"):
+    rng = np.random.default_rng(seed)
+    half = extent / 2.0
+    parts = []
+    trunk_parts = []
+    for _ in range(trees):
+        x, z = rng.uniform(-half + 3, half - 3, 2)
+        h = rng.uniform(4.0, 8.0)
+        r = rng.uniform(1.5, 3.0)
+        trunk_parts.append(_triangles_to_vertices(*cylinder((x, 0.0, z), 0.15, h)))
+        # uniform points in the crown sphere
+        d = uniform_sphere(leaves_per_crown, rng)
+        rad = r * rng.uniform(0, 1, leaves_per_crown) ** (1.0 / 3.0)
+        centres = np.array([x, h, z]) + d * rad[:, None]
+        centres[:, 1] = np.maximum(centres[:, 1], 0.3)
+        normals = uniform_sphere(leaves_per_crown, rng)
+        parts.append(_triangles_to_vertices(*equilateral(centres, normals, leaf_edge, rng)))
+    leaves = np.concatenate(parts)
+    trunks = np.concatenate(trunk_parts)
+    nq = int(round(math.sqrt(soil_quads)))
+    soil = _triangles_to_vertices(*soil_grid(-half, half, -half, half, nq, nq))
+    verts = np.concatenate([leaves, trunks, soil])
+    obj = (len(leaves) + len(trunks)) // 3
+    return Scene(verts, obj, name, trunk_count=len(trunks) // 3)
+
+
+def config2(seed=0):
+    return forest(60, 50.0, 10000, seed, name=f"config2(seed={seed})")
+
+
+def config3(seed=0):
+    return forest(150, 80.0, 10000, seed, name=f"config3(seed={seed})")
+
+
+# ---- directions and optics ------------------------------------------------
+def sun_direction(zenith_deg, azimuth_deg):
+    """facetrtcore.cpp:491-498 in float32 arithmetic order."""
+    pi = np.float32(3.14159265358979323846)
+    zen = np.float32(zenith_deg) * pi / np.float32(180.0)
+    az = np.float32(azimuth_deg) * pi / np.float32(180.0)
+    return np.array([np.sin(zen) * np.cos(az), np.cos(zen), np.sin(zen) * np.sin(az)], np.float32)
+
+
+def hemisphere_directions(count=40):
+    """facetrtcore.cpp:475-489 (golden-spiral upper hemisphere)."""
+    golden = np.float32(2.39996322972865332)
+    out = np.zeros((count, 3), np.float32)
+    for i in range(count):
+        y = (np.float32(i) + np.float32(0.5)) / np.float32(count)
+        r = np.sqrt(max(np.float32(0.0), np.float32(1.0) - y * y), dtype=np.float32)
+        az = golden * np.float32(i)
+        out[i] = [r * np.cos(az), y, r * np.sin(az)]
+    return out
+
+
+def direct_geometry(scene, sunlit, sun):
+    """sunlit_s * max(0, n_s . sun) per side (the D of makeOptics without the beam)."""
+    n = scene.normals().astype(np.float32)
+    c = n @ np.asarray(sun, np.float32)
+    cos = np.empty(2 * len(n), np.float32)
+    cos[0::2] = np.maximum(c, 0)
+    cos[1::2] = np.maximum(-c, 0)
+    return (np.asarray(sunlit, np.float32) * cos).astype(np.float32)
+
+
+def band_optics(scene, bands=64, leaf=(0.04, 0.48), soil=(0.12, 0.30), leaf_tau_ratio=0.4):
+    """Per-band reflectance/transmittance (bands, S): leaf rho ramps leaf[0] ->
+    leaf[1] with tau = leaf_tau_ratio * rho, soil rho soil[0] -> soil[1] and
+    tau = 0; trunk facets take the leaf reflectance with tau = 0.  Both sides
+    of a facet share its material."""
+    F = scene.facet_count
+    t = np.linspace(0.0, 1.0, bands, dtype=np.float64) if bands > 1 else np.zeros(1)
+    lr = leaf[0] + (leaf[1] - leaf[0]) * t
+    sr = soil[0] + (soil[1] - soil[0]) * t
+    nleaf = scene.leaf_count - scene.trunk_count
+    rho_f = np.empty((bands, F))
+    tau_f = np.zeros((bands, F))
+    rho_f[:, :nleaf] = lr[:, None]
+    tau_f[:, :nleaf] = (leaf_tau_ratio * lr)[:, None]
+    rho_f[:, nleaf:scene.leaf_count] = lr[:, None]
+    rho_f[:, scene.leaf_count:] = sr[:, None]
+    rho = np.repeat(rho_f, 2, axis=1).astype(np.float32)
+    tau = np.repeat(tau_f, 2, axis=1).astype(np.float32)
+    return rho, tau
+
+
+def reference_optics(scene, sunlit, sun, beam=700.0, leaf_rho=0.10, leaf_tau=0.05,
+                     ground_rho=0.20, ground_tau=0.0):
+    """makeOptics (facetrtcore.cpp:500-522) with its constants as arguments."""
+    F = scene.facet_count
+    o = np.zeros((2 * F, 4), np.float32)
+    leaf = np.arange(F) < scene.leaf_count
+    o[:, 0] = np.repeat(np.where(leaf, leaf_rho, ground_rho), 2)
+    o[:, 1] = np.repeat(np.where(leaf, leaf_tau, ground_tau), 2)
+    o[:, 3] = direct_geometry(scene, sunlit, sun) * np.float32(beam)
+    return o
+
+
+def hemisphere_samples(rays, sets=32, seed=1234):
+    """Per-set sample tables for the hemisphere ray caster.
+
+    uv: (sets, rays, 2) barycentric weights of vertices b and c (origin =
+    a + u (b - a) + v (c - a)), strictly inside the triangle;
+    dirs: (sets, rays, 3) cosine-distributed unit directions in the side's
+    local frame (z along the side normal).  Stratified: a rotated
+    golden-ratio lattice per set (Cranley-Patterson shift), mapped with
+    Malley's method; computed in float64 and stored as float32."""
+    rng = np.random.default_rng(seed)
+    j = np.arange(rays, dtype=np.float64)
+    phi = (math.sqrt(5.0) - 1.0) / 2.0
+    uv = np.empty((sets, rays, 2), np.float32)
+    dirs = np.empty((sets, rays, 3), np.float32)
+    for p in range(sets):
+        s1, s2, s3, s4 = rng.uniform(0, 1, 4)
+        u1 = np.mod((j + 0.5) / rays + s1, 1.0)
+        u2 = np.mod(j * phi + s2, 1.0)
+        r = np.sqrt(u1)
+        a = 2 * np.pi * u2
+        d = np.stack([r * np.cos(a), r * np.sin(a), np.sqrt(np.maximum(1.0 - u1, 0.0))], 1)
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        dirs[p] = d
+        w1 = 0.02 + 0.96 * np.mod(j * phi + s3, 1.0)
+        w2 = 0.02 + 0.96 * np.mod((j + 0.5) / rays + s4, 1.0)
+        su = np.sqrt(w1)
+        uv[p, :, 0] = su * (1.0 - w2)
+        uv[p, :, 1] = su * w2
+    return uv, dirs

@@ -1,0 +1,160 @@
+"""Solves on the GPU through the C ABI against the CPU oracle.
+
+Tolerances (floating point):
+  * facetcu_solve / _accelerated (FP32 gather, reference radiosity.comp) vs
+    the reference CPU solve (FP64 gather): max relative error 1e-5;
+  * incident irradiance (FP64 gather on both sides): 1e-6;
+  * batched FP64 vs the oracle's FP64 Jacobi: 1e-9;
+  * batched FP32 and MIXED (BF16 defect + FP32 residual correction) vs FP64
+    truth of the same graph: 1e-4 (the bar of the headline metric).
+"""
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Graph
+from streamsim_gb300 import facetcu, scenes
+from tests.gpu_helpers import model_for, oracle_cfg, rel_err, require_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    require_gpu()
+
+
+@pytest.fixture(scope="module")
+def c1(oracle):
+    sc = scenes.config1(seed=0)
+    m = model_for(sc.vertices, 512, 64)
+    m.buildVisibilityGraph(scenes.hemisphere_directions())
+    sun = scenes.sun_direction(30, 135)
+    lit = m.computeSunlitFraction(sun)
+    g = Graph(*m.graph())
+    yield dict(scene=sc, model=m, sun=sun, lit=lit, graph=g)
+    m.close()
+
+
+def test_solve_matches_reference_cpu_solver(oracle, c1):
+    optics = scenes.reference_optics(c1["scene"], c1["lit"], c1["sun"])
+    r = c1["model"].solve(optics, 100.0, 64, 1.0)
+    b_ref, md_ref = oracle.solve(c1["graph"], optics, 100.0, 64)
+    assert r["iterations"] == 64
+    assert rel_err(r["radiosity"], b_ref) < 1e-5
+    assert r["maxDelta"] <= 1e-3
+    # diffuse-only baseline and light enhancement (facetrtcore.cpp:1561-1583)
+    diffuse = optics.copy()
+    diffuse[:, 3] = 0
+    r0 = c1["model"].solve(diffuse, 100.0)
+    b0, _ = oracle.solve(c1["graph"], diffuse, 100.0, 64)
+    enh = np.maximum(0, r["radiosity"] - r0["radiosity"])
+    enh_ref = np.maximum(0, b_ref - b0)
+    assert np.max(np.abs(enh - enh_ref)) < 1e-5 * np.max(b_ref)
+
+
+def test_solve_relaxation_and_validation(oracle, c1):
+    optics = scenes.reference_optics(c1["scene"], c1["lit"], c1["sun"])
+    r = c1["model"].solve(optics, 100.0, 200, 0.5)
+    b_ref, _ = oracle.solve(c1["graph"], optics, 100.0, 200, 0.5)
+    assert rel_err(r["radiosity"], b_ref) < 1e-5
+    bad = optics.copy()
+    bad[5, 0] = 0.9
+    bad[5, 1] = 0.2
+    with pytest.raises(ValueError, match="reflectance\\+transmittance"):
+        c1["model"].solve(bad, 100.0)
+    with pytest.raises(ValueError, match="relaxation"):
+        c1["model"].solve(optics, 100.0, 8, 0.0)
+    with pytest.raises(ValueError, match="skyRadiosity"):
+        c1["model"].solve(optics, -1.0)
+    with pytest.raises(ValueError):
+        c1["model"].solve(optics[:-2], 100.0)
+
+
+def test_solve_accelerated_semantics(oracle, c1):
+    optics = scenes.reference_optics(c1["scene"], c1["lit"], c1["sun"])
+    r = c1["model"].solveAccelerated(optics, 100.0, None, 64, 8, 1e-4, 1.0)
+    assert r["iterations"] % 8 == 0 and r["iterations"] < 64
+    assert r["maxDelta"] <= 1e-4
+    b_ref, _ = oracle.solve(c1["graph"], optics, 100.0, r["iterations"])
+    assert rel_err(r["radiosity"], b_ref) < 1e-5
+    # warm start from the converged answer stops after the first batch
+    w = c1["model"].solveAccelerated(optics, 100.0, r["radiosity"], 64, 8, 1e-4, 1.0)
+    assert w["iterations"] == 8
+    with pytest.raises(ValueError, match="Initial radiosity"):
+        bad = r["radiosity"].copy()
+        bad[0] = -1
+        c1["model"].solveAccelerated(optics, 100.0, bad)
+
+
+def test_incident_irradiance(oracle, c1):
+    optics = scenes.reference_optics(c1["scene"], c1["lit"], c1["sun"])
+    b, _ = oracle.solve(c1["graph"], optics, 100.0, 64)
+    h = c1["model"].incidentIrradiance(b, optics, 100.0)
+    h_ref = oracle.incident(c1["graph"], b, optics, 100.0)
+    assert rel_err(h, h_ref) < 1e-6
+
+
+def _bands(sc, lit, sun, bands):
+    rho, tau = scenes.band_optics(sc, bands)
+    dgeo = scenes.direct_geometry(sc, lit, sun)[None, :]
+    sky = np.full(bands, 100.0, np.float32)
+    beam = np.full(bands, 800.0, np.float32)
+    return rho, tau, dgeo, sky, beam
+
+
+def test_batched_fp64_matches_oracle_fp64(oracle, c1):
+    sc = c1["scene"]
+    rho, tau, dgeo, sky, beam = _bands(sc, c1["lit"], c1["sun"], 2)
+    out, res = c1["model"].solveBatched(rho, tau, sky, beam, dgeo,
+                                        precision=facetcu.PRECISION_FP64, tolerance=1e-13)
+    assert res["converged"] == 1
+    for b in range(2):
+        optics = np.zeros((sc.surface_count, 4), np.float32)
+        optics[:, 0] = rho[b]
+        optics[:, 1] = tau[b]
+        optics[:, 3] = dgeo[0] * beam[b]
+        truth, _ = oracle.solve_f64(c1["graph"], optics, float(sky[b]), 2000, 1e-14)
+        assert rel_err(out[b], truth) < 1e-6  # output rounded to float32
+
+
+@pytest.mark.parametrize("precision", [facetcu.PRECISION_FP32, facetcu.PRECISION_MIXED])
+@pytest.mark.parametrize("bands,suns", [(2, 1), (64, 1), (5, 3)])
+def test_batched_meets_1e4_vs_fp64(c1, precision, bands, suns):
+    sc = c1["scene"]
+    rho, tau, _, sky, beam = _bands(sc, c1["lit"], c1["sun"], bands)
+    sky = np.linspace(50, 150, bands).astype(np.float32)
+    dgeo = np.stack([scenes.direct_geometry(sc, c1["lit"], scenes.sun_direction(z, 135))
+                     for z in np.linspace(10, 60, suns)])
+    truth, rt = c1["model"].solveBatched(rho, tau, sky, beam, dgeo,
+                                         precision=facetcu.PRECISION_FP64, tolerance=1e-12)
+    out, res = c1["model"].solveBatched(rho, tau, sky, beam, dgeo, precision=precision,
+                                        tolerance=1e-6)
+    assert res["converged"] == 1
+    assert out.shape == (bands * suns, sc.surface_count)
+    assert rel_err(out, truth) < 1e-4
+    if precision == facetcu.PRECISION_MIXED:
+        assert res["residual_corrections"] >= 1
+
+
+def test_batched_column_layout_matches_single_solves(c1):
+    """Column r = sun * bands + band equals the single-RHS solve of that band/sun."""
+    sc = c1["scene"]
+    bands, suns = 3, 2
+    rho, tau, _, sky, beam = _bands(sc, c1["lit"], c1["sun"], bands)
+    dgeo = np.stack([scenes.direct_geometry(sc, c1["lit"], scenes.sun_direction(z, 90))
+                     for z in (20, 50)])
+    out, _ = c1["model"].solveBatched(rho, tau, sky, beam, dgeo, tolerance=1e-7)
+    for k in range(suns):
+        for b in range(bands):
+            single, _ = c1["model"].solveBatched(rho[b:b + 1], tau[b:b + 1], sky[b:b + 1],
+                                                 beam[b:b + 1], dgeo[k:k + 1], tolerance=1e-7)
+            assert rel_err(out[k * bands + b], single[0]) < 1e-5
+
+
+def test_batched_warm_start_given(c1):
+    sc = c1["scene"]
+    rho, tau, dgeo, sky, beam = _bands(sc, c1["lit"], c1["sun"], 4)
+    out, res = c1["model"].solveBatched(rho, tau, sky, beam, dgeo, tolerance=1e-6)
+    out2, res2 = c1["model"].solveBatched(rho, tau, sky, beam, dgeo, tolerance=1e-6, initial=out)
+    assert res2["iterations"] < res["iterations"] / 3
+    assert rel_err(out2, out) < 1e-5

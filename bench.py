@@ -1,0 +1,429 @@
+#!/usr/bin/env python3
+"""FacetRT batched radiosity benchmark on one GB300 (or N replicas).
+
+Metric: facet·band·sun radiosity solves/s at <= 1e-4 max relative error
+against an FP64 solve of the same discrete system.
+
+Workload (the configuration the metric is quoted on): the 60-tree forest on
+a 50 x 50 m soil of 20,000 triangles (203,840 facets, 407,680 sides), 64
+bands (leaf rho 0.04 -> 0.48, tau = 0.4 rho; soil 0.12 -> 0.30), one sun at
+zenith 30 deg / azimuth 135 deg, direct 800 W m-2 and sky 100 W m-2 per band.
+The view-factor graph is built once before timing (hemisphere ray casting,
+512 rays per facet side, top-K 256 when available, else the reference's
+40-direction global-line raster); a step is one complete 64-band solve from
+optics to converged radiosity (max relative change < 1e-6, the config-1 stop
+rule), with every input already resident in HBM.  L2 is flushed (a 512 MB
+write) between timed steps.
+
+`--impl reference` times the reference's own CPU Jacobi (solveCpu,
+facetrtcore.cpp:1476-1529; oracle/_ref when it was compiled, else the C
+restatement in oracle/) on the same graph and optics on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "facet·band·sun radiosity solves/s at ≤1e-4 rel err: learned+BF16 vs plain FP32"
+UNIT = "facet·band·sun solves/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    p.add_argument("--precision", default="mixed", choices=["fp32", "mixed"])
+    p.add_argument("--view-factors", default="auto", choices=["auto", "raster", "hemisphere"])
+    p.add_argument("--bands", type=int, default=64)
+    p.add_argument("--tolerance", type=float, default=1e-6)
+    p.add_argument("--rays", type=int, default=512)
+    p.add_argument("--top-k", type=int, default=256)
+    p.add_argument("--raster", type=int, default=1024)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--quick", action="store_true", help="config-1 scene, for smoke timing")
+    return p.parse_args()
+
+
+# ---- distributed plumbing (replicas only: no data-path collective) ---------
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, world, local
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---- clocks ------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---- workload ---------------------------------------------------------------
+def build_workload(args, fc, scenes, oracle_mod=None):
+    sc = scenes.config1(seed=0) if args.quick else scenes.config2(seed=0)
+    m = fc.FacetrtCuda()
+    m.initialize(args.raster, args.raster, 1024)
+    m.setGeometry(sc.vertices)
+    sun = scenes.sun_direction(30.0, 135.0)
+    mode = args.view_factors
+    has_hemi = hasattr(m.lib, "facetcu_build_hemisphere_graph")
+    if mode == "auto":
+        mode = "hemisphere" if has_hemi else "raster"
+    t0 = time.perf_counter()
+    if mode == "hemisphere":
+        uv, dirs = scenes.hemisphere_samples(args.rays, 32, seed=7)
+        diag, dropped = m.buildHemisphereGraph(uv, dirs, args.rays, args.top_k, 32)
+        lit = m.hemisphereSunlit(sun, uv, min(args.rays, 256), 32)
+        vf = {"mode": "hemisphere", "rays_per_side": args.rays, "top_k": args.top_k,
+              "dropped_ray_fraction": dropped / (args.rays * 2.0 * sc.facet_count)}
+    else:
+        diag = m.buildVisibilityGraph(scenes.hemisphere_directions())
+        lit = m.computeSunlitFraction(sun)
+        vf = {"mode": "raster", "directions": 40, "raster": args.raster}
+    vf["build_s"] = time.perf_counter() - t0
+    vf["directed_edges"] = int(diag["directed_edge_count"])
+    rho, tau = scenes.band_optics(sc, args.bands)
+    dgeo = scenes.direct_geometry(sc, lit, sun)[None, :]
+    sky = np.full(args.bands, 100.0, np.float32)
+    beam = np.full(args.bands, 800.0, np.float32)
+    return dict(scene=sc, model=m, rho=rho, tau=tau, dgeo=dgeo, sky=sky, beam=beam, vf=vf,
+                sun=sun, lit=lit)
+
+
+def workload_name(args, w):
+    sc = w["scene"]
+    return (f"{'config1' if args.quick else 'config2'} forest: {sc.facet_count:,} facets, "
+            f"{args.bands} bands x 1 sun, view factors: {w['vf']['mode']}")
+
+
+# ---- reference CPU arm --------------------------------------------------------
+def reference_cpu(w, budget_s=20.0, threads=None):
+    """The reference's solveCpu on host cores: one band per thread, the
+    reference's fixed 64 sweeps; a bounded sample of bands."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import pyoracle
+    from oracle.pyoracle import Graph
+    m = w["model"]
+    g = Graph(*m.graph())
+    ref = None
+    kind = "port"
+    try:
+        path = pyoracle.build_reference()
+        if path:
+            ref = pyoracle.Reference(path)
+            kind = "reference"
+    except Exception:
+        ref = None
+    solver = ref if ref is not None else pyoracle.Oracle()
+    S = g.surface_count
+    threads = threads or os.cpu_count() or 1
+
+    def optics_for(b):
+        o = np.zeros((S, 4), np.float32)
+        o[:, 0] = w["rho"][b]
+        o[:, 1] = w["tau"][b]
+        o[:, 3] = w["dgeo"][0] * w["beam"][b]
+        return o
+
+    # one band first to size the sample
+    t0 = time.perf_counter()
+    solver.solve(g, optics_for(len(w["sky"]) - 1), float(w["sky"][-1]), 64)
+    one = time.perf_counter() - t0
+    bands = max(1, min(len(w["sky"]), int(budget_s / max(one, 1e-6)) * threads // 2 or 1))
+    bands = min(bands, threads * max(1, int(budget_s / max(one, 1e-6))))
+    bands = max(1, min(bands, len(w["sky"])))
+    picks = np.linspace(0, len(w["sky"]) - 1, bands).round().astype(int)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=min(threads, bands)) as ex:
+        list(ex.map(lambda b: solver.solve(g, optics_for(b), float(w["sky"][b]), 64), picks))
+    dt = time.perf_counter() - t0
+    value = w["scene"].facet_count * bands / dt
+    return {"value": value, "unit": UNIT, "cores": int(min(threads, bands)), "kind": kind,
+            "sample": f"{bands} of {len(w['sky'])} bands x 1 sun, 64 Jacobi sweeps each "
+                      f"(reference solveCpu, FP64 gather), one band per thread, {dt:.2f} s",
+            "seconds": dt}
+
+
+# ---- GPU arm ------------------------------------------------------------------
+def run_gpu(args, rank, world, local):
+    import torch
+
+    from streamsim_gb300 import facetcu as fc
+    from streamsim_gb300 import scenes
+
+    torch.cuda.set_device(local)
+    w = build_workload(args, fc, scenes)
+    m = w["model"]
+    sc = w["scene"]
+    S = sc.surface_count
+    B = args.bands
+    prec = fc.PRECISION_MIXED if args.precision == "mixed" else fc.PRECISION_FP32
+
+    # FP64 truth of the same graph (not timed)
+    truth, tres = m.solveBatched(w["rho"], w["tau"], w["sky"], w["beam"], w["dgeo"],
+                                 precision=fc.PRECISION_FP64, tolerance=1e-12,
+                                 maximum_iterations=4000)
+
+    dev = torch.device("cuda", local)
+    t = {k: torch.from_numpy(np.ascontiguousarray(w[k])).to(dev)
+         for k in ("rho", "tau", "sky", "beam", "dgeo")}
+    out = torch.empty((B, S), dtype=torch.float32, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.ExternalStream(m.stream(), device=dev)
+    cfg = fc.BatchConfig(B, 1, prec, fc.WARM_NONE, 2000, args.tolerance, 0, 0)
+
+    def step(c=cfg):
+        return m.solveBatchedDevice(c, t["rho"].data_ptr(), t["tau"].data_ptr(), None,
+                                    t["sky"].data_ptr(), t["beam"].data_ptr(),
+                                    t["dgeo"].data_ptr(), None, out.data_ptr())
+
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        res = step()
+    err_out = out.cpu().numpy()
+    scale = np.maximum(np.abs(truth), 1e-6 * np.abs(truth).max())
+    err = float(np.max(np.abs(err_out - truth) / scale))
+
+    times = []
+    launches = []
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            res = step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            launches.append(res["kernel_launches"])
+    torch.cuda.synchronize()
+    barrier(world)
+    step_s = allreduce_max(float(np.mean(times)), world)
+    units = sc.facet_count * B * 1
+    value = units * world / step_s
+
+    # sweep-kernel roofline: one extra solve with per-sweep CUDA events
+    cfg_t = fc.BatchConfig(B, 1, prec, fc.WARM_NONE, 2000, args.tolerance, 0,
+                           fc.BATCH_TIME_SWEEPS)
+    rt = step(cfg_t)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = rt["sweep_bytes"] / max(rt["sweep_seconds"], 1e-12) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None,
+                "kernel": "k_sweep_defect<32>" if prec == fc.PRECISION_MIXED else "k_sweep<32,float>",
+                "avg_sweep_ms": rt["sweep_seconds"] / max(rt["sweeps"], 1) * 1e3,
+                "algorithmic_bytes_per_sweep": rt["sweep_bytes"] / max(rt["sweeps"], 1),
+                "peak_source": "measured" if peaks else "fallback"}
+    try:
+        prof = json.load(open(os.path.join(ROOT, "profiles", "sweep_traffic.json")))
+        roofline["traffic"] = prof.get("bytes_per_sweep")
+    except (OSError, ValueError):
+        pass
+
+    # end to end through the host-buffer C ABI (pinned buffers, copies timed)
+    pin = {k: torch.from_numpy(np.ascontiguousarray(w[k])).pin_memory()
+           for k in ("rho", "tau", "sky", "beam", "dgeo")}
+    host_out = torch.empty((B, S), dtype=torch.float32).pin_memory()
+    h2d = sum(v.numel() * 4 for v in pin.values())
+    d2h = host_out.numel() * 4
+
+    def e2e_call():
+        return m.lib.facetcu_solve_batched(
+            m.h, fc.C.byref(cfg), fc.C.c_void_p(pin["rho"].data_ptr()),
+            fc.C.c_void_p(pin["tau"].data_ptr()), None, fc.C.c_void_p(pin["sky"].data_ptr()),
+            fc.C.c_void_p(pin["beam"].data_ptr()), fc.C.c_void_p(pin["dgeo"].data_ptr()), None,
+            fc.C.c_void_p(host_out.data_ptr()), fc.C.byref(fc.BatchResult()))
+
+    e2e_call()
+    e2e_times = []
+    for _ in range(max(2, args.steps)):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = e2e_call()
+        e2e_times.append(time.perf_counter() - t0)
+        assert rc in (fc.OK, fc.NOT_CONVERGED), rc
+    e2e_s = allreduce_max(float(np.mean(e2e_times)), world)
+    e2e = {"value": units * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h)}
+
+    # plain FP32 GPU solver: the reference's per-band solve (radiosity.comp,
+    # 64 sweeps per band) through facetcu_solve, sampled on 4 bands.
+    plain = None
+    if not args.no_plain:
+        picks = np.linspace(0, B - 1, 4).round().astype(int)
+        opt = []
+        for b in picks:
+            o = np.zeros((S, 4), np.float32)
+            o[:, 0] = w["rho"][b]
+            o[:, 1] = w["tau"][b]
+            o[:, 3] = w["dgeo"][0] * w["beam"][b]
+            opt.append(o)
+        m.solve(opt[0], 100.0, 64)
+        t0 = time.perf_counter()
+        perr = 0.0
+        for b, o in zip(picks, opt):
+            r = m.solve(o, float(w["sky"][b]), 64)
+            perr = max(perr, float(np.max(np.abs(r["radiosity"] - truth[b]) / scale[b])))
+        dt = time.perf_counter() - t0
+        plain = {"value": sc.facet_count * len(picks) / dt, "unit": UNIT,
+                 "sample": f"{len(picks)} bands x 64 sweeps of the reference-semantics kernel",
+                 "max_rel_err_vs_fp64": perr}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = reference_cpu(w)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16+f32" if prec == fc.PRECISION_MIXED else "f32",
+            "data": "synthetic (seeded scene generator, no dataset)",
+            "config": {"workload": workload_name(args, w), "facets": sc.facet_count,
+                       "sides": S, "bands": B, "suns": 1,
+                       "precision": args.precision, "tolerance": args.tolerance,
+                       "view_factors": w["vf"], "parallelism": f"replicas x{world}",
+                       "l2": "flushed (512 MB write) between timed steps"},
+            "max_rel_err_vs_fp64": err, "iterations": res["iterations"],
+            "residual_corrections": res["residual_corrections"],
+            "fp64_truth_iterations": tres["iterations"],
+            "roofline": roofline, "e2e": e2e, "gpu_launches": int(np.mean(launches)),
+            "clocks": clocks.summary(), "plain_fp32": plain,
+            "speedup_vs_plain_fp32": (value / plain["value"]) if plain else None,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    m.close()
+
+
+def run_reference(args, rank, world, local):
+    if rank != 0:
+        return
+    from streamsim_gb300 import facetcu as fc
+    from streamsim_gb300 import scenes
+    # the graph is built by the library (not timed); only the CPU solve is timed
+    w = build_workload(args, fc, scenes)
+    cpu = reference_cpu(w, budget_s=max(10.0, 4.0 * args.steps))
+    line = {"metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": cpu["seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 state, f64 gather",
+            "data": "synthetic (seeded scene generator, no dataset)",
+            "config": {"workload": workload_name(args, w), "facets": w["scene"].facet_count,
+                       "bands": args.bands, "suns": 1, "view_factors": w["vf"]},
+            "impl": "reference",
+            "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    w["model"].close()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world, local)
+    else:
+        run_gpu(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -133,22 +133,26 @@ int facetcu_set_graph(facetcu_context *ctx, uint32_t surface_count,
 /* ---- solves (reference semantics) ------------------------------------ */
 /* FacetrtVulkan::solve (facetrt_vulkan.cpp:1177-1247): `iterations` Jacobi
  * sweeps from B = 0 with the two-sided update of radiosity.comp:49-106;
- * FP32 gather in CSR order.  radiosity: 2F. */
+ * FP32 gather in CSR order.  optics_count must be 2F (the reference checks
+ * optics.size(), facetrt_vulkan.cpp:1162); radiosity receives 2F floats;
+ * initial (solve_accelerated) holds 2F floats when given. */
 int facetcu_solve(facetcu_context *ctx, const facetcu_surface_optics *optics,
-                  float sky_radiosity, uint32_t iterations, float relaxation,
-                  float *radiosity, uint32_t *iterations_done, float *max_delta);
+                  uint64_t optics_count, float sky_radiosity, uint32_t iterations,
+                  float relaxation, float *radiosity, uint32_t *iterations_done,
+                  float *max_delta);
 /* FacetrtVulkan::solveAccelerated (facetrt_vulkan.cpp:1249-1358): optional
  * warm start, batches of batch_iterations sweeps, stop when the absolute
  * max|dB| of the last sweep <= tolerance. initial may be NULL. */
 int facetcu_solve_accelerated(facetcu_context *ctx, const facetcu_surface_optics *optics,
-                              float sky_radiosity, const float *initial,
+                              uint64_t optics_count, float sky_radiosity, const float *initial,
                               uint32_t maximum_iterations, uint32_t batch_iterations,
                               float tolerance, float relaxation, float *radiosity,
                               uint32_t *iterations_done, float *max_delta);
 /* FacetrtVulkan::incidentIrradiance (facetrt_vulkan.cpp:1360-1399):
- * H_s = max(0, diffuse_s + D_s) from a solution, FP64 gather. */
+ * H_s = max(0, diffuse_s + D_s) from a solution, FP64 gather.  radiosity,
+ * optics and irradiance hold `count` = 2F elements. */
 int facetcu_incident_irradiance(facetcu_context *ctx, const float *radiosity,
-                                const facetcu_surface_optics *optics,
+                                const facetcu_surface_optics *optics, uint64_t count,
                                 float sky_radiosity, float *irradiance);
 
 /* ---- batched solves (no reference counterpart) ------------------------ */
@@ -178,15 +182,20 @@ typedef struct {
     uint32_t warm_start;        /* FACETCU_WARM_* */
     uint32_t maximum_iterations;
     float tolerance;            /* relative change per column */
-    uint32_t panel_width;       /* RHS columns per resident panel; 0 = autotuned */
-    uint32_t flags;             /* reserved, 0 */
+    uint32_t panel_width;       /* RHS columns per resident panel (<= 32); 0 = 32 */
+    uint32_t flags;             /* FACETCU_BATCH_TIME_SWEEPS: time every sweep kernel */
 } facetcu_batch_config;
+#define FACETCU_BATCH_TIME_SWEEPS 1u
 typedef struct {
     uint32_t iterations;        /* sweeps of the slowest panel */
     uint32_t residual_corrections;
     uint32_t converged;         /* 1 if every column met the tolerance */
     float max_relative_change;  /* worst column at exit */
-    double seconds;             /* device time of the solve */
+    double seconds;             /* device time of the solve (CUDA events) */
+    uint32_t kernel_launches;   /* kernels the solve launched */
+    uint32_t sweeps;            /* sweep kernels run, summed over panels */
+    double sweep_seconds;       /* summed sweep-kernel time (TIME_SWEEPS only) */
+    double sweep_bytes;         /* algorithmic HBM bytes of those sweeps */
 } facetcu_batch_result;
 int facetcu_solve_batched(facetcu_context *ctx, const facetcu_batch_config *config,
                           const float *reflectance, const float *transmittance,

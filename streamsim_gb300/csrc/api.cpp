@@ -175,6 +175,12 @@ void validate_optics(const facetcu_surface_optics* optics, size_t n)
     }
 }
 
+void validate_count(uint64_t count, uint32_t surfaces)
+{
+    if (count != surfaces)
+        throw Error(FACETCU_INVALID_ARGUMENT, "Optics array must contain exactly two sides per facet");
+}
+
 void validate_sky(float sky)
 {
     if (!std::isfinite(sky) || sky < 0.0f)
@@ -583,13 +589,14 @@ int facetcu_set_graph(facetcu_context* ctx, uint32_t surface_count, const uint32
 }
 
 // FacetrtVulkan::solve (facetrt_vulkan.cpp:1177-1247)
-int facetcu_solve(facetcu_context* ctx, const facetcu_surface_optics* optics, float sky,
-                  uint32_t iterations, float relaxation, float* radiosity,
-                  uint32_t* iterations_done, float* max_delta)
+int facetcu_solve(facetcu_context* ctx, const facetcu_surface_optics* optics,
+                  uint64_t optics_count, float sky, uint32_t iterations, float relaxation,
+                  float* radiosity, uint32_t* iterations_done, float* max_delta)
 {
     return guarded(ctx, [&] {
         require_graph(ctx, "solve()");
         const uint32_t S = ctx->graph.surfaces;
+        validate_count(optics_count, S);
         validate_optics(optics, S);
         validate_sky(sky);
         validate_relax(relaxation);
@@ -618,13 +625,15 @@ int facetcu_solve(facetcu_context* ctx, const facetcu_surface_optics* optics, fl
 
 // FacetrtVulkan::solveAccelerated (facetrt_vulkan.cpp:1249-1358)
 int facetcu_solve_accelerated(facetcu_context* ctx, const facetcu_surface_optics* optics,
-                              float sky, const float* initial, uint32_t maximum_iterations,
-                              uint32_t batch_iterations, float tolerance, float relaxation,
-                              float* radiosity, uint32_t* iterations_done, float* max_delta)
+                              uint64_t optics_count, float sky, const float* initial,
+                              uint32_t maximum_iterations, uint32_t batch_iterations,
+                              float tolerance, float relaxation, float* radiosity,
+                              uint32_t* iterations_done, float* max_delta)
 {
     return guarded(ctx, [&] {
         require_graph(ctx, "solveAccelerated()");
         const uint32_t S = ctx->graph.surfaces;
+        validate_count(optics_count, S);
         validate_optics(optics, S);
         validate_sky(sky);
         validate_relax(relaxation);
@@ -676,10 +685,12 @@ int facetcu_solve_accelerated(facetcu_context* ctx, const facetcu_surface_optics
 
 // FacetrtVulkan::incidentIrradiance (facetrt_vulkan.cpp:1360-1399)
 int facetcu_incident_irradiance(facetcu_context* ctx, const float* radiosity,
-                                const facetcu_surface_optics* optics, float sky, float* irradiance)
+                                const facetcu_surface_optics* optics, uint64_t count, float sky,
+                                float* irradiance)
 {
     return guarded(ctx, [&] {
-        if (!ctx->initialized || !ctx->graph_ready || !radiosity || !optics)
+        if (!ctx->initialized || !ctx->graph_ready || !radiosity || !optics || !irradiance ||
+            count != uint64_t(ctx->graph.surfaces))
             throw Error(FACETCU_INVALID_ARGUMENT,
                         "Incident irradiance requires a completed solve and visibility graph");
         FCU_CHECK(cudaSetDevice(ctx->device));

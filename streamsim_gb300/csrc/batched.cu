@@ -419,7 +419,34 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
     g.facets = S / 2u;
     PanelParams pp{prho, ptau, pemis, pdir, psky};
 
-    uint32_t worst_iterations = 0, corrections = 0;
+    uint32_t worst_iterations = 0, corrections = 0, launches = 0, sweeps = 0;
+    double sweep_seconds = 0.0, sweep_bytes = 0.0;
+    const bool timed = (cfg.flags & FACETCU_BATCH_TIME_SWEEPS) != 0u;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (timed) {
+        FCU_CHECK(cudaEventCreate(&t0));
+        FCU_CHECK(cudaEventCreate(&t1));
+    }
+    // Algorithmic HBM bytes of one sweep: the graph once (packed or 8-byte
+    // edges, row offsets, denominators, sky counts), the panel read and
+    // written once, and the four per-side parameter planes.
+    const double edge_bytes = gr.packed_valid ? 4.0 : 8.0;
+    const double graph_bytes = double(gr.nnz) * edge_bytes + double(S + 1) * 4.0 + double(S) * 8.0;
+    const double panel_bytes = double(cells) * double(elem) * 2.0 + double(cells) * 16.0;
+    auto timed_sweep = [&](auto&& launch) {
+        if (timed) FCU_CHECK(cudaEventRecord(t0, s));
+        launch();
+        ++launches;
+        ++sweeps;
+        if (timed) {
+            FCU_CHECK(cudaEventRecord(t1, s));
+            FCU_CHECK(cudaEventSynchronize(t1));
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, t0, t1);
+            sweep_seconds += double(ms) * 1e-3;
+            sweep_bytes += graph_bytes + panel_bytes;
+        }
+    };
     bool all_converged = true;
     float worst_change = 0.0f;
     const uint32_t max_it = cfg.maximum_iterations ? cfg.maximum_iterations : 1000u;
@@ -427,6 +454,7 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
     const uint32_t check_every = 8;
 
     for (uint32_t c0 = 0; c0 < R; c0 += uint32_t(P)) {
+        launches += 4;  // prepare, sky, panel in, panel out
         k_prepare_panel<<<blocks_for(cells, 256), 256, 0, s>>>(S, p.bands, R, c0, P, p.rho, p.tau,
                                                                 p.emis, p.beam, p.dgeo, prho, ptau,
                                                                 pemis, pdir);
@@ -453,14 +481,17 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
                     const uint32_t sweep = it + k;
                     char* in = (sweep & 1u) ? x1 : x0;
                     char* out = (sweep & 1u) ? x0 : x1;
-                    if (fp64)
-                        launch_sweep<double>(P, g, pp, reinterpret_cast<const double*>(in),
-                                             reinterpret_cast<double*>(out), stats, flag, s);
-                    else
-                        launch_sweep<float>(P, g, pp, reinterpret_cast<const float*>(in),
-                                            reinterpret_cast<float*>(out), stats, flag, s);
+                    timed_sweep([&] {
+                        if (fp64)
+                            launch_sweep<double>(P, g, pp, reinterpret_cast<const double*>(in),
+                                                 reinterpret_cast<double*>(out), stats, flag, s);
+                        else
+                            launch_sweep<float>(P, g, pp, reinterpret_cast<const float*>(in),
+                                                reinterpret_cast<float*>(out), stats, flag, s);
+                    });
                     k_check<<<1, 64, 0, s>>>(stats, flag, P, tol, sweep);
                     FCU_LAUNCH("k_check");
+                    ++launches;
                 }
                 it += batch;
                 FCU_CHECK(cudaMemcpyAsync(host_flag, flag, 12, cudaMemcpyDeviceToHost, s));
@@ -477,9 +508,10 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
             float* Y = reinterpret_cast<float*>(x1);
             while (it < max_it) {
                 // FP32 residual sweep: Y = Q + K X; converged check on it.
-                launch_sweep<float>(P, g, pp, X, Y, stats, flag, s);
+                timed_sweep([&] { launch_sweep<float>(P, g, pp, X, Y, stats, flag, s); });
                 k_check<<<1, 64, 0, s>>>(stats, flag, P, tol, it);
                 FCU_LAUNCH("k_check");
+                ++launches;
                 ++it;
                 ++corrections;
                 FCU_CHECK(cudaMemcpyAsync(host_flag, flag, 12, cudaMemcpyDeviceToHost, s));
@@ -492,6 +524,7 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
                 std::memcpy(&start_change, &host_flag[2], 4);
                 k_defect_init<<<blocks_for(cells, 256), 256, 0, s>>>(X, Y, d0, cells, flag);
                 FCU_LAUNCH("k_defect_init");
+                ++launches;
                 std::swap(X, Y);  // X = newest FP32 iterate
                 // defect sweeps in batches; stop the cycle when the relative
                 // defect fell below start_change * cycle_drop or under tol
@@ -502,12 +535,13 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
                     const uint32_t batch = std::min(check_every, max_it - it);
                     uint32_t sub_flag[3];
                     for (uint32_t k = 0; k < batch; ++k) {
-                        launch_defect(P, g, pp, din, dout, X, stats, flag, s);
+                        timed_sweep([&] { launch_defect(P, g, pp, din, dout, X, stats, flag, s); });
                         std::swap(din, dout);
                         k_check<<<1, 64, 0, s>>>(stats, flag + 3, P,
                                                  std::max(tol, start_change * cycle_drop),
                                                  it + k);
                         FCU_LAUNCH("k_check");
+                        ++launches;
                     }
                     it += batch;
                     FCU_CHECK(cudaMemcpyAsync(sub_flag, flag + 3, 12, cudaMemcpyDeviceToHost, s));
@@ -541,7 +575,15 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
         FCU_CHECK(cudaMemsetAsync(flag, 0, 32, s));
     }
     FCU_CHECK(cudaStreamSynchronize(s));
+    if (timed) {
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+    }
     if (result) {
+        result->kernel_launches = launches;
+        result->sweeps = sweeps;
+        result->sweep_seconds = sweep_seconds;
+        result->sweep_bytes = sweep_bytes;
         result->iterations = worst_iterations;
         result->residual_corrections = corrections;
         result->converged = all_converged ? 1u : 0u;

@@ -32,6 +32,7 @@ PRECISION_MIXED = 1
 PRECISION_FP64 = 2
 WARM_NONE = 0
 WARM_GIVEN = 1
+BATCH_TIME_SWEEPS = 1
 
 
 class FacetcuError(RuntimeError):
@@ -93,7 +94,9 @@ class BatchConfig(C.Structure):
 class BatchResult(C.Structure):
     _fields_ = [("iterations", C.c_uint32), ("residual_corrections", C.c_uint32),
                 ("converged", C.c_uint32), ("max_relative_change", C.c_float),
-                ("seconds", C.c_double)]
+                ("seconds", C.c_double), ("kernel_launches", C.c_uint32),
+                ("sweeps", C.c_uint32), ("sweep_seconds", C.c_double),
+                ("sweep_bytes", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -119,11 +122,12 @@ SIGNATURES = {
     "facetcu_graph_size": (C.c_int, [_ctx, C.POINTER(_u32), C.POINTER(C.c_uint64)]),
     "facetcu_get_graph": (C.c_int, [_ctx, _vp, _vp, _vp, _vp]),
     "facetcu_set_graph": (C.c_int, [_ctx, _u32, _vp, _vp, _vp, _vp]),
-    "facetcu_solve": (C.c_int, [_ctx, _vp, C.c_float, _u32, C.c_float, _vp, C.POINTER(_u32),
-                                C.POINTER(C.c_float)]),
-    "facetcu_solve_accelerated": (C.c_int, [_ctx, _vp, C.c_float, _vp, _u32, _u32, C.c_float,
-                                            C.c_float, _vp, C.POINTER(_u32), C.POINTER(C.c_float)]),
-    "facetcu_incident_irradiance": (C.c_int, [_ctx, _vp, _vp, C.c_float, _vp]),
+    "facetcu_solve": (C.c_int, [_ctx, _vp, C.c_uint64, C.c_float, _u32, C.c_float, _vp,
+                                C.POINTER(_u32), C.POINTER(C.c_float)]),
+    "facetcu_solve_accelerated": (C.c_int, [_ctx, _vp, C.c_uint64, C.c_float, _vp, _u32, _u32,
+                                            C.c_float, C.c_float, _vp, C.POINTER(_u32),
+                                            C.POINTER(C.c_float)]),
+    "facetcu_incident_irradiance": (C.c_int, [_ctx, _vp, _vp, C.c_uint64, C.c_float, _vp]),
     "facetcu_solve_batched": (C.c_int, [_ctx, C.POINTER(BatchConfig)] + [_vp] * 8 +
                               [C.POINTER(BatchResult)]),
     "facetcu_solve_batched_device": (C.c_int, [_ctx, C.POINTER(BatchConfig)] + [_vp] * 8 +
@@ -329,49 +333,60 @@ class FacetrtCuda:
 
     def solve(self, optics, sky_radiosity, iterations=64, relaxation=1.0):
         o = _f32(optics).reshape(-1, 4)
-        out = np.zeros(len(o), np.float32)
+        out = np.zeros(max(len(o), 2 * self.facet_count), np.float32)
         it = C.c_uint32()
         md = C.c_float()
-        self._check(self.lib.facetcu_solve(self.h, _ptr(o), sky_radiosity, iterations, relaxation,
-                                           _ptr(out), C.byref(it), C.byref(md)))
+        self._check(self.lib.facetcu_solve(self.h, _ptr(o), len(o), sky_radiosity, iterations,
+                                           relaxation, _ptr(out), C.byref(it), C.byref(md)))
         return {"radiosity": out, "iterations": it.value, "maxDelta": md.value}
 
     def solveAccelerated(self, optics, sky_radiosity, initial=None, maximum_iterations=64,
                          batch_iterations=8, tolerance=1.0e-4, relaxation=1.0):
         o = _f32(optics).reshape(-1, 4)
         init = None if initial is None else _f32(initial)
-        out = np.zeros(len(o), np.float32)
+        if init is not None and len(init) != len(o):
+            raise ValueError("Initial radiosity must contain one finite non-negative value per surface")
+        out = np.zeros(max(len(o), 2 * self.facet_count), np.float32)
         it = C.c_uint32()
         md = C.c_float()
         self._check(self.lib.facetcu_solve_accelerated(
-            self.h, _ptr(o), sky_radiosity, _ptr(init), maximum_iterations, batch_iterations,
-            tolerance, relaxation, _ptr(out), C.byref(it), C.byref(md)))
+            self.h, _ptr(o), len(o), sky_radiosity, _ptr(init), maximum_iterations,
+            batch_iterations, tolerance, relaxation, _ptr(out), C.byref(it), C.byref(md)))
         return {"radiosity": out, "iterations": it.value, "maxDelta": md.value}
 
     def incidentIrradiance(self, radiosity, optics, sky_radiosity):
         o = _f32(optics).reshape(-1, 4)
         r = _f32(radiosity)
+        if len(r) != len(o):
+            raise ValueError("Incident irradiance requires a completed solve and visibility graph")
         out = np.zeros(len(o), np.float32)
-        self._check(self.lib.facetcu_incident_irradiance(self.h, _ptr(r), _ptr(o), sky_radiosity,
-                                                         _ptr(out)))
+        self._check(self.lib.facetcu_incident_irradiance(self.h, _ptr(r), _ptr(o), len(o),
+                                                         sky_radiosity, _ptr(out)))
         return out
 
     # -- batched extension ------------------------------------------------
     def solveBatched(self, reflectance, transmittance, sky, beam, direct_geometry=None,
                      emission=None, precision=PRECISION_FP32, tolerance=1e-6,
-                     maximum_iterations=1000, initial=None, panel_width=0, raise_on_nonconvergence=True):
+                     maximum_iterations=1000, initial=None, panel_width=0, raise_on_nonconvergence=True,
+                     flags=0):
         """reflectance/transmittance/emission: (bands, S); sky, beam: (bands,);
         direct_geometry: (suns, S).  Returns radiosity (suns*bands, S) and the result dict."""
         rho = _f32(reflectance)
         tau = _f32(transmittance)
         bands = rho.shape[0]
         S = rho.shape[1]
+        if S != 2 * self.facet_count or tau.shape != rho.shape or \
+                (emission is not None and np.shape(emission) != rho.shape) or \
+                len(np.ravel(sky)) != bands or len(np.ravel(beam)) != bands:
+            raise ValueError("band arrays must be (bands, 2 * facets) with one sky/beam per band")
         emis = None if emission is None else _f32(emission)
         dgeo = None if direct_geometry is None else _f32(direct_geometry).reshape(-1, S)
         suns = 1 if dgeo is None else dgeo.shape[0]
         cfg = BatchConfig(bands, suns, precision, WARM_GIVEN if initial is not None else WARM_NONE,
-                          maximum_iterations, tolerance, panel_width, 0)
+                          maximum_iterations, tolerance, panel_width, flags)
         init = None if initial is None else _f32(initial)
+        if init is not None and init.size != suns * bands * S:
+            raise ValueError("initial radiosity must hold suns * bands * 2F values")
         out = np.zeros((suns * bands, S), np.float32)
         res = BatchResult()
         rc = self.lib.facetcu_solve_batched(self.h, C.byref(cfg), _ptr(rho), _ptr(tau), _ptr(emis),

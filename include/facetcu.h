@@ -79,6 +79,14 @@ typedef struct {
 /* FacetrtVulkan::CsrEdge (facetrt_vulkan.h:114-117). */
 typedef struct { uint32_t neighbor, count; } facetcu_csr_edge;
 
+/* ---- host helpers (no GPU needed) -------------------------------------- */
+/* makeHemisphereDirections (facetrtcore.cpp:475-489): `count` golden-spiral
+ * directions of the upper hemisphere (Y up), computed with the C library's
+ * float cos/sin like the reference. */
+void facetcu_hemisphere_directions(uint32_t count, facetcu_direction *out);
+/* sunDirection (facetrtcore.cpp:491-498): +X north, +Z east, Y up. */
+facetcu_direction facetcu_sun_direction(float zenith_degrees, float azimuth_degrees);
+
 /* ---- lifetime -------------------------------------------------------- */
 int facetcu_create(facetcu_context **out);
 void facetcu_release(facetcu_context *ctx);

@@ -222,6 +222,29 @@ uint32_t run_sweeps(facetcu_context* ctx, float sky, float relax, uint32_t count
 
 extern "C" {
 
+// facetrtcore.cpp:475-489
+void facetcu_hemisphere_directions(uint32_t count, facetcu_direction* out)
+{
+    if (!out) return;
+    const float golden = 2.39996322972865332f;
+    for (uint32_t i = 0; i < count; ++i) {
+        const float y = (static_cast<float>(i) + 0.5f) / static_cast<float>(count);
+        const float radius = std::sqrt(std::max(0.0f, 1.0f - y * y));
+        const float azimuth = golden * static_cast<float>(i);
+        out[i] = {radius * std::cos(azimuth), y, radius * std::sin(azimuth)};
+    }
+}
+
+// facetrtcore.cpp:491-498
+facetcu_direction facetcu_sun_direction(float zenith_degrees, float azimuth_degrees)
+{
+    const float pi = 3.14159265358979323846f;
+    const float zenith = zenith_degrees * pi / 180.0f;
+    const float azimuth = azimuth_degrees * pi / 180.0f;
+    return {std::sin(zenith) * std::cos(azimuth), std::cos(zenith),
+            std::sin(zenith) * std::sin(azimuth)};
+}
+
 int facetcu_create(facetcu_context** out)
 {
     if (!out) return FACETCU_INVALID_ARGUMENT;

@@ -108,6 +108,8 @@ _ctx = C.c_void_p
 
 # name -> (restype, argtypes) for every symbol of include/facetcu.h
 SIGNATURES = {
+    "facetcu_hemisphere_directions": (None, [_u32, _vp]),
+    "facetcu_sun_direction": (Direction, [C.c_float, C.c_float]),
     "facetcu_create": (C.c_int, [C.POINTER(_vp)]),
     "facetcu_release": (None, [_ctx]),
     "facetcu_last_error": (C.c_char_p, [_ctx]),
@@ -168,6 +170,19 @@ def header_symbols(header=None):
     header = header or os.path.join(HERE, "..", "include", "facetcu.h")
     text = open(header).read()
     return sorted(set(re.findall(r"\b(facetcu_[a-z0-9_]+)\s*\(", text)))
+
+
+def hemisphere_directions(count=40):
+    """makeHemisphereDirections (facetrtcore.cpp:475-489), computed by the library."""
+    out = np.zeros((count, 3), np.float32)
+    load().facetcu_hemisphere_directions(count, C.c_void_p(out.ctypes.data))
+    return out
+
+
+def sun_direction(zenith_deg, azimuth_deg):
+    """sunDirection (facetrtcore.cpp:491-498), computed by the library."""
+    d = load().facetcu_sun_direction(zenith_deg, azimuth_deg)
+    return np.array([d.x, d.y, d.z], np.float32)
 
 
 def device_count():

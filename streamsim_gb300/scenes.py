@@ -170,23 +170,17 @@ def config3(seed=0):
 
 # ---- directions and optics ------------------------------------------------
 def sun_direction(zenith_deg, azimuth_deg):
-    """facetrtcore.cpp:491-498 in float32 arithmetic order."""
-    pi = np.float32(3.14159265358979323846)
-    zen = np.float32(zenith_deg) * pi / np.float32(180.0)
-    az = np.float32(azimuth_deg) * pi / np.float32(180.0)
-    return np.array([np.sin(zen) * np.cos(az), np.cos(zen), np.sin(zen) * np.sin(az)], np.float32)
+    """facetrtcore.cpp:491-498, evaluated by the library's C++ host code so
+    that it rounds exactly as the reference's (C library cos/sin)."""
+    from . import facetcu
+    return facetcu.sun_direction(zenith_deg, azimuth_deg)
 
 
 def hemisphere_directions(count=40):
-    """facetrtcore.cpp:475-489 (golden-spiral upper hemisphere)."""
-    golden = np.float32(2.39996322972865332)
-    out = np.zeros((count, 3), np.float32)
-    for i in range(count):
-        y = (np.float32(i) + np.float32(0.5)) / np.float32(count)
-        r = np.sqrt(max(np.float32(0.0), np.float32(1.0) - y * y), dtype=np.float32)
-        az = golden * np.float32(i)
-        out[i] = [r * np.cos(az), y, r * np.sin(az)]
-    return out
+    """facetrtcore.cpp:475-489 (golden-spiral upper hemisphere), evaluated by
+    the library's C++ host code."""
+    from . import facetcu
+    return facetcu.hemisphere_directions(count)
 
 
 def direct_geometry(scene, sunlit, sun):

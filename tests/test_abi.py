@@ -63,3 +63,14 @@ def test_call_order_and_arguments_without_gpu(lib):
 def test_null_context_is_rejected(lib):
     assert lib.facetcu_destroy(None) == facetcu.INVALID_ARGUMENT
     assert lib.facetcu_create(None) == facetcu.INVALID_ARGUMENT
+
+
+def test_host_direction_helpers_match_reference(oracle, reference):
+    """makeHemisphereDirections / sunDirection (facetrtcore.cpp:475-498) of the
+    library's C++ host code round exactly like the reference's."""
+    d = facetcu.hemisphere_directions(40)
+    assert np.array_equal(d.view(np.uint32), reference.hemisphere_directions().view(np.uint32))
+    assert np.array_equal(d.view(np.uint32), oracle.hemisphere_directions().view(np.uint32))
+    for zen, az in [(30, 135), (0, 0), (75, 290), (45.5, 12.25), (89.9, 359.0)]:
+        assert np.array_equal(facetcu.sun_direction(zen, az).view(np.uint32),
+                              reference.sun_direction(zen, az).view(np.uint32))

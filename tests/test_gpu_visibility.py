@@ -24,9 +24,9 @@ def test_validation_scene_graph_bit_exact(oracle, golden_scene, name, raster):
     layers = oracle.adaptive_layers(F, 0, raster)
     bounds = (s["bmin"], s["bmax"])  # the CPU backend rasterises in the Scene bounds
     m = model_for(s["vertices"], raster, layers, bounds)
-    diag = m.buildVisibilityGraph(scenes.hemisphere_directions())
-    g = oracle.build_graph(s["vertices"], oracle_cfg(s["vertices"], raster, layers, bounds),
-                           oracle.hemisphere_directions())
+    dirs = scenes.hemisphere_directions()
+    diag = m.buildVisibilityGraph(dirs)
+    g = oracle.build_graph(s["vertices"], oracle_cfg(s["vertices"], raster, layers, bounds), dirs)
     assert graphs_equal(m.graph(), g) is None
     assert diag["directed_edge_count"] == g.nnz
     assert diag["fragment_overflow"] == 0 and diag["hash_overflow"] == 0
@@ -38,13 +38,34 @@ def test_validation_scene_graph_bit_exact(oracle, golden_scene, name, raster):
     m.close()
 
 
+def test_single_directions_and_repeated_direction(oracle, golden_scene):
+    """Each direction alone is exact, and 40 copies of one direction give
+    exactly 40 times its counts (exercises the multi-tile pair sort)."""
+    s = golden_scene("urban_tree_building")
+    bounds = (s["bmin"], s["bmax"])
+    m = model_for(s["vertices"], 256, 64, bounds)
+    dirs = scenes.hemisphere_directions()
+    cfg = oracle_cfg(s["vertices"], 256, 64, bounds)
+    for d in (0, 7, 19, 33):
+        m.buildVisibilityGraph(dirs[d:d + 1])
+        assert graphs_equal(m.graph(), oracle.build_graph(s["vertices"], cfg, dirs[d:d + 1])) is None
+    m.buildVisibilityGraph(dirs[5:6])
+    rows1, nb1, cnt1, den1, sky1 = m.graph()
+    m.buildVisibilityGraph(np.repeat(dirs[5:6], 40, axis=0))
+    rows, nb, cnt, den, sky = m.graph()
+    assert np.array_equal(rows, rows1) and np.array_equal(nb, nb1)
+    assert np.array_equal(cnt, 40 * cnt1) and np.array_equal(den, 40 * den1)
+    assert np.array_equal(sky, 40 * sky1)
+    m.close()
+
+
 def test_vertex_bounds_frame_matches_oracle(oracle):
     """Default frame = vertex bounds (FacetrtVulkan::setGeometry)."""
     sc = scenes.config1(seed=0)
     m = model_for(sc.vertices, 512, 64)
-    m.buildVisibilityGraph(scenes.hemisphere_directions())
-    g = oracle.build_graph(sc.vertices, oracle_cfg(sc.vertices, 512, 64),
-                           oracle.hemisphere_directions())
+    dirs = scenes.hemisphere_directions()
+    m.buildVisibilityGraph(dirs)
+    g = oracle.build_graph(sc.vertices, oracle_cfg(sc.vertices, 512, 64), dirs)
     assert graphs_equal(m.graph(), g) is None
     sun = scenes.sun_direction(30, 135)
     assert np.array_equal(m.computeSunlitFraction(sun),
@@ -62,8 +83,9 @@ def test_equal_depth_chains_and_deep_pixels(oracle):
     reference's std::sort order (chains > 64 take the deep-chain kernel)."""
     v = _stacked(1)
     m = model_for(v, 64, 128)
-    m.buildVisibilityGraph(scenes.hemisphere_directions())
-    g = oracle.build_graph(v, oracle_cfg(v, 64, 128), oracle.hemisphere_directions())
+    dirs = scenes.hemisphere_directions()
+    m.buildVisibilityGraph(dirs)
+    g = oracle.build_graph(v, oracle_cfg(v, 64, 128), dirs)
     assert g.max_depth == 100
     assert graphs_equal(m.graph(), g) is None
     sun = scenes.sun_direction(30, 135)
@@ -75,8 +97,9 @@ def test_periodic_tiles(oracle):
     v = _stacked(2)
     per = (4, 1.3, 1.1)
     m = model_for(v, 64, 512, periodic=per)
-    diag = m.buildVisibilityGraph(scenes.hemisphere_directions())
-    g = oracle.build_graph(v, oracle_cfg(v, 64, 512, periodic=per), oracle.hemisphere_directions())
+    dirs = scenes.hemisphere_directions()
+    diag = m.buildVisibilityGraph(dirs)
+    g = oracle.build_graph(v, oracle_cfg(v, 64, 512, periodic=per), dirs)
     assert graphs_equal(m.graph(), g) is None
     assert diag["max_closure_error"] == pytest.approx(g.max_closure_error, abs=0)
     m.close()

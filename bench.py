@@ -153,7 +153,8 @@ def build_workload(args, fc, scenes, oracle_mod=None):
     if mode == "hemisphere":
         uv, dirs = scenes.hemisphere_samples(args.rays, 32, seed=7)
         diag, dropped = m.buildHemisphereGraph(uv, dirs, args.rays, args.top_k, 32)
-        lit = m.hemisphereSunlit(sun, uv, min(args.rays, 256), 32)
+        suv, _ = scenes.hemisphere_samples(256, 32, seed=8)
+        lit = m.hemisphereSunlit(sun, suv, 256, 32)
         vf = {"mode": "hemisphere", "rays_per_side": args.rays, "top_k": args.top_k,
               "dropped_ray_fraction": dropped / (args.rays * 2.0 * sc.facet_count)}
     else:

@@ -126,6 +126,33 @@ int facetcu_compute_sunlit_fraction(facetcu_context *ctx,
                                     const facetcu_direction *sun_direction,
                                     float *fraction);
 
+/* Hemisphere ray-cast view factors (no reference counterpart): for every
+ * side, rays_per_side cosine-distributed rays from points on the facet,
+ * nearest hit by an LBVH; the top_k most-hit sides are kept per row and the
+ * row is renormalised over kept + sky rays (denominator = kept + sky).
+ * sample_uv: sets * rays_per_side * 2 barycentric (u, v); sample_dir:
+ * sets * rays_per_side * 3 local directions (z along the side normal);
+ * side s uses set s % sets. dropped (optional) = rays hitting sides cut by
+ * top_k, summed over all rows.  Limits: rays_per_side <= 1023, 2F <= 2^22.
+ * The LBVH is built on first use after setGeometry and kept. */
+typedef struct {
+    uint32_t rays_per_side;
+    uint32_t top_k;
+    uint32_t sample_sets;
+    uint32_t reserved;
+} facetcu_hemisphere_config;
+int facetcu_build_hemisphere_graph(facetcu_context *ctx,
+                                   const facetcu_hemisphere_config *config,
+                                   const float *sample_uv, const float *sample_dir,
+                                   facetcu_graph_diagnostics *diagnostics,
+                                   uint64_t *dropped);
+/* Sun visibility by shadow rays from `samples` points per side (set s % sets
+ * of sample_uv, which holds sets * samples * 2 floats); sides facing away
+ * from the sun get 0. fraction: 2F. */
+int facetcu_hemisphere_sunlit(facetcu_context *ctx, const facetcu_direction *sun_direction,
+                              uint32_t samples, uint32_t sample_sets,
+                              const float *sample_uv, float *fraction);
+
 /* Graph access (count form: F_sn = count_sn / denom_s, sky_s / denom_s). */
 int facetcu_graph_size(facetcu_context *ctx, uint32_t *surface_count,
                        uint64_t *directed_edge_count);

@@ -841,8 +841,6 @@ void orc_make_optics(const orc_vertex *v, uint32_t F, uint32_t leaf_count,
 /* kernel evaluates exactly these expressions; nearest hit = smallest t,    */
 /* ties to the lower facet index; the origin facet is skipped.              */
 /* ------------------------------------------------------------------------ */
-#define ORC_SAMPLE_SETS 32U
-
 static void side_frame(vec3 N, vec3 *T, vec3 *Bt)
 {
     const vec3 helper = fabsf(N.v[1]) < 0.9f ? v3(0.0f, 1.0f, 0.0f) : v3(1.0f, 0.0f, 0.0f);
@@ -915,7 +913,7 @@ static int cmp_u32(const void *a, const void *b)
 }
 
 int orc_hemisphere_graph(const orc_vertex *V, uint32_t F, const float *uv,
-                         const float *dirs, uint32_t rays, uint32_t top_k,
+                         const float *dirs, uint32_t rays, uint32_t sets, uint32_t top_k,
                          orc_graph *g, uint64_t *dropped_out)
 {
     memset(g, 0, sizeof(*g));
@@ -932,7 +930,7 @@ int orc_hemisphere_graph(const orc_vertex *V, uint32_t F, const float *uv,
     uint64_t dropped = 0, nnz = 0;
     for (uint32_t s = 0; s < S; ++s) {
         const uint32_t f = s >> 1U;
-        const uint32_t set = s % ORC_SAMPLE_SETS;
+        const uint32_t set = s % sets;
         vec3 N = v3(V[f * 3U].normal[0], V[f * 3U].normal[1], V[f * 3U].normal[2]);
         if (s & 1U) N = v3(-N.v[0], -N.v[1], -N.v[2]);
         vec3 T, Bt;
@@ -985,12 +983,12 @@ int orc_hemisphere_graph(const orc_vertex *V, uint32_t F, const float *uv,
 }
 
 int orc_hemisphere_sunlit(const orc_vertex *V, uint32_t F, const float *uv,
-                          uint32_t samples, orc_direction sun, float *fraction)
+                          uint32_t samples, uint32_t sets, orc_direction sun, float *fraction)
 {
     const vec3 d = v3(sun.x, sun.y, sun.z);
     for (uint32_t s = 0; s < 2U * F; ++s) {
         const uint32_t f = s >> 1U;
-        const uint32_t set = s % ORC_SAMPLE_SETS;
+        const uint32_t set = s % sets;
         vec3 N = v3(V[f * 3U].normal[0], V[f * 3U].normal[1], V[f * 3U].normal[2]);
         if (s & 1U) N = v3(-N.v[0], -N.v[1], -N.v[2]);
         if (!(vdot(N, d) > 0.0f)) { fraction[s] = 0.0f; continue; }

@@ -112,10 +112,10 @@ void orc_make_optics(const orc_vertex *vertices, uint32_t facet_count,
  * index first), denominators = kept + sky, sorted by neighbour. */
 int orc_hemisphere_graph(const orc_vertex *vertices, uint32_t facet_count,
                          const float *sample_uv, const float *sample_dir,
-                         uint32_t rays_per_side, uint32_t top_k,
+                         uint32_t rays_per_side, uint32_t sets, uint32_t top_k,
                          orc_graph *out, uint64_t *dropped);
 int orc_hemisphere_sunlit(const orc_vertex *vertices, uint32_t facet_count,
-                          const float *sample_uv, uint32_t samples,
+                          const float *sample_uv, uint32_t samples, uint32_t sets,
                           orc_direction sun, float *fraction);
 
 void orc_free(void *p);

@@ -154,10 +154,10 @@ class Oracle:
         L.orc_make_optics.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                       OrcDirection] + [C.c_float] * 5 + [C.c_void_p]
         L.orc_hemisphere_graph.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
-                                           C.c_uint32, C.c_uint32, C.POINTER(OrcGraph),
-                                           C.POINTER(C.c_uint64)]
+                                           C.c_uint32, C.c_uint32, C.c_uint32,
+                                           C.POINTER(OrcGraph), C.POINTER(C.c_uint64)]
         L.orc_hemisphere_sunlit.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
-                                            OrcDirection, C.c_void_p]
+                                            C.c_uint32, OrcDirection, C.c_void_p]
         L.orc_free.argtypes = [C.c_void_p]
 
     # -- geometry helpers -------------------------------------------------
@@ -275,24 +275,24 @@ class Oracle:
         return out
 
     # -- hemisphere mode -----------------------------------------------
-    def hemisphere_graph(self, vertices, sample_uv, sample_dir, rays, top_k):
+    def hemisphere_graph(self, vertices, sample_uv, sample_dir, rays, sets, top_k):
         vertices = np.ascontiguousarray(vertices, np.float32)
         sample_uv = np.ascontiguousarray(sample_uv, np.float32)
         sample_dir = np.ascontiguousarray(sample_dir, np.float32)
         g = OrcGraph()
         dropped = C.c_uint64()
         self.lib.orc_hemisphere_graph(vertices.ctypes.data, len(vertices) // 3,
-                                      sample_uv.ctypes.data, sample_dir.ctypes.data, rays,
+                                      sample_uv.ctypes.data, sample_dir.ctypes.data, rays, sets,
                                       top_k, C.byref(g), C.byref(dropped))
         return self._take_graph(g), dropped.value
 
-    def hemisphere_sunlit(self, vertices, sample_uv, samples, sun):
+    def hemisphere_sunlit(self, vertices, sample_uv, samples, sets, sun):
         vertices = np.ascontiguousarray(vertices, np.float32)
         sample_uv = np.ascontiguousarray(sample_uv, np.float32)
         out = np.zeros(2 * (len(vertices) // 3), np.float32)
         d = OrcDirection(*[float(x) for x in sun])
         self.lib.orc_hemisphere_sunlit(vertices.ctypes.data, len(vertices) // 3,
-                                       sample_uv.ctypes.data, samples, d, out.ctypes.data)
+                                       sample_uv.ctypes.data, samples, sets, d, out.ctypes.data)
         return out
 
 

@@ -44,6 +44,10 @@ struct facetcu_context {
     DeviceBuffer sun_total, sun_visible;
     BatchState batch;
     DeviceBuffer batch_inputs;
+
+    Lbvh bvh;
+    bool bvh_ready = false;
+    DeviceBuffer samples_uv, samples_dir, fraction;
 };
 
 namespace {
@@ -337,6 +341,10 @@ int facetcu_destroy(facetcu_context* ctx)
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     ctx->stream = nullptr;
     ctx->facets = 0;
+    for (DeviceBuffer* b : {&ctx->bvh.nodes, &ctx->bvh.tri, &ctx->bvh.parent, &ctx->bvh.flags,
+                            &ctx->samples_uv, &ctx->samples_dir, &ctx->fraction})
+        b->release();
+    ctx->bvh_ready = false;
     ctx->vertices_host.clear();
     ctx->bounds_override = false;
     ctx->initialized = false;
@@ -378,6 +386,7 @@ int facetcu_set_geometry(facetcu_context* ctx, const facetcu_vertex* vertices,
         FCU_CHECK(cudaStreamSynchronize(ctx->stream));
         ctx->graph_ready = false;
         ctx->graph.packed_valid = false;
+        ctx->bvh_ready = false;
         ctx->facets = uint32_t(vertex_count / 3);
         ctx->vertices_host.assign(vertices, vertices + vertex_count);
         for (int a = 0; a < 3; ++a) {
@@ -535,6 +544,91 @@ int facetcu_compute_sunlit_fraction(facetcu_context* ctx, const facetcu_directio
         FCU_CHECK(cudaStreamSynchronize(s));
         for (uint32_t i = 0; i < S; ++i)
             fraction[i] = t[i] ? float(v[i]) / float(t[i]) : 0.0f;
+        return FACETCU_OK;
+    });
+}
+
+namespace {
+void ensure_bvh(facetcu_context* ctx)
+{
+    if (ctx->bvh_ready) return;
+    for (int a = 0; a < 3; ++a) {
+        ctx->bvh.scene_min[a] = ctx->bmin[a];
+        ctx->bvh.scene_max[a] = ctx->bmax[a];
+    }
+    lbvh_build(ctx->vertices.as<facetcu_vertex>(), ctx->facets, ctx->bvh, ctx->ws, ctx->stream);
+    ctx->bvh_ready = true;
+}
+}  // namespace
+
+int facetcu_build_hemisphere_graph(facetcu_context* ctx, const facetcu_hemisphere_config* config,
+                                   const float* sample_uv, const float* sample_dir,
+                                   facetcu_graph_diagnostics* diagnostics, uint64_t* dropped)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "buildHemisphereGraph()");
+        if (ctx->facets == 0)
+            throw Error(FACETCU_LOGIC_ERROR, "setGeometry() must be called before buildHemisphereGraph()");
+        if (!config || !sample_uv || !sample_dir)
+            throw Error(FACETCU_INVALID_ARGUMENT, "hemisphere config and sample tables are required");
+        if (config->rays_per_side == 0 || config->rays_per_side > 1023)
+            throw Error(FACETCU_INVALID_ARGUMENT, "rays_per_side must be in [1, 1023]");
+        if (config->top_k == 0 || config->sample_sets == 0)
+            throw Error(FACETCU_INVALID_ARGUMENT, "top_k and sample_sets must be positive");
+        const uint32_t S = ctx->facets * 2u;
+        if (S > (1u << 22))
+            throw Error(FACETCU_OVERFLOW_ERROR, "hemisphere graphs support at most 2^22 sides");
+        cudaStream_t s = ctx->stream;
+        ctx->graph_ready = false;
+        const size_t n = size_t(config->sample_sets) * config->rays_per_side;
+        upload(ctx->samples_uv, sample_uv, n * 8, s);
+        upload(ctx->samples_dir, sample_dir, n * 12, s);
+        ensure_bvh(ctx);
+        DeviceGraph& g = ctx->graph;
+        unsigned long long drop = 0;
+        hemisphere_graph(ctx->vertices.as<facetcu_vertex>(), ctx->facets, ctx->bvh,
+                         ctx->samples_uv.as<float>(), ctx->samples_dir.as<float>(),
+                         config->rays_per_side, config->sample_sets, config->top_k, g, &drop,
+                         ctx->ws, s);
+        float closure = 0.0f;
+        uint32_t sampled = 0;
+        graph_closure(g, &closure, &sampled, ctx->ws, s);
+        graph_pack(g, ctx->ws, s);
+        FCU_CHECK(cudaStreamSynchronize(s));
+        facetcu_graph_diagnostics diag{};
+        diag.facet_count = ctx->facets;
+        diag.surface_count = S;
+        diag.directed_edge_count = uint32_t(g.nnz);
+        diag.max_closure_error = closure;
+        if (diagnostics) *diagnostics = diag;
+        if (dropped) *dropped = drop;
+        ctx->graph_ready = true;
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_hemisphere_sunlit(facetcu_context* ctx, const facetcu_direction* sun, uint32_t samples,
+                              uint32_t sample_sets, const float* sample_uv, float* fraction)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "hemisphereSunlit()");
+        if (ctx->facets == 0)
+            throw Error(FACETCU_LOGIC_ERROR, "setGeometry() must be called before hemisphereSunlit()");
+        if (!sun || !sample_uv || !fraction || samples == 0 || sample_sets == 0)
+            throw Error(FACETCU_INVALID_ARGUMENT, "sun, samples and output are required");
+        if (!std::isfinite(sun->x) || !std::isfinite(sun->y) || !std::isfinite(sun->z) ||
+            !(sun->x * sun->x + sun->y * sun->y + sun->z * sun->z > 0.0f))
+            throw Error(FACETCU_INVALID_ARGUMENT, "sun direction must be finite and non-zero");
+        cudaStream_t s = ctx->stream;
+        const uint32_t S = ctx->facets * 2u;
+        upload(ctx->samples_uv, sample_uv, size_t(sample_sets) * samples * 8, s);
+        ensure_bvh(ctx);
+        float* d = static_cast<float*>(ctx->fraction.reserve(size_t(S) * 4));
+        hemisphere_sunlit(ctx->vertices.as<facetcu_vertex>(), ctx->facets, ctx->bvh,
+                          ctx->samples_uv.as<float>(), samples, sample_sets,
+                          make_float3(sun->x, sun->y, sun->z), d, s);
+        FCU_CHECK(cudaMemcpyAsync(fraction, d, size_t(S) * 4, cudaMemcpyDeviceToHost, s));
+        FCU_CHECK(cudaStreamSynchronize(s));
         return FACETCU_OK;
     });
 }

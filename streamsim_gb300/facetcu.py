@@ -134,13 +134,12 @@ SIGNATURES = {
                               [C.POINTER(BatchResult)]),
     "facetcu_solve_batched_device": (C.c_int, [_ctx, C.POINTER(BatchConfig)] + [_vp] * 8 +
                                      [C.POINTER(BatchResult)]),
-}
-OPTIONAL_SIGNATURES = {
     "facetcu_build_hemisphere_graph": (C.c_int, [_ctx, C.POINTER(HemisphereConfig), _vp, _vp,
                                                  C.POINTER(GraphDiagnostics),
                                                  C.POINTER(C.c_uint64)]),
     "facetcu_hemisphere_sunlit": (C.c_int, [_ctx, C.POINTER(Direction), _u32, _u32, _vp, _vp]),
 }
+OPTIONAL_SIGNATURES = {}
 
 _LIB = None
 
@@ -306,6 +305,8 @@ class FacetrtCuda:
         cfg = HemisphereConfig(rays_per_side, top_k, sample_sets, 0)
         uv = _f32(sample_uv)
         dr = _f32(sample_dir)
+        if uv.size != 2 * rays_per_side * sample_sets or dr.size != 3 * rays_per_side * sample_sets:
+            raise ValueError("sample tables must hold sets * rays_per_side * (2 | 3) floats")
         diag = GraphDiagnostics()
         dropped = C.c_uint64()
         rc = self.lib.facetcu_build_hemisphere_graph(self.h, C.byref(cfg), _ptr(uv), _ptr(dr),
@@ -317,6 +318,8 @@ class FacetrtCuda:
     def hemisphereSunlit(self, sun, sample_uv, samples, sample_sets):
         sun = _f32(sun, (3,))
         uv = _f32(sample_uv)
+        if uv.size != 2 * samples * sample_sets:
+            raise ValueError("sample_uv must hold sets * samples * 2 floats")
         out = np.zeros(2 * self.facet_count, np.float32)
         d = Direction(*[float(x) for x in sun])
         self._check(self.lib.facetcu_hemisphere_sunlit(self.h, C.byref(d), samples, sample_sets,

@@ -89,12 +89,13 @@ def test_hemisphere_view_factors_statistics(oracle):
     v = sc.vertices.reshape(-1, 3, 6)[:, :, :3].astype(np.float64)
     area = 0.5 * np.linalg.norm(np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]), axis=1)
     A = np.repeat(area, 2)
-    lhs = (A[:, None] * F).sum()
-    rhs = (A[None, :] * F.T).sum()
-    assert abs(lhs - rhs) / lhs < 1e-12  # totals are a permutation
-    pair = A[:, None] * F
-    sym_err = np.abs(pair - pair.T).sum() / pair.sum()
-    assert sym_err < 0.5  # Monte Carlo noise at 256 rays; exact reciprocity is not expected
+    # reciprocity in aggregate: area-weighted exchange leaf -> soil equals
+    # soil -> leaf up to Monte Carlo noise (pairs are too noisy at 256 rays)
+    leaf = np.zeros(S, bool)
+    leaf[:2 * sc.leaf_count] = True
+    to_soil = (A[leaf, None] * F[np.ix_(leaf, ~leaf)]).sum()
+    to_leaf = (A[~leaf, None] * F[np.ix_(~leaf, leaf)]).sum()
+    assert abs(to_soil - to_leaf) / to_soil < 0.05
     # bottom sides of soil (facing down) see nothing but their own plane: all sky
     soil_bottom = np.arange(2 * sc.leaf_count + 1, S, 2)
     assert np.all(sky[soil_bottom] == den[soil_bottom])

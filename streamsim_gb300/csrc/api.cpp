@@ -328,6 +328,10 @@ int facetcu_destroy(facetcu_context* ctx)
     ctx->graph.sky.release();
     ctx->graph.packed.release();
     ctx->graph.packed_valid = false;
+    for (DeviceBuffer* b : {&ctx->graph.order, &ctx->graph.rank, &ctx->graph.p_rows,
+                            &ctx->graph.p_packed, &ctx->graph.p_denom, &ctx->graph.p_sky})
+        b->release();
+    ctx->graph.perm_valid = false;
     ctx->graph_ready = false;
     for (DeviceBuffer* b : {&ctx->raster.counts, &ctx->raster.offsets, &ctx->raster.records,
                             &ctx->raster.big_list, &ctx->raster.deep_list, &ctx->raster.stats,
@@ -386,6 +390,7 @@ int facetcu_set_geometry(facetcu_context* ctx, const facetcu_vertex* vertices,
         FCU_CHECK(cudaStreamSynchronize(ctx->stream));
         ctx->graph_ready = false;
         ctx->graph.packed_valid = false;
+        ctx->graph.perm_valid = false;
         ctx->bvh_ready = false;
         ctx->facets = uint32_t(vertex_count / 3);
         ctx->vertices_host.assign(vertices, vertices + vertex_count);
@@ -695,6 +700,7 @@ int facetcu_set_graph(facetcu_context* ctx, uint32_t surface_count, const uint32
         upload(g.denominators, denominators, size_t(surface_count) * 4, s);
         upload(g.sky, sky_counts, size_t(surface_count) * 4, s);
         g.packed_valid = false;
+        g.perm_valid = false;
         float closure;
         uint32_t sampled;
         graph_closure(g, &closure, &sampled, ctx->ws, s);
@@ -847,6 +853,11 @@ int run_batched(facetcu_context* ctx, const facetcu_batch_config* cfg, const flo
                 const float* dgeo, const float* initial, float* out, facetcu_batch_result* result)
 {
     BatchProblem p{};
+    p.vertices = ctx->vertices.as<facetcu_vertex>();
+    for (int a = 0; a < 3; ++a) {
+        p.lo[a] = ctx->bmin[a];
+        p.hi[a] = ctx->bmax[a];
+    }
     p.S = ctx->graph.surfaces;
     p.bands = cfg->band_count;
     p.suns = cfg->sun_count;

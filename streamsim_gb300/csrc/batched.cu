@@ -7,19 +7,23 @@
 //   B'_s,c = e_s,c + rho_s,c * H_s,c + tau_s,c * H_{s^1},c
 // (denom_s = 0: H = L_c + D_s,c).
 //
-// GB300 mapping.  The panel is stored side-major ([S][P], P <= 32 floats per
-// side), so one warp owns one facet (both sides) and the gather of neighbour
-// n reads one contiguous P-float row: for P = 32 a single 128-byte line per
-// edge, shared by every column.  The graph is read once per sweep for all
-// P columns, from a packed 4-byte edge array (22-bit neighbour, 10-bit
-// count) when it fits.  The grid is persistent (a multiple of the SM count);
-// each warp keeps per-column max|dB| and max|B| in registers and one
+// GB300 mapping.  The panel is stored side-major ([S][P]), so the gather of
+// neighbour n reads one contiguous row of P values shared by every column.
+// Wide panels (P = 32, 64, 128) give each lane P/32 adjacent columns: one
+// vector load per lane per edge (float / float2 / float4 in FP32, 1/2/4
+// packed BF16 in the defect sweep), one warp shuffle per packed 4-byte edge
+// (22-bit neighbour, 10-bit count), full 32-edge chunks without predication.
+// Narrow panels (P < 32, few RHS) split the warp into 32/P edge groups.
+// The graph is renumbered once along a Morton curve of facet centroids and
+// every warp sweeps a contiguous run of facets, so the neighbour rows a CTA
+// touches stay hot in L1/L2.  The grid is persistent (a multiple of the SM
+// count); each warp keeps per-column max|dB| and max|B| in registers and one
 // atomicMax per CTA and column publishes them.  A one-block check kernel
 // after every sweep sets a device-side done flag, so sweeps run in batches
 // without host round trips and stop at the exact sweep that converged.
 //
 // Precision modes:
-//   FP32  — panel and gather in FP32 (the plain batched solver);
+//   FP32  — panel and gather in FP32;
 //   FP64  — the same sweep in double (the truth the 1e-4 bar is checked on);
 //   MIXED — defect iteration: an FP32 sweep gives d = B' - B; then
 //           d <- K d runs with d stored in BF16 (half the gather bytes),
@@ -36,6 +40,7 @@ namespace facetcu {
 namespace {
 
 constexpr int kWarps = 8;  // warps per CTA
+constexpr int kMaxP = 128;
 constexpr uint32_t kNeighborMask = (1u << 22) - 1u;
 
 struct PanelParams {
@@ -76,11 +81,21 @@ template <> __device__ __forceinline__ float load_as_float<__nv_bfloat16>(const 
     return __bfloat162float(*p);
 }
 
-// Row gather: sum over the edges of side s of count * X[n*P + col], for the
-// lane's column; lanes are split into 32/P groups that take every
-// (32/P)-th edge, then reduced.  Acc is float for FP32/BF16 and double for FP64.
+template <typename T> __device__ __forceinline__ float absf(T x) { return float(x < T(0) ? -x : x); }
+
+// The facet range of one warp: contiguous runs keep neighbour rows local.
+__device__ __forceinline__ void warp_range(uint32_t facets, uint32_t& begin, uint32_t& end)
+{
+    const uint32_t warps = gridDim.x * kWarps;
+    const uint32_t w = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const uint32_t chunk = (facets + warps - 1) / warps;
+    begin = min(facets, w * chunk);
+    end = min(facets, begin + chunk);
+}
+
+// ---- narrow panels (P < 32): 32/P edge groups per warp -------------------
 template <int P, typename T, typename Acc>
-__device__ __forceinline__ Acc gather_row(const GraphView& g, uint32_t s, const T* X, int lane)
+__device__ __forceinline__ Acc gather_narrow(const GraphView& g, uint32_t s, const T* X, int lane)
 {
     constexpr int G = 32 / P;
     const int grp = lane / P, col = lane % P;
@@ -123,28 +138,271 @@ __device__ __forceinline__ Acc gather_row(const GraphView& g, uint32_t s, const 
     return acc;
 }
 
-template <typename T> __device__ __forceinline__ float absf(T x) { return float(x < T(0) ? -x : x); }
+// ---- wide panels (P = 32 * CPL): lane owns CPL adjacent columns -----------
+template <int CPL> struct RowF32;
+template <> struct RowF32<1> {
+    static __device__ __forceinline__ void load(const float* X, uint32_t nb, int lane, float* v)
+    {
+        v[0] = __ldg(X + size_t(nb) * 32 + lane);
+    }
+};
+template <> struct RowF32<2> {
+    static __device__ __forceinline__ void load(const float* X, uint32_t nb, int lane, float* v)
+    {
+        const float2 q = __ldg(reinterpret_cast<const float2*>(X) + size_t(nb) * 32 + lane);
+        v[0] = q.x;
+        v[1] = q.y;
+    }
+};
+template <> struct RowF32<4> {
+    static __device__ __forceinline__ void load(const float* X, uint32_t nb, int lane, float* v)
+    {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(X) + size_t(nb) * 32 + lane);
+        v[0] = q.x;
+        v[1] = q.y;
+        v[2] = q.z;
+        v[3] = q.w;
+    }
+};
+template <int CPL> struct RowBF16;
+template <> struct RowBF16<1> {
+    static __device__ __forceinline__ void load(const __nv_bfloat16* X, uint32_t nb, int lane, float* v)
+    {
+        const unsigned short h = __ldg(reinterpret_cast<const unsigned short*>(X) + size_t(nb) * 32 + lane);
+        v[0] = __uint_as_float(uint32_t(h) << 16);
+    }
+};
+template <> struct RowBF16<2> {
+    static __device__ __forceinline__ void load(const __nv_bfloat16* X, uint32_t nb, int lane, float* v)
+    {
+        const uint32_t w = __ldg(reinterpret_cast<const uint32_t*>(X) + size_t(nb) * 32 + lane);
+        v[0] = __uint_as_float(w << 16);
+        v[1] = __uint_as_float(w & 0xFFFF0000u);
+    }
+};
+template <> struct RowBF16<4> {
+    static __device__ __forceinline__ void load(const __nv_bfloat16* X, uint32_t nb, int lane, float* v)
+    {
+        const uint2 w = __ldg(reinterpret_cast<const uint2*>(X) + size_t(nb) * 32 + lane);
+        v[0] = __uint_as_float(w.x << 16);
+        v[1] = __uint_as_float(w.x & 0xFFFF0000u);
+        v[2] = __uint_as_float(w.y << 16);
+        v[3] = __uint_as_float(w.y & 0xFFFF0000u);
+    }
+};
 
-__device__ __forceinline__ void publish_stats(float md, float mb, int lane, int P, uint32_t* stats)
+template <int CPL, bool kBF16>
+__device__ __forceinline__ void load_row(const void* X, uint32_t nb, int lane, float* v)
 {
-    // CTA-level max over warps, then one atomic per column.
-    __shared__ float s_md[kWarps][32], s_mb[kWarps][32];
-    const int warp = threadIdx.x >> 5;
-    s_md[warp][lane] = md;
-    s_mb[warp][lane] = mb;
-    __syncthreads();
-    if (warp == 0 && lane < P) {
-        float a = 0.0f, b = 0.0f;
-        for (int w = 0; w < kWarps; ++w) {
-            a = fmaxf(a, s_md[w][lane]);
-            b = fmaxf(b, s_mb[w][lane]);
+    if constexpr (kBF16)
+        RowBF16<CPL>::load(static_cast<const __nv_bfloat16*>(X), nb, lane, v);
+    else
+        RowF32<CPL>::load(static_cast<const float*>(X), nb, lane, v);
+}
+
+// acc[k] += sum over edges of s of count * X[n][lane*CPL + k].  Packed
+// 4-byte edges when `packed` is set (one shuffle per edge), else the 8-byte
+// {neighbor, count} records (two shuffles per edge).
+template <int CPL, bool kBF16>
+__device__ __forceinline__ void gather_wide(const uint32_t* __restrict__ rows,
+                                            const uint32_t* __restrict__ packed,
+                                            const facetcu_csr_edge* __restrict__ edges, uint32_t s,
+                                            const void* X, int lane, float* acc)
+{
+    constexpr int U = 8;
+    const uint32_t start = __ldg(rows + s), end = __ldg(rows + s + 1);
+    uint32_t base = start;
+    if (!packed) {
+        for (; base < end; base += 32) {
+            const uint32_t n = min(32u, end - base);
+            uint2 e = make_uint2(0u, 0u);
+            if (uint32_t(lane) < n) e = __ldg(reinterpret_cast<const uint2*>(edges) + base + lane);
+            for (uint32_t j = 0; j < n; ++j) {
+                const uint32_t nb = __shfl_sync(0xffffffffu, e.x, int(j));
+                const float c = float(__shfl_sync(0xffffffffu, e.y, int(j)));
+                float v[CPL];
+                load_row<CPL, kBF16>(X, nb, lane, v);
+#pragma unroll
+                for (int k = 0; k < CPL; ++k) acc[k] += c * v[k];
+            }
         }
-        atomicMax(stats + lane, __float_as_uint(a));
-        atomicMax(stats + 32 + lane, __float_as_uint(b));
+        return;
+    }
+    for (; base + 32 <= end; base += 32) {
+        const uint32_t pk = __ldg(packed + base + lane);
+#pragma unroll
+        for (int j = 0; j < 32; j += U) {
+            float v[U][CPL];
+            float c[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t p = __shfl_sync(0xffffffffu, pk, j + u);
+                c[u] = float(p >> 22);
+                load_row<CPL, kBF16>(X, p & kNeighborMask, lane, v[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int k = 0; k < CPL; ++k) acc[k] += c[u] * v[u][k];
+        }
+    }
+    if (base < end) {
+        const uint32_t n = end - base;
+        const uint32_t pk = uint32_t(lane) < n ? __ldg(packed + base + lane) : 0u;
+        for (uint32_t j = 0; j < n; j += U) {
+            float v[U][CPL];
+            float c[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t p = __shfl_sync(0xffffffffu, pk, int((j + u) & 31u));
+                if (j + u < n) {
+                    c[u] = float(p >> 22);
+                    load_row<CPL, kBF16>(X, p & kNeighborMask, lane, v[u]);
+                } else {
+                    c[u] = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < CPL; ++k) v[u][k] = 0.0f;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int k = 0; k < CPL; ++k) acc[k] += c[u] * v[u][k];
+        }
     }
 }
 
-// One full sweep B_out = Q + K B_in over the panel (FP32 or FP64 state).
+// CTA-level max over warps, then one atomic per column.
+template <int NC>
+__device__ __forceinline__ void publish_stats(const float* md, const float* mb, int lane, int P,
+                                              uint32_t* stats)
+{
+    __shared__ float s_md[kWarps][kMaxP], s_mb[kWarps][kMaxP];
+    const int warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        s_md[warp][lane * NC + k] = md[k];
+        s_mb[warp][lane * NC + k] = mb[k];
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < P; c += blockDim.x) {
+        float a = 0.0f, b = 0.0f;
+        for (int w = 0; w < kWarps; ++w) {
+            a = fmaxf(a, s_md[w][c]);
+            b = fmaxf(b, s_mb[w][c]);
+        }
+        atomicMax(stats + c, __float_as_uint(a));
+        atomicMax(stats + kMaxP + c, __float_as_uint(b));
+    }
+}
+
+// One full FP32 sweep B_out = Q + K B_in over a wide panel.
+template <int CPL>
+__global__ void __launch_bounds__(kWarps * 32) k_sweep_wide(GraphView g, PanelParams pp,
+                                                            const float* __restrict__ Bin,
+                                                            float* __restrict__ Bout,
+                                                            uint32_t* stats, const uint32_t* done)
+{
+    if (*done) return;
+    constexpr int P = 32 * CPL;
+    const int lane = threadIdx.x & 31;
+    float md[CPL], mb[CPL], L[CPL];
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+        md[k] = 0.0f;
+        mb[k] = 0.0f;
+        L[k] = pp.skyL[lane * CPL + k];
+    }
+    uint32_t fb, fe;
+    warp_range(g.facets, fb, fe);
+    for (uint32_t f = fb; f < fe; ++f) {
+        float h[2][CPL];
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const uint32_t s = 2u * f + side;
+            float acc[CPL];
+#pragma unroll
+            for (int k = 0; k < CPL; ++k) acc[k] = 0.0f;
+            gather_wide<CPL, false>(g.rows, g.packed, g.edges, s, Bin, lane, acc);
+            const uint32_t d = __ldg(g.denom + s);
+            const float skyc = float(__ldg(g.skyc + s));
+#pragma unroll
+            for (int k = 0; k < CPL; ++k) {
+                const float dir = pp.direct[size_t(s) * P + lane * CPL + k];
+                h[side][k] = (d != 0u ? (skyc * L[k] + acc[k]) / float(d) : L[k]) + dir;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) {
+            const size_t i0 = size_t(2u * f) * P + lane * CPL + k, i1 = i0 + P;
+            const float b0 = pp.emis[i0] + pp.rho[i0] * h[0][k] + pp.tau[i0] * h[1][k];
+            const float b1 = pp.emis[i1] + pp.rho[i1] * h[1][k] + pp.tau[i1] * h[0][k];
+            const float o0 = Bin[i0], o1 = Bin[i1];
+            Bout[i0] = b0;
+            Bout[i1] = b1;
+            md[k] = fmaxf(md[k], fmaxf(fabsf(b0 - o0), fabsf(b1 - o1)));
+            mb[k] = fmaxf(mb[k], fmaxf(fabsf(b0), fabsf(b1)));
+        }
+    }
+    publish_stats<CPL>(md, mb, lane, P, stats);
+}
+
+// Defect sweep over a wide panel: d_out = K d_in (BF16 in and out, FP32
+// accumulation), X += d_out.  Stats: max|d_out|, max|X|.
+template <int CPL>
+__global__ void __launch_bounds__(kWarps * 32) k_defect_wide(GraphView g, PanelParams pp,
+                                                             const __nv_bfloat16* __restrict__ Din,
+                                                             __nv_bfloat16* __restrict__ Dout,
+                                                             float* __restrict__ X, uint32_t* stats,
+                                                             const uint32_t* done)
+{
+    if (*done) return;
+    constexpr int P = 32 * CPL;
+    const int lane = threadIdx.x & 31;
+    float md[CPL], mb[CPL];
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+        md[k] = 0.0f;
+        mb[k] = 0.0f;
+    }
+    uint32_t fb, fe;
+    warp_range(g.facets, fb, fe);
+    for (uint32_t f = fb; f < fe; ++f) {
+        float h[2][CPL];
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const uint32_t s = 2u * f + side;
+            float acc[CPL];
+#pragma unroll
+            for (int k = 0; k < CPL; ++k) acc[k] = 0.0f;
+            gather_wide<CPL, true>(g.rows, g.packed, g.edges, s, Din, lane, acc);
+            const uint32_t d = __ldg(g.denom + s);
+            const float inv = d ? 1.0f / float(d) : 0.0f;
+#pragma unroll
+            for (int k = 0; k < CPL; ++k) h[side][k] = acc[k] * inv;
+        }
+        float d0[CPL], d1[CPL];
+        const size_t base0 = size_t(2u * f) * P + lane * CPL, base1 = base0 + P;
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) {
+            d0[k] = pp.rho[base0 + k] * h[0][k] + pp.tau[base0 + k] * h[1][k];
+            d1[k] = pp.rho[base1 + k] * h[1][k] + pp.tau[base1 + k] * h[0][k];
+            const float x0 = X[base0 + k] + d0[k], x1 = X[base1 + k] + d1[k];
+            X[base0 + k] = x0;
+            X[base1 + k] = x1;
+            md[k] = fmaxf(md[k], fmaxf(fabsf(d0[k]), fabsf(d1[k])));
+            mb[k] = fmaxf(mb[k], fmaxf(fabsf(x0), fabsf(x1)));
+        }
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) {
+            Dout[base0 + k] = __float2bfloat16_rn(d0[k]);
+            Dout[base1 + k] = __float2bfloat16_rn(d1[k]);
+        }
+    }
+    publish_stats<CPL>(md, mb, lane, P, stats);
+}
+
+// Narrow-panel sweep (FP32 or FP64 state; also used for the FP64 truth).
 template <int P, typename T>
 __global__ void __launch_bounds__(kWarps * 32) k_sweep(GraphView g, PanelParams pp, const T* Bin,
                                                        T* Bout, uint32_t* stats,
@@ -154,16 +412,17 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep(GraphView g, PanelParams 
     using Acc = T;
     const int lane = threadIdx.x & 31;
     const int col = lane % P;
-    const uint32_t warps_total = gridDim.x * kWarps;
-    float md = 0.0f, mb = 0.0f;
+    float md[1] = {0.0f}, mb[1] = {0.0f};
     const Acc L = Acc(pp.skyL[col]);
-    for (uint32_t f = blockIdx.x * kWarps + (threadIdx.x >> 5); f < g.facets; f += warps_total) {
+    uint32_t fb, fe;
+    warp_range(g.facets, fb, fe);
+    for (uint32_t f = fb; f < fe; ++f) {
         const uint32_t s0 = 2u * f, s1 = s0 + 1u;
         Acc h[2];
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             const uint32_t s = s0 + k;
-            const Acc acc = gather_row<P, T, Acc>(g, s, Bin, lane);
+            const Acc acc = gather_narrow<P, T, Acc>(g, s, Bin, lane);
             const uint32_t d = g.denom[s];
             const Acc dir = Acc(pp.direct[size_t(s) * P + col]);
             h[k] = (d == 0u ? L : (Acc(g.skyc[s]) * L + acc) / Acc(d)) + dir;
@@ -175,15 +434,14 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep(GraphView g, PanelParams 
             const Acc o0 = Bin[i0], o1 = Bin[i1];
             Bout[i0] = b0;
             Bout[i1] = b1;
-            md = fmaxf(md, fmaxf(absf(b0 - o0), absf(b1 - o1)));
-            mb = fmaxf(mb, fmaxf(absf(b0), absf(b1)));
+            md[0] = fmaxf(md[0], fmaxf(absf(b0 - o0), absf(b1 - o1)));
+            mb[0] = fmaxf(mb[0], fmaxf(absf(b0), absf(b1)));
         }
     }
-    publish_stats(md, mb, lane, P, stats);
+    // lanes >= P hold zeros; column c of the stats is lane c (one column each)
+    publish_stats<1>(md, mb, lane, P, stats);
 }
 
-// Defect sweep of the MIXED mode: d_out = K d_in with d in BF16, FP32
-// accumulation; X += d_out (FP32 panel).  Stats: max|d_out|, max|X|.
 template <int P>
 __global__ void __launch_bounds__(kWarps * 32) k_sweep_defect(GraphView g, PanelParams pp,
                                                               const __nv_bfloat16* Din,
@@ -194,15 +452,16 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep_defect(GraphView g, Panel
     if (*done) return;
     const int lane = threadIdx.x & 31;
     const int col = lane % P;
-    const uint32_t warps_total = gridDim.x * kWarps;
-    float md = 0.0f, mb = 0.0f;
-    for (uint32_t f = blockIdx.x * kWarps + (threadIdx.x >> 5); f < g.facets; f += warps_total) {
+    float md[1] = {0.0f}, mb[1] = {0.0f};
+    uint32_t fb, fe;
+    warp_range(g.facets, fb, fe);
+    for (uint32_t f = fb; f < fe; ++f) {
         const uint32_t s0 = 2u * f, s1 = s0 + 1u;
         float h[2];
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             const uint32_t s = s0 + k;
-            const float acc = gather_row<P, __nv_bfloat16, float>(g, s, Din, lane);
+            const float acc = gather_narrow<P, __nv_bfloat16, float>(g, s, Din, lane);
             const uint32_t d = g.denom[s];
             h[k] = d == 0u ? 0.0f : acc / float(d);
         }
@@ -215,14 +474,14 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep_defect(GraphView g, Panel
             const float x0 = X[i0] + d0, x1 = X[i1] + d1;
             X[i0] = x0;
             X[i1] = x1;
-            md = fmaxf(md, fmaxf(fabsf(d0), fabsf(d1)));
-            mb = fmaxf(mb, fmaxf(fabsf(x0), fabsf(x1)));
+            md[0] = fmaxf(md[0], fmaxf(fabsf(d0), fabsf(d1)));
+            mb[0] = fmaxf(mb[0], fmaxf(fabsf(x0), fabsf(x1)));
         }
     }
-    publish_stats(md, mb, lane, P, stats);
+    publish_stats<1>(md, mb, lane, P, stats);
 }
 
-// d = Bnew - Bold (FP32) -> BF16, and keep Bnew as the FP32 panel in place.
+// d = Bnew - Bold (FP32) -> BF16.
 __global__ void k_defect_init(const float* Bold, const float* Bnew, __nv_bfloat16* D, size_t n,
                               const uint32_t* done)
 {
@@ -231,9 +490,9 @@ __global__ void k_defect_init(const float* Bold, const float* Bnew, __nv_bfloat1
     if (i < n) D[i] = __float2bfloat16_rn(Bnew[i] - Bold[i]);
 }
 
-// Convergence check after sweep `it` (0-based): every active column must
-// satisfy max|dB| <= tol * max|B|.  flag[0] = done, flag[1] = sweeps run,
-// flag[2] = max relative change bits of the last sweep.
+// Convergence check after sweep `it` (0-based): every column must satisfy
+// max|dB| <= tol * max|B|.  flag[0] = done, flag[1] = sweeps run, flag[2] =
+// max relative change bits of the last sweep.  Clears the stats.
 __global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint32_t it)
 {
     __shared__ int all_ok;
@@ -246,7 +505,7 @@ __global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint3
     const bool already = flag[0] != 0u;
     if (threadIdx.x < uint32_t(P)) {
         const float md = __uint_as_float(stats[threadIdx.x]);
-        const float mb = __uint_as_float(stats[32 + threadIdx.x]);
+        const float mb = __uint_as_float(stats[kMaxP + threadIdx.x]);
         const float rel = mb > 0.0f ? md / mb : (md > 0.0f ? INFINITY : 0.0f);
         if (!(md <= tol * mb) && !(md == 0.0f)) atomicExch(&all_ok, 0);
         atomicMax(reinterpret_cast<int*>(&worst), __float_as_int(rel));
@@ -257,14 +516,20 @@ __global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint3
         flag[2] = __float_as_uint(worst);
         if (all_ok) flag[0] = 1;
     }
-    if (threadIdx.x < 64) stats[threadIdx.x] = 0;
+    for (int i = threadIdx.x; i < 2 * kMaxP; i += blockDim.x) stats[i] = 0;
 }
 
-// Panel parameters for columns [c0, c0 + P) (column c = sun * bands + band).
+__device__ __forceinline__ uint32_t old_side(const uint32_t* order, uint32_t s)
+{
+    return order ? 2u * order[s >> 1] + (s & 1u) : s;
+}
+
+// Panel parameters for columns [c0, c0 + P) (column c = sun * bands + band),
+// rows in solver order (order maps solver facet -> caller facet).
 __global__ void k_prepare_panel(uint32_t S, uint32_t bands, uint32_t R, uint32_t c0, int P,
-                                const float* rho, const float* tau, const float* emis,
-                                const float* beam, const float* dgeo, float* prho, float* ptau,
-                                float* pemis, float* pdir)
+                                const uint32_t* order, const float* rho, const float* tau,
+                                const float* emis, const float* beam, const float* dgeo,
+                                float* prho, float* ptau, float* pemis, float* pdir)
 {
     const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= size_t(S) * P) return;
@@ -278,51 +543,94 @@ __global__ void k_prepare_panel(uint32_t S, uint32_t bands, uint32_t R, uint32_t
         pdir[i] = 0.0f;
         return;
     }
+    const uint32_t so = old_side(order, s);
     const uint32_t b = c % bands, k = c / bands;
-    const size_t bi = size_t(b) * S + s;
+    const size_t bi = size_t(b) * S + so;
     prho[i] = rho[bi];
     ptau[i] = tau[bi];
     pemis[i] = emis ? emis[bi] : 0.0f;
-    pdir[i] = dgeo ? beam[b] * dgeo[size_t(k) * S + s] : 0.0f;
+    pdir[i] = dgeo ? beam[b] * dgeo[size_t(k) * S + so] : 0.0f;
 }
 
 __global__ void k_panel_sky(uint32_t bands, uint32_t R, uint32_t c0, int P, const float* sky,
                             float* psky)
 {
-    const int j = threadIdx.x;
-    if (j >= P) return;
-    const uint32_t c = c0 + j;
-    psky[j] = c < R ? sky[c % bands] : 0.0f;
+    for (int j = threadIdx.x; j < P; j += blockDim.x) {
+        const uint32_t c = c0 + j;
+        psky[j] = c < R ? sky[c % bands] : 0.0f;
+    }
 }
 
-// [R][S] <-> [S][P] panel copies.
+// [R][S] (caller order) -> [S][P] (solver order)
 template <typename T>
-__global__ void k_panel_in(const float* src, uint32_t S, uint32_t R, uint32_t c0, int P, T* dst)
+__global__ void k_panel_in(const float* src, uint32_t S, uint32_t R, uint32_t c0, int P,
+                           const uint32_t* order, T* dst)
 {
     const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= size_t(S) * P) return;
     const uint32_t s = uint32_t(i / P), j = uint32_t(i % P), c = c0 + j;
-    dst[i] = (src && c < R) ? T(src[size_t(c) * S + s]) : T(0);
+    dst[i] = (src && c < R) ? T(src[size_t(c) * S + old_side(order, s)]) : T(0);
 }
 
+// [S][P] (solver order) -> [R][S] (caller order), through a shared tile
 template <typename T>
-__global__ void k_panel_out(const T* src, uint32_t S, uint32_t R, uint32_t c0, int P, float* dst)
+__global__ void k_panel_out(const T* src, uint32_t S, uint32_t R, uint32_t c0, int P,
+                            const uint32_t* order, float* dst)
 {
-    // tile transpose through shared memory: 32 sides x P columns per block
-    __shared__ float tile[32][33];
+    __shared__ float tile[32][kMaxP + 1];
     const uint32_t sb = blockIdx.x * 32;
-    const int t = threadIdx.x;  // 256 threads
-    for (int k = t; k < 32 * P; k += blockDim.x) {
+    for (int k = threadIdx.x; k < 32 * P; k += blockDim.x) {
         const int ls = k / P, j = k % P;
         const uint32_t s = sb + ls;
         tile[ls][j] = s < S ? float(src[size_t(s) * P + j]) : 0.0f;
     }
     __syncthreads();
-    for (int k = t; k < 32 * P; k += blockDim.x) {
+    for (int k = threadIdx.x; k < 32 * P; k += blockDim.x) {
         const int j = k / 32, ls = k % 32;
         const uint32_t s = sb + ls, c = c0 + j;
-        if (s < S && c < R) dst[size_t(c) * S + s] = tile[ls][j];
+        if (s < S && c < R) dst[size_t(c) * S + old_side(order, s)] = tile[ls][j];
     }
+}
+
+// ---- Morton renumbering of the graph -----------------------------------------
+__global__ void k_rank(const uint32_t* order, uint32_t facets, uint32_t* rank)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < facets) rank[order[i]] = i;
+}
+
+__global__ void k_perm_lengths(const uint32_t* order, uint32_t S, const uint32_t* rows,
+                               const uint32_t* denom, const uint32_t* sky, uint32_t* len,
+                               uint32_t* pden, uint32_t* psky)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const uint32_t so = 2u * order[s >> 1] + (s & 1u);
+    len[s] = rows[so + 1] - rows[so];
+    pden[s] = denom[so];
+    psky[s] = sky[so];
+}
+
+__global__ void k_perm_copy(const uint32_t* order, const uint32_t* rank, uint32_t S,
+                            const uint32_t* rows, const uint32_t* packed, const uint32_t* prows,
+                            uint32_t* ppacked)
+{
+    const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= S) return;
+    const uint32_t so = 2u * order[s >> 1] + (s & 1u);
+    const uint32_t b = rows[so], n = rows[so + 1] - b, pb = prows[s];
+    for (uint32_t i = lane; i < n; i += 32) {
+        const uint32_t p = packed[b + i];
+        const uint32_t nb = p & kNeighborMask;
+        const uint32_t nn = 2u * rank[nb >> 1] + (nb & 1u);
+        ppacked[pb + i] = nn | (p & ~kNeighborMask);
+    }
+}
+
+__global__ void k_set_last(uint32_t* rows, uint32_t n, const unsigned long long* total)
+{
+    rows[n] = uint32_t(*total);
 }
 
 inline unsigned blocks_for(size_t n, unsigned b) { return unsigned((n + b - 1) / b); }
@@ -344,6 +652,17 @@ void launch_sweep(int P, const GraphView& g, const PanelParams& pp, const T* in,
                   uint32_t* stats, const uint32_t* done, cudaStream_t s)
 {
     const int grid = persistent_grid();
+    if constexpr (sizeof(T) == 4) {
+        if (P >= 32) {
+            switch (P) {
+            case 32: k_sweep_wide<1><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, done); break;
+            case 64: k_sweep_wide<2><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, done); break;
+            default: k_sweep_wide<4><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, done); break;
+            }
+            FCU_LAUNCH("k_sweep_wide");
+            return;
+        }
+    }
     switch (P) {
     case 1: k_sweep<1, T><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, done); break;
     case 2: k_sweep<2, T><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, done); break;
@@ -360,6 +679,15 @@ void launch_defect(int P, const GraphView& g, const PanelParams& pp, const __nv_
                    cudaStream_t s)
 {
     const int grid = persistent_grid();
+    if (P >= 32) {
+        switch (P) {
+        case 32: k_defect_wide<1><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, done); break;
+        case 64: k_defect_wide<2><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, done); break;
+        default: k_defect_wide<4><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, done); break;
+        }
+        FCU_LAUNCH("k_defect_wide");
+        return;
+    }
     switch (P) {
     case 1: k_sweep_defect<1><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, done); break;
     case 2: k_sweep_defect<2><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, done); break;
@@ -371,53 +699,78 @@ void launch_defect(int P, const GraphView& g, const PanelParams& pp, const __nv_
     FCU_LAUNCH("k_sweep_defect");
 }
 
-int panel_width_for(uint32_t R, uint32_t requested)
+// Panel widths: power of two, at most `cap` (128 for FP32/BF16 with a
+// packed graph, 32 otherwise), at least the remaining columns when fewer.
+int panel_width(uint32_t remaining, uint32_t requested, uint32_t cap)
 {
-    uint32_t p = requested ? requested : 32u;
-    if (p > 32u) p = 32u;
+    uint32_t p = requested ? std::min(requested, cap) : cap;
     uint32_t w = 1;
-    while (w < p && w < R) w <<= 1;
-    return int(w);
+    while (w < p && w < remaining) w <<= 1;
+    return int(std::min(w, cap));
+}
+
+// Build (once per graph) the Morton-renumbered copy used by the solver.
+void ensure_permuted(DeviceGraph& gr, const BatchProblem& p, Workspace& ws, cudaStream_t s)
+{
+    if (gr.perm_valid || !gr.packed_valid || !p.vertices) return;
+    const uint32_t S = gr.surfaces, F = S / 2u;
+    uint32_t* order = static_cast<uint32_t*>(gr.order.reserve(size_t(F) * 4 + 4));
+    uint32_t* rank = static_cast<uint32_t*>(gr.rank.reserve(size_t(F) * 4 + 4));
+    morton_order(p.vertices, F, p.lo, p.hi, order, ws, s);
+    k_rank<<<blocks_for(F, 256), 256, 0, s>>>(order, F, rank);
+    FCU_LAUNCH("k_rank");
+    uint32_t* prows = static_cast<uint32_t*>(gr.p_rows.reserve((size_t(S) + 1) * 4));
+    uint32_t* pden = static_cast<uint32_t*>(gr.p_denom.reserve(size_t(S) * 4));
+    uint32_t* psky = static_cast<uint32_t*>(gr.p_sky.reserve(size_t(S) * 4));
+    uint32_t* ppk = static_cast<uint32_t*>(gr.p_packed.reserve(gr.nnz * 4 + 4));
+    k_perm_lengths<<<blocks_for(S, 256), 256, 0, s>>>(order, S, gr.row_offsets.as<uint32_t>(),
+                                                       gr.denominators.as<uint32_t>(),
+                                                       gr.sky.as<uint32_t>(), prows, pden, psky);
+    FCU_LAUNCH("k_perm_lengths");
+    unsigned long long* total = static_cast<unsigned long long*>(ws.e.reserve(64));
+    exclusive_scan_u32(prows, prows, S, total, ws, s);
+    k_set_last<<<1, 1, 0, s>>>(prows, S, total);
+    FCU_LAUNCH("k_set_last");
+    k_perm_copy<<<blocks_for(size_t(S) * 32, 256), 256, 0, s>>>(
+        order, rank, S, gr.row_offsets.as<uint32_t>(), gr.packed.as<uint32_t>(), prows, ppk);
+    FCU_LAUNCH("k_perm_copy");
+    FCU_CHECK(cudaStreamSynchronize(s));
+    gr.perm_valid = true;
 }
 
 }  // namespace
 
 // Host driver.  Returns FACETCU_OK or FACETCU_NOT_CONVERGED.
-int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_batch_config& cfg,
+int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu_batch_config& cfg,
                   const float* d_initial, float* d_out, BatchState& st, Workspace& ws,
                   cudaStream_t s, facetcu_batch_result* result)
 {
-    (void)ws;
+    DeviceGraph& gr = const_cast<DeviceGraph&>(gr_in);
     const uint32_t S = p.S, R = p.bands * p.suns;
-    const int P = panel_width_for(R, cfg.panel_width);
-    const size_t cells = size_t(S) * P;
-    const bool fp64 = cfg.precision == 2u;
+    const bool fp64 = cfg.precision == FACETCU_PRECISION_FP64;
     const bool mixed = cfg.precision == FACETCU_PRECISION_MIXED;
     const size_t elem = fp64 ? 8 : 4;
-    char* x0 = static_cast<char*>(st.x0.reserve(cells * elem));
-    char* x1 = static_cast<char*>(st.x1.reserve(cells * elem));
-    float* prm = static_cast<float*>(st.q.reserve(cells * 4 * 4 + 64 * 4));
-    float* prho = prm;
-    float* ptau = prm + cells;
-    float* pemis = prm + 2 * cells;
-    float* pdir = prm + 3 * cells;
-    float* psky = prm + 4 * cells;
-    uint32_t* stats = static_cast<uint32_t*>(st.colstats.reserve(256 * 4));
-    uint32_t* flag = stats + 64;
-    __nv_bfloat16* d0 = nullptr;
-    __nv_bfloat16* d1 = nullptr;
-    if (mixed) {
-        d0 = static_cast<__nv_bfloat16*>(st.half.reserve(cells * 2 * 2));
-        d1 = d0 + cells;
-    }
+    ensure_permuted(gr, p, ws, s);
+    const bool perm = gr.perm_valid;
+    const uint32_t* order = perm ? gr.order.as<uint32_t>() : nullptr;
     GraphView g;
-    g.rows = gr.row_offsets.as<uint32_t>();
-    g.packed = gr.packed_valid ? gr.packed.as<uint32_t>() : nullptr;
+    g.rows = perm ? gr.p_rows.as<uint32_t>() : gr.row_offsets.as<uint32_t>();
+    g.packed = perm ? gr.p_packed.as<uint32_t>()
+                    : (gr.packed_valid ? gr.packed.as<uint32_t>() : nullptr);
     g.edges = gr.edges.as<facetcu_csr_edge>();
-    g.denom = gr.denominators.as<uint32_t>();
-    g.skyc = gr.sky.as<uint32_t>();
+    g.denom = perm ? gr.p_denom.as<uint32_t>() : gr.denominators.as<uint32_t>();
+    g.skyc = perm ? gr.p_sky.as<uint32_t>() : gr.sky.as<uint32_t>();
     g.facets = S / 2u;
-    PanelParams pp{prho, ptau, pemis, pdir, psky};
+    const uint32_t cap = fp64 ? 32u : uint32_t(kMaxP);
+    const int Pmax = panel_width(R, cfg.panel_width, cap);
+    const size_t cells_max = size_t(S) * Pmax;
+    char* x0 = static_cast<char*>(st.x0.reserve(cells_max * elem));
+    char* x1 = static_cast<char*>(st.x1.reserve(cells_max * elem));
+    float* prm = static_cast<float*>(st.q.reserve(cells_max * 4 * 4 + kMaxP * 4));
+    uint32_t* stats = static_cast<uint32_t*>(st.colstats.reserve((2 * kMaxP + 16) * 4));
+    uint32_t* flag = stats + 2 * kMaxP;
+    __nv_bfloat16* dbuf = nullptr;
+    if (mixed) dbuf = static_cast<__nv_bfloat16*>(st.half.reserve(cells_max * 2 * 2));
 
     uint32_t worst_iterations = 0, corrections = 0, launches = 0, sweeps = 0;
     double sweep_seconds = 0.0, sweep_bytes = 0.0;
@@ -430,49 +783,59 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
     // Algorithmic HBM bytes of one sweep: the graph once (packed or 8-byte
     // edges, row offsets, denominators, sky counts), the panel read and
     // written once, and the four per-side parameter planes.
-    const double edge_bytes = gr.packed_valid ? 4.0 : 8.0;
+    const double edge_bytes = g.packed ? 4.0 : 8.0;
     const double graph_bytes = double(gr.nnz) * edge_bytes + double(S + 1) * 4.0 + double(S) * 8.0;
-    const double panel_bytes = double(cells) * double(elem) * 2.0 + double(cells) * 16.0;
-    auto timed_sweep = [&](auto&& launch) {
-        if (timed) FCU_CHECK(cudaEventRecord(t0, s));
-        launch();
-        ++launches;
-        ++sweeps;
-        if (timed) {
-            FCU_CHECK(cudaEventRecord(t1, s));
-            FCU_CHECK(cudaEventSynchronize(t1));
-            float ms = 0.0f;
-            cudaEventElapsedTime(&ms, t0, t1);
-            sweep_seconds += double(ms) * 1e-3;
-            sweep_bytes += graph_bytes + panel_bytes;
-        }
-    };
     bool all_converged = true;
     float worst_change = 0.0f;
     const uint32_t max_it = cfg.maximum_iterations ? cfg.maximum_iterations : 1000u;
     const float tol = cfg.tolerance;
     const uint32_t check_every = 8;
 
-    for (uint32_t c0 = 0; c0 < R; c0 += uint32_t(P)) {
+    for (uint32_t c0 = 0; c0 < R;) {
+        const int P = panel_width(R - c0, cfg.panel_width, uint32_t(Pmax));
+        const size_t cells = size_t(S) * P;
+        float* prho = prm;
+        float* ptau = prm + cells;
+        float* pemis = prm + 2 * cells;
+        float* pdir = prm + 3 * cells;
+        float* psky = prm + 4 * cells;
+        PanelParams pp{prho, ptau, pemis, pdir, psky};
+        __nv_bfloat16* d0 = dbuf;
+        __nv_bfloat16* d1 = dbuf ? dbuf + cells : nullptr;
+        const double panel_bytes = double(cells) * double(elem) * 2.0 + double(cells) * 16.0;
+        auto timed_sweep = [&](auto&& launch) {
+            if (timed) FCU_CHECK(cudaEventRecord(t0, s));
+            launch();
+            ++launches;
+            ++sweeps;
+            if (timed) {
+                FCU_CHECK(cudaEventRecord(t1, s));
+                FCU_CHECK(cudaEventSynchronize(t1));
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, t0, t1);
+                sweep_seconds += double(ms) * 1e-3;
+                sweep_bytes += graph_bytes + panel_bytes;
+            }
+        };
         launches += 4;  // prepare, sky, panel in, panel out
-        k_prepare_panel<<<blocks_for(cells, 256), 256, 0, s>>>(S, p.bands, R, c0, P, p.rho, p.tau,
-                                                                p.emis, p.beam, p.dgeo, prho, ptau,
-                                                                pemis, pdir);
+        k_prepare_panel<<<blocks_for(cells, 256), 256, 0, s>>>(S, p.bands, R, c0, P, order, p.rho,
+                                                                p.tau, p.emis, p.beam, p.dgeo,
+                                                                prho, ptau, pemis, pdir);
         FCU_LAUNCH("k_prepare_panel");
-        k_panel_sky<<<1, 32, 0, s>>>(p.bands, R, c0, P, p.sky, psky);
+        k_panel_sky<<<1, 128, 0, s>>>(p.bands, R, c0, P, p.sky, psky);
         FCU_LAUNCH("k_panel_sky");
-        FCU_CHECK(cudaMemsetAsync(stats, 0, 128 * 4, s));
+        FCU_CHECK(cudaMemsetAsync(stats, 0, (2 * kMaxP + 16) * 4, s));
         const float* init = cfg.warm_start == FACETCU_WARM_GIVEN ? d_initial : nullptr;
         if (fp64)
             k_panel_in<double><<<blocks_for(cells, 256), 256, 0, s>>>(
-                init, S, R, c0, P, reinterpret_cast<double*>(x0));
+                init, S, R, c0, P, order, reinterpret_cast<double*>(x0));
         else
             k_panel_in<float><<<blocks_for(cells, 256), 256, 0, s>>>(
-                init, S, R, c0, P, reinterpret_cast<float*>(x0));
+                init, S, R, c0, P, order, reinterpret_cast<float*>(x0));
         FCU_LAUNCH("k_panel_in");
 
         uint32_t it = 0;
-        int cur = 0;  // buffer holding the current iterate (FP32/FP64 modes)
+        int cur = 0;
         uint32_t host_flag[3] = {0, 0, 0};
         if (!mixed) {
             while (it < max_it) {
@@ -489,7 +852,7 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
                             launch_sweep<float>(P, g, pp, reinterpret_cast<const float*>(in),
                                                 reinterpret_cast<float*>(out), stats, flag, s);
                     });
-                    k_check<<<1, 64, 0, s>>>(stats, flag, P, tol, sweep);
+                    k_check<<<1, kMaxP, 0, s>>>(stats, flag, P, tol, sweep);
                     FCU_LAUNCH("k_check");
                     ++launches;
                 }
@@ -498,8 +861,7 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
                 FCU_CHECK(cudaStreamSynchronize(s));
                 if (host_flag[0]) break;
             }
-            const uint32_t done_sweeps = host_flag[1];
-            cur = int(done_sweeps & 1u);
+            cur = int(host_flag[1] & 1u);
         } else {
             // FP32 sweep, then BF16 defect sweeps until the defect has shrunk
             // by `cycle_drop`, then a fresh FP32 sweep (residual correction).
@@ -507,9 +869,8 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
             float* X = reinterpret_cast<float*>(x0);
             float* Y = reinterpret_cast<float*>(x1);
             while (it < max_it) {
-                // FP32 residual sweep: Y = Q + K X; converged check on it.
                 timed_sweep([&] { launch_sweep<float>(P, g, pp, X, Y, stats, flag, s); });
-                k_check<<<1, 64, 0, s>>>(stats, flag, P, tol, it);
+                k_check<<<1, kMaxP, 0, s>>>(stats, flag, P, tol, it);
                 FCU_LAUNCH("k_check");
                 ++launches;
                 ++it;
@@ -526,8 +887,6 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
                 FCU_LAUNCH("k_defect_init");
                 ++launches;
                 std::swap(X, Y);  // X = newest FP32 iterate
-                // defect sweeps in batches; stop the cycle when the relative
-                // defect fell below start_change * cycle_drop or under tol
                 __nv_bfloat16* din = d0;
                 __nv_bfloat16* dout = d1;
                 bool cycle_done = false;
@@ -537,9 +896,9 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
                     for (uint32_t k = 0; k < batch; ++k) {
                         timed_sweep([&] { launch_defect(P, g, pp, din, dout, X, stats, flag, s); });
                         std::swap(din, dout);
-                        k_check<<<1, 64, 0, s>>>(stats, flag + 3, P,
-                                                 std::max(tol, start_change * cycle_drop),
-                                                 it + k);
+                        k_check<<<1, kMaxP, 0, s>>>(stats, flag + 3, P,
+                                                    std::max(tol, start_change * cycle_drop),
+                                                    it + k);
                         FCU_LAUNCH("k_check");
                         ++launches;
                     }
@@ -548,8 +907,6 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
                     FCU_CHECK(cudaStreamSynchronize(s));
                     if (sub_flag[0]) {
                         cycle_done = true;
-                        // sweeps after the one that met the cycle target still
-                        // ran (no early exit inside a batch); count them
                         FCU_CHECK(cudaMemsetAsync(flag + 3, 0, 12, s));
                     }
                 }
@@ -558,14 +915,12 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
             host_flag[1] = it;
         }
         const char* final_buf = cur ? x1 : x0;
-        if (fp64) {
-            // FP64 panels are returned rounded to float
+        if (fp64)
             k_panel_out<double><<<blocks_for(S, 32), 256, 0, s>>>(
-                reinterpret_cast<const double*>(final_buf), S, R, c0, P, d_out);
-        } else {
+                reinterpret_cast<const double*>(final_buf), S, R, c0, P, order, d_out);
+        else
             k_panel_out<float><<<blocks_for(S, 32), 256, 0, s>>>(
-                reinterpret_cast<const float*>(final_buf), S, R, c0, P, d_out);
-        }
+                reinterpret_cast<const float*>(final_buf), S, R, c0, P, order, d_out);
         FCU_LAUNCH("k_panel_out");
         worst_iterations = std::max(worst_iterations, host_flag[1]);
         float change;
@@ -573,6 +928,7 @@ int batched_solve(const DeviceGraph& gr, const BatchProblem& p, const facetcu_ba
         worst_change = std::max(worst_change, change);
         if (!host_flag[0]) all_converged = false;
         FCU_CHECK(cudaMemsetAsync(flag, 0, 32, s));
+        c0 += uint32_t(P);
     }
     FCU_CHECK(cudaStreamSynchronize(s));
     if (timed) {

@@ -144,6 +144,7 @@ void graph_from_pairs(uint64_t* d_pairs, size_t n, int side_bits, DeviceGraph& g
     FCU_LAUNCH("k_csr_fill");
     FCU_CHECK(cudaStreamSynchronize(s));
     g.packed_valid = false;
+    g.perm_valid = false;
 }
 
 void graph_closure(const DeviceGraph& g, float* closure, uint32_t* sampled, Workspace& ws,
@@ -169,6 +170,7 @@ bool graph_pack(DeviceGraph& g, Workspace& ws, cudaStream_t s)
 {
     (void)ws;
     if (g.packed_valid) return true;
+    g.perm_valid = false;
     if (g.surfaces > (1u << 22) || g.max_count >= 1024u) return false;
     uint32_t* p = static_cast<uint32_t*>(g.packed.reserve((g.nnz + 1) * 4));
     if (g.nnz) {

@@ -416,6 +416,7 @@ void hemisphere_graph(const facetcu_vertex* d_vertices, uint32_t facets, const L
     FCU_LAUNCH("k_hemi_compact");
     FCU_CHECK(cudaStreamSynchronize(s));
     g.packed_valid = false;
+    g.perm_valid = false;
     if (dropped) *dropped = host[0];
 }
 

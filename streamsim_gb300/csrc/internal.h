@@ -141,6 +141,12 @@ struct DeviceGraph {
     DeviceBuffer packed;        // nnz u32: neighbor | count << 22 (batched solver)
     bool packed_valid = false;
     uint32_t max_count = 0;
+    // Morton-ordered copy used by the batched solver: facets renumbered along
+    // a Morton curve of their centroids, rows and neighbour ids remapped.
+    bool perm_valid = false;
+    DeviceBuffer order;         // new facet -> old facet
+    DeviceBuffer rank;          // old facet -> new facet
+    DeviceBuffer p_rows, p_packed, p_denom, p_sky;
 };
 // Sort undirected pair keys, count runs, emit the symmetric CSR.
 void graph_from_pairs(uint64_t* d_pairs, size_t pair_count, int side_bits, DeviceGraph& g,
@@ -162,6 +168,8 @@ void incident_irradiance(const DeviceGraph& g, const facetcu_surface_optics* d_o
 
 // ---- batched solver (batched.cu) ---------------------------------------
 struct BatchProblem {
+    const facetcu_vertex* vertices;  // for the Morton order of the solver graph
+    float lo[3], hi[3];              // scene bounds
     uint32_t S;            // sides
     uint32_t bands, suns;  // R = bands * suns
     const float* rho;      // bands * S
@@ -193,6 +201,9 @@ struct Lbvh {
 };
 void lbvh_build(const facetcu_vertex* d_vertices, uint32_t facets, Lbvh& bvh, Workspace& ws,
                 cudaStream_t s);
+// Facet ids sorted by the 30-bit Morton code of their centroids in [lo, hi].
+void morton_order(const facetcu_vertex* d_vertices, uint32_t facets, const float lo[3],
+                  const float hi[3], uint32_t* d_order, Workspace& ws, cudaStream_t s);
 void hemisphere_graph(const facetcu_vertex* d_vertices, uint32_t facets, const Lbvh& bvh,
                       const float* d_uv, const float* d_dir, uint32_t rays, uint32_t sets,
                       uint32_t top_k, DeviceGraph& g, unsigned long long* dropped,

@@ -212,4 +212,26 @@ void lbvh_build(const facetcu_vertex* d_vertices, uint32_t n, Lbvh& bvh, Workspa
     FCU_CHECK(cudaStreamSynchronize(s));
 }
 
+void morton_order(const facetcu_vertex* d_vertices, uint32_t n, const float lo[3],
+                  const float hi[3], uint32_t* d_order, Workspace& ws, cudaStream_t s)
+{
+    Bounds sb;
+    for (int a = 0; a < 3; ++a) {
+        sb.lo[a] = lo[a];
+        sb.hi[a] = hi[a];
+    }
+    DeviceBuffer keys_a, keys_b, ids_b, boxes;
+    uint64_t* ka = static_cast<uint64_t*>(keys_a.reserve(size_t(n) * 8));
+    uint64_t* kb = static_cast<uint64_t*>(keys_b.reserve(size_t(n) * 8));
+    uint32_t* ia = d_order;
+    uint32_t* ib = static_cast<uint32_t*>(ids_b.reserve(size_t(n) * 4));
+    float* lb = static_cast<float*>(boxes.reserve(size_t(n) * 24));
+    k_morton<<<grid(n, 256), 256, 0, s>>>(d_vertices, n, sb, ka, ia, lb, 0.0f);
+    FCU_LAUNCH("k_morton");
+    radix_sort_u64(ka, kb, ia, ib, n, 30, ws, s);
+    if (ia != d_order)
+        FCU_CHECK(cudaMemcpyAsync(d_order, ia, size_t(n) * 4, cudaMemcpyDeviceToDevice, s));
+    FCU_CHECK(cudaStreamSynchronize(s));
+}
+
 }  // namespace facetcu

@@ -74,10 +74,17 @@ def test_hemisphere_sunlit_bit_exact(oracle):
 
 
 def test_hemisphere_view_factors_statistics(oracle):
-    """Against geometry: an isolated horizontal soil sees only sky upwards;
-    reciprocity A_i F_ij ~ A_j F_ji holds in aggregate (Monte Carlo)."""
-    sc = scenes.config1(seed=4, leaves=400, grid=8)
-    rays = 256
+    """Against geometry: downward soil sides see only sky; reciprocity
+    A_i F_ij ~ A_j F_ji holds in aggregate between panels and soil (Monte
+    Carlo; large panels keep the hit counts high)."""
+    rng = np.random.default_rng(4)
+    n = 40
+    centres = np.stack([rng.uniform(-3, 3, n), rng.uniform(0.5, 2.0, n), rng.uniform(-3, 3, n)], 1)
+    normals = scenes.uniform_sphere(n, rng)
+    panels = scenes._triangles_to_vertices(*scenes.equilateral(centres, normals, 1.2, rng))
+    soil = scenes._triangles_to_vertices(*scenes.soil_grid(-5, 5, -5, 5, 8, 8))
+    sc = scenes.Scene(np.concatenate([panels, soil]), len(panels) // 3, "panels")
+    rays = 512
     uv, dirs = scenes.hemisphere_samples(rays, 16, seed=11)
     m = _model(sc.vertices)
     m.buildHemisphereGraph(uv, dirs, rays, rays, 16)
@@ -89,14 +96,12 @@ def test_hemisphere_view_factors_statistics(oracle):
     v = sc.vertices.reshape(-1, 3, 6)[:, :, :3].astype(np.float64)
     area = 0.5 * np.linalg.norm(np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]), axis=1)
     A = np.repeat(area, 2)
-    # reciprocity in aggregate: area-weighted exchange leaf -> soil equals
-    # soil -> leaf up to Monte Carlo noise (pairs are too noisy at 256 rays)
-    leaf = np.zeros(S, bool)
-    leaf[:2 * sc.leaf_count] = True
-    to_soil = (A[leaf, None] * F[np.ix_(leaf, ~leaf)]).sum()
-    to_leaf = (A[~leaf, None] * F[np.ix_(~leaf, leaf)]).sum()
-    assert abs(to_soil - to_leaf) / to_soil < 0.05
-    # bottom sides of soil (facing down) see nothing but their own plane: all sky
+    obj = np.zeros(S, bool)
+    obj[:2 * sc.leaf_count] = True
+    to_soil = (A[obj, None] * F[np.ix_(obj, ~obj)]).sum()
+    to_obj = (A[~obj, None] * F[np.ix_(~obj, obj)]).sum()
+    assert abs(to_soil - to_obj) / to_soil < 0.05
+    # downward soil sides see nothing: all sky
     soil_bottom = np.arange(2 * sc.leaf_count + 1, S, 2)
     assert np.all(sky[soil_bottom] == den[soil_bottom])
     m.close()

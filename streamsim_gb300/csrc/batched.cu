@@ -138,126 +138,79 @@ __device__ __forceinline__ Acc gather_narrow(const GraphView& g, uint32_t s, con
     return acc;
 }
 
-// ---- wide panels (P = 32 * CPL): lane owns CPL adjacent columns -----------
-template <int CPL> struct RowF32;
-template <> struct RowF32<1> {
-    static __device__ __forceinline__ void load(const float* X, uint32_t nb, int lane, float* v)
+// ---- wide panels (P = 32, 64, 128) ---------------------------------------
+// Each lane moves 16 bytes of a neighbour row per load: CPL = 4 FP32 or 8
+// BF16 columns.  L = P / CPL lanes cover one row, so a warp gathers
+// G = 32 / L edges per load instruction (e.g. P = 64 BF16: 8 lanes per
+// 128-byte row, 4 edges at once); the G partial sums are folded with
+// shuffles at the end of the row and the first L lanes own the result.
+template <bool kBF16> struct Vec16;
+template <> struct Vec16<false> {  // 4 x FP32
+    static constexpr int kCols = 4;
+    static __device__ __forceinline__ void load(const void* X, size_t idx16, float* v)
     {
-        v[0] = __ldg(X + size_t(nb) * 32 + lane);
-    }
-};
-template <> struct RowF32<2> {
-    static __device__ __forceinline__ void load(const float* X, uint32_t nb, int lane, float* v)
-    {
-        const float2 q = __ldg(reinterpret_cast<const float2*>(X) + size_t(nb) * 32 + lane);
-        v[0] = q.x;
-        v[1] = q.y;
-    }
-};
-template <> struct RowF32<4> {
-    static __device__ __forceinline__ void load(const float* X, uint32_t nb, int lane, float* v)
-    {
-        const float4 q = __ldg(reinterpret_cast<const float4*>(X) + size_t(nb) * 32 + lane);
+        const float4 q = __ldg(reinterpret_cast<const float4*>(X) + idx16);
         v[0] = q.x;
         v[1] = q.y;
         v[2] = q.z;
         v[3] = q.w;
     }
 };
-template <int CPL> struct RowBF16;
-template <> struct RowBF16<1> {
-    static __device__ __forceinline__ void load(const __nv_bfloat16* X, uint32_t nb, int lane, float* v)
+template <> struct Vec16<true> {  // 8 x BF16
+    static constexpr int kCols = 8;
+    static __device__ __forceinline__ void load(const void* X, size_t idx16, float* v)
     {
-        const unsigned short h = __ldg(reinterpret_cast<const unsigned short*>(X) + size_t(nb) * 32 + lane);
-        v[0] = __uint_as_float(uint32_t(h) << 16);
-    }
-};
-template <> struct RowBF16<2> {
-    static __device__ __forceinline__ void load(const __nv_bfloat16* X, uint32_t nb, int lane, float* v)
-    {
-        const uint32_t w = __ldg(reinterpret_cast<const uint32_t*>(X) + size_t(nb) * 32 + lane);
-        v[0] = __uint_as_float(w << 16);
-        v[1] = __uint_as_float(w & 0xFFFF0000u);
-    }
-};
-template <> struct RowBF16<4> {
-    static __device__ __forceinline__ void load(const __nv_bfloat16* X, uint32_t nb, int lane, float* v)
-    {
-        const uint2 w = __ldg(reinterpret_cast<const uint2*>(X) + size_t(nb) * 32 + lane);
-        v[0] = __uint_as_float(w.x << 16);
-        v[1] = __uint_as_float(w.x & 0xFFFF0000u);
-        v[2] = __uint_as_float(w.y << 16);
-        v[3] = __uint_as_float(w.y & 0xFFFF0000u);
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(X) + idx16);
+        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            v[2 * i] = __uint_as_float(w[i] << 16);
+            v[2 * i + 1] = __uint_as_float(w[i] & 0xFFFF0000u);
+        }
     }
 };
 
-template <int CPL, bool kBF16>
-__device__ __forceinline__ void load_row(const void* X, uint32_t nb, int lane, float* v)
+// acc[k] += sum over edges e of side s of count_e * X[n_e][col0 + k], where
+// col0 = (lane % L) * CPL; valid in every lane after the fold (lanes of the
+// same sub-index hold the same sums).
+template <int P, bool kBF16>
+__device__ __forceinline__ void gather_split(const uint32_t* __restrict__ rows,
+                                             const uint32_t* __restrict__ packed,
+                                             const facetcu_csr_edge* __restrict__ edges,
+                                             uint32_t s, const void* X, int lane, float* acc)
 {
-    if constexpr (kBF16)
-        RowBF16<CPL>::load(static_cast<const __nv_bfloat16*>(X), nb, lane, v);
-    else
-        RowF32<CPL>::load(static_cast<const float*>(X), nb, lane, v);
-}
-
-// acc[k] += sum over edges of s of count * X[n][lane*CPL + k].  Packed
-// 4-byte edges when `packed` is set (one shuffle per edge), else the 8-byte
-// {neighbor, count} records (two shuffles per edge).
-template <int CPL, bool kBF16>
-__device__ __forceinline__ void gather_wide(const uint32_t* __restrict__ rows,
-                                            const uint32_t* __restrict__ packed,
-                                            const facetcu_csr_edge* __restrict__ edges, uint32_t s,
-                                            const void* X, int lane, float* acc)
-{
-    constexpr int U = 8;
+    constexpr int CPL = Vec16<kBF16>::kCols;
+    constexpr int L = P / CPL;  // lanes per row = 16-byte vectors per row
+    constexpr int G = 32 / L;   // edges per load instruction
+    constexpr int U = 4;
+    const int grp = lane / L, sub = lane % L;
     const uint32_t start = __ldg(rows + s), end = __ldg(rows + s + 1);
-    uint32_t base = start;
-    if (!packed) {
-        for (; base < end; base += 32) {
-            const uint32_t n = min(32u, end - base);
-            uint2 e = make_uint2(0u, 0u);
-            if (uint32_t(lane) < n) e = __ldg(reinterpret_cast<const uint2*>(edges) + base + lane);
-            for (uint32_t j = 0; j < n; ++j) {
-                const uint32_t nb = __shfl_sync(0xffffffffu, e.x, int(j));
-                const float c = float(__shfl_sync(0xffffffffu, e.y, int(j)));
-                float v[CPL];
-                load_row<CPL, kBF16>(X, nb, lane, v);
-#pragma unroll
-                for (int k = 0; k < CPL; ++k) acc[k] += c * v[k];
+    for (uint32_t base = start; base < end; base += 32) {
+        const uint32_t n = min(32u, end - base);
+        uint32_t nbv = 0;
+        float cv = 0.0f;
+        if (uint32_t(lane) < n) {
+            if (packed) {
+                const uint32_t p = __ldg(packed + base + lane);
+                nbv = p & kNeighborMask;
+                cv = float(p >> 22);
+            } else {
+                const uint2 e = __ldg(reinterpret_cast<const uint2*>(edges) + base + lane);
+                nbv = e.x;
+                cv = float(e.y);
             }
         }
-        return;
-    }
-    for (; base + 32 <= end; base += 32) {
-        const uint32_t pk = __ldg(packed + base + lane);
-#pragma unroll
-        for (int j = 0; j < 32; j += U) {
+        for (uint32_t j = 0; j < n; j += G * U) {
             float v[U][CPL];
             float c[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const uint32_t p = __shfl_sync(0xffffffffu, pk, j + u);
-                c[u] = float(p >> 22);
-                load_row<CPL, kBF16>(X, p & kNeighborMask, lane, v[u]);
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u)
-#pragma unroll
-                for (int k = 0; k < CPL; ++k) acc[k] += c[u] * v[u][k];
-        }
-    }
-    if (base < end) {
-        const uint32_t n = end - base;
-        const uint32_t pk = uint32_t(lane) < n ? __ldg(packed + base + lane) : 0u;
-        for (uint32_t j = 0; j < n; j += U) {
-            float v[U][CPL];
-            float c[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const uint32_t p = __shfl_sync(0xffffffffu, pk, int((j + u) & 31u));
-                if (j + u < n) {
-                    c[u] = float(p >> 22);
-                    load_row<CPL, kBF16>(X, p & kNeighborMask, lane, v[u]);
+                const uint32_t idx = j + u * G + grp;
+                const int src = int(idx & 31u);
+                const uint32_t nb = __shfl_sync(0xffffffffu, nbv, src);
+                c[u] = __shfl_sync(0xffffffffu, cv, src);
+                if (idx < n) {
+                    Vec16<kBF16>::load(X, size_t(nb) * L + sub, v[u]);
                 } else {
                     c[u] = 0.0f;
 #pragma unroll
@@ -270,19 +223,54 @@ __device__ __forceinline__ void gather_wide(const uint32_t* __restrict__ rows,
                 for (int k = 0; k < CPL; ++k) acc[k] += c[u] * v[u][k];
         }
     }
+#pragma unroll
+    for (int o = L; o < 32; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
 }
 
-// CTA-level max over warps, then one atomic per column.
+// Dynamic hand-out of facet chunks (contiguous in Morton order); the counter
+// is reset by k_check after every sweep.
+constexpr uint32_t kChunk = 8;
+__device__ __forceinline__ uint32_t next_chunk(uint32_t* counter, int lane)
+{
+    uint32_t c = 0;
+    if (lane == 0) c = atomicAdd(counter, 1u);
+    return __shfl_sync(0xffffffffu, c, 0);
+}
+
+__device__ __forceinline__ void load4(const float* p, float* v)
+{
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+}
+__device__ __forceinline__ void store4(float* p, const float* v)
+{
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+// CTA-level max over warps, then one atomic per column; columns [col0,
+// col0 + n) of the lane hold md/mb (lanes with n = 0 contribute nothing).
 template <int NC>
-__device__ __forceinline__ void publish_stats(const float* md, const float* mb, int lane, int P,
-                                              uint32_t* stats)
+__device__ __forceinline__ void publish_cols(const float* md, const float* mb, int col0, bool own,
+                                             int P, uint32_t* stats)
 {
     __shared__ float s_md[kWarps][kMaxP], s_mb[kWarps][kMaxP];
     const int warp = threadIdx.x >> 5;
+    for (int c = (threadIdx.x & 31); c < kMaxP; c += 32) {
+        s_md[warp][c] = 0.0f;
+        s_mb[warp][c] = 0.0f;
+    }
+    __syncwarp();
+    if (own) {
 #pragma unroll
-    for (int k = 0; k < NC; ++k) {
-        s_md[warp][lane * NC + k] = md[k];
-        s_mb[warp][lane * NC + k] = mb[k];
+        for (int k = 0; k < NC; ++k) {
+            s_md[warp][col0 + k] = md[k];
+            s_mb[warp][col0 + k] = mb[k];
+        }
     }
     __syncthreads();
     for (int c = threadIdx.x; c < P; c += blockDim.x) {
@@ -296,110 +284,162 @@ __device__ __forceinline__ void publish_stats(const float* md, const float* mb, 
     }
 }
 
+// Narrow-kernel statistics: lane c < P holds column c.
+template <int NC>
+__device__ __forceinline__ void publish_stats(const float* md, const float* mb, int lane, int P,
+                                              uint32_t* stats)
+{
+    publish_cols<NC>(md, mb, lane * NC, lane < P, P, stats);
+}
+
 // One full FP32 sweep B_out = Q + K B_in over a wide panel.
-template <int CPL>
-__global__ void __launch_bounds__(kWarps * 32) k_sweep_wide(GraphView g, PanelParams pp,
+template <int P>
+__global__ void __launch_bounds__(kWarps * 32, 3) k_sweep_wide(GraphView g, PanelParams pp,
                                                             const float* __restrict__ Bin,
                                                             float* __restrict__ Bout,
-                                                            uint32_t* stats, const uint32_t* done)
+                                                            uint32_t* stats, uint32_t* counter,
+                                                            const uint32_t* done)
 {
     if (*done) return;
-    constexpr int P = 32 * CPL;
+    constexpr int CPL = 4;
+    constexpr int L = P / CPL;
     const int lane = threadIdx.x & 31;
-    float md[CPL], mb[CPL], L[CPL];
+    const bool owner = lane < L;
+    const int col0 = (lane % L) * CPL;
+    float md[CPL], mb[CPL], Lsky[CPL];
 #pragma unroll
     for (int k = 0; k < CPL; ++k) {
         md[k] = 0.0f;
         mb[k] = 0.0f;
-        L[k] = pp.skyL[lane * CPL + k];
+        Lsky[k] = pp.skyL[col0 + k];
     }
-    uint32_t fb, fe;
-    warp_range(g.facets, fb, fe);
-    for (uint32_t f = fb; f < fe; ++f) {
-        float h[2][CPL];
+    const uint32_t chunks = (g.facets + kChunk - 1) / kChunk;
+    for (uint32_t ch = next_chunk(counter, lane); ch < chunks; ch = next_chunk(counter, lane)) {
+        const uint32_t fe = min(g.facets, (ch + 1) * kChunk);
+        for (uint32_t f = ch * kChunk; f < fe; ++f) {
+            float h[2][CPL];
 #pragma unroll
-        for (int side = 0; side < 2; ++side) {
-            const uint32_t s = 2u * f + side;
-            float acc[CPL];
+            for (int side = 0; side < 2; ++side) {
+                const uint32_t s = 2u * f + side;
+                float acc[CPL];
 #pragma unroll
-            for (int k = 0; k < CPL; ++k) acc[k] = 0.0f;
-            gather_wide<CPL, false>(g.rows, g.packed, g.edges, s, Bin, lane, acc);
-            const uint32_t d = __ldg(g.denom + s);
-            const float skyc = float(__ldg(g.skyc + s));
+                for (int k = 0; k < CPL; ++k) acc[k] = 0.0f;
+                gather_split<P, false>(g.rows, g.packed, g.edges, s, Bin, lane, acc);
+                const uint32_t d = __ldg(g.denom + s);
+                const float skyc = float(__ldg(g.skyc + s));
+                float dir[CPL];
+                load4(pp.direct + size_t(s) * P + col0, dir);
 #pragma unroll
-            for (int k = 0; k < CPL; ++k) {
-                const float dir = pp.direct[size_t(s) * P + lane * CPL + k];
-                h[side][k] = (d != 0u ? (skyc * L[k] + acc[k]) / float(d) : L[k]) + dir;
+                for (int k = 0; k < CPL; ++k)
+                    h[side][k] = (d != 0u ? (skyc * Lsky[k] + acc[k]) / float(d) : Lsky[k]) + dir[k];
+            }
+            if (owner) {
+                const size_t i0 = size_t(2u * f) * P + col0, i1 = i0 + P;
+                float e0[CPL], e1[CPL], r0[CPL], r1[CPL], t0[CPL], t1[CPL], o0[CPL], o1[CPL];
+                float b0[CPL], b1[CPL];
+                load4(pp.emis + i0, e0);
+                load4(pp.emis + i1, e1);
+                load4(pp.rho + i0, r0);
+                load4(pp.rho + i1, r1);
+                load4(pp.tau + i0, t0);
+                load4(pp.tau + i1, t1);
+                load4(Bin + i0, o0);
+                load4(Bin + i1, o1);
+#pragma unroll
+                for (int k = 0; k < CPL; ++k) {
+                    b0[k] = e0[k] + r0[k] * h[0][k] + t0[k] * h[1][k];
+                    b1[k] = e1[k] + r1[k] * h[1][k] + t1[k] * h[0][k];
+                    md[k] = fmaxf(md[k], fmaxf(fabsf(b0[k] - o0[k]), fabsf(b1[k] - o1[k])));
+                    mb[k] = fmaxf(mb[k], fmaxf(fabsf(b0[k]), fabsf(b1[k])));
+                }
+                store4(Bout + i0, b0);
+                store4(Bout + i1, b1);
             }
         }
-#pragma unroll
-        for (int k = 0; k < CPL; ++k) {
-            const size_t i0 = size_t(2u * f) * P + lane * CPL + k, i1 = i0 + P;
-            const float b0 = pp.emis[i0] + pp.rho[i0] * h[0][k] + pp.tau[i0] * h[1][k];
-            const float b1 = pp.emis[i1] + pp.rho[i1] * h[1][k] + pp.tau[i1] * h[0][k];
-            const float o0 = Bin[i0], o1 = Bin[i1];
-            Bout[i0] = b0;
-            Bout[i1] = b1;
-            md[k] = fmaxf(md[k], fmaxf(fabsf(b0 - o0), fabsf(b1 - o1)));
-            mb[k] = fmaxf(mb[k], fmaxf(fabsf(b0), fabsf(b1)));
-        }
     }
-    publish_stats<CPL>(md, mb, lane, P, stats);
+    publish_cols<CPL>(md, mb, col0, owner, P, stats);
 }
 
 // Defect sweep over a wide panel: d_out = K d_in (BF16 in and out, FP32
 // accumulation), X += d_out.  Stats: max|d_out|, max|X|.
-template <int CPL>
-__global__ void __launch_bounds__(kWarps * 32) k_defect_wide(GraphView g, PanelParams pp,
+template <int P>
+__global__ void __launch_bounds__(kWarps * 32, 3) k_defect_wide(GraphView g, PanelParams pp,
                                                              const __nv_bfloat16* __restrict__ Din,
                                                              __nv_bfloat16* __restrict__ Dout,
                                                              float* __restrict__ X, uint32_t* stats,
+                                                             uint32_t* counter,
                                                              const uint32_t* done)
 {
     if (*done) return;
-    constexpr int P = 32 * CPL;
+    constexpr int CPL = 8;
+    constexpr int L = P / CPL;
     const int lane = threadIdx.x & 31;
+    const bool owner = lane < L;
+    const int col0 = (lane % L) * CPL;
     float md[CPL], mb[CPL];
 #pragma unroll
     for (int k = 0; k < CPL; ++k) {
         md[k] = 0.0f;
         mb[k] = 0.0f;
     }
-    uint32_t fb, fe;
-    warp_range(g.facets, fb, fe);
-    for (uint32_t f = fb; f < fe; ++f) {
-        float h[2][CPL];
+    const uint32_t chunks = (g.facets + kChunk - 1) / kChunk;
+    for (uint32_t ch = next_chunk(counter, lane); ch < chunks; ch = next_chunk(counter, lane)) {
+        const uint32_t fe = min(g.facets, (ch + 1) * kChunk);
+        for (uint32_t f = ch * kChunk; f < fe; ++f) {
+            float h[2][CPL];
 #pragma unroll
-        for (int side = 0; side < 2; ++side) {
-            const uint32_t s = 2u * f + side;
-            float acc[CPL];
+            for (int side = 0; side < 2; ++side) {
+                const uint32_t s = 2u * f + side;
+                float acc[CPL];
 #pragma unroll
-            for (int k = 0; k < CPL; ++k) acc[k] = 0.0f;
-            gather_wide<CPL, true>(g.rows, g.packed, g.edges, s, Din, lane, acc);
-            const uint32_t d = __ldg(g.denom + s);
-            const float inv = d ? 1.0f / float(d) : 0.0f;
+                for (int k = 0; k < CPL; ++k) acc[k] = 0.0f;
+                gather_split<P, true>(g.rows, g.packed, g.edges, s, Din, lane, acc);
+                const uint32_t d = __ldg(g.denom + s);
+                const float inv = d ? 1.0f / float(d) : 0.0f;
 #pragma unroll
-            for (int k = 0; k < CPL; ++k) h[side][k] = acc[k] * inv;
-        }
-        float d0[CPL], d1[CPL];
-        const size_t base0 = size_t(2u * f) * P + lane * CPL, base1 = base0 + P;
+                for (int k = 0; k < CPL; ++k) h[side][k] = acc[k] * inv;
+            }
+            if (owner) {
+                const size_t i0 = size_t(2u * f) * P + col0, i1 = i0 + P;
+                float r0[CPL], r1[CPL], t0[CPL], t1[CPL], x0[CPL], x1[CPL];
 #pragma unroll
-        for (int k = 0; k < CPL; ++k) {
-            d0[k] = pp.rho[base0 + k] * h[0][k] + pp.tau[base0 + k] * h[1][k];
-            d1[k] = pp.rho[base1 + k] * h[1][k] + pp.tau[base1 + k] * h[0][k];
-            const float x0 = X[base0 + k] + d0[k], x1 = X[base1 + k] + d1[k];
-            X[base0 + k] = x0;
-            X[base1 + k] = x1;
-            md[k] = fmaxf(md[k], fmaxf(fabsf(d0[k]), fabsf(d1[k])));
-            mb[k] = fmaxf(mb[k], fmaxf(fabsf(x0), fabsf(x1)));
-        }
+                for (int q = 0; q < CPL; q += 4) {
+                    load4(pp.rho + i0 + q, r0 + q);
+                    load4(pp.rho + i1 + q, r1 + q);
+                    load4(pp.tau + i0 + q, t0 + q);
+                    load4(pp.tau + i1 + q, t1 + q);
+                    load4(X + i0 + q, x0 + q);
+                    load4(X + i1 + q, x1 + q);
+                }
+                uint32_t w0[CPL / 2], w1[CPL / 2];
 #pragma unroll
-        for (int k = 0; k < CPL; ++k) {
-            Dout[base0 + k] = __float2bfloat16_rn(d0[k]);
-            Dout[base1 + k] = __float2bfloat16_rn(d1[k]);
+                for (int k = 0; k < CPL; k += 2) {
+                    float d0[2], d1[2];
+#pragma unroll
+                    for (int m = 0; m < 2; ++m) {
+                        d0[m] = r0[k + m] * h[0][k + m] + t0[k + m] * h[1][k + m];
+                        d1[m] = r1[k + m] * h[1][k + m] + t1[k + m] * h[0][k + m];
+                        x0[k + m] += d0[m];
+                        x1[k + m] += d1[m];
+                        md[k + m] = fmaxf(md[k + m], fmaxf(fabsf(d0[m]), fabsf(d1[m])));
+                        mb[k + m] = fmaxf(mb[k + m], fmaxf(fabsf(x0[k + m]), fabsf(x1[k + m])));
+                    }
+                    w0[k / 2] = uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(d0[0]))) |
+                                (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(d0[1]))) << 16);
+                    w1[k / 2] = uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(d1[0]))) |
+                                (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(d1[1]))) << 16);
+                }
+#pragma unroll
+                for (int q = 0; q < CPL; q += 4) {
+                    store4(X + i0 + q, x0 + q);
+                    store4(X + i1 + q, x1 + q);
+                }
+                *reinterpret_cast<uint4*>(Dout + i0) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+                *reinterpret_cast<uint4*>(Dout + i1) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+            }
         }
     }
-    publish_stats<CPL>(md, mb, lane, P, stats);
+    publish_cols<CPL>(md, mb, col0, owner, P, stats);
 }
 
 // Narrow-panel sweep (FP32 or FP64 state; also used for the FP64 truth).
@@ -493,7 +533,8 @@ __global__ void k_defect_init(const float* Bold, const float* Bnew, __nv_bfloat1
 // Convergence check after sweep `it` (0-based): every column must satisfy
 // max|dB| <= tol * max|B|.  flag[0] = done, flag[1] = sweeps run, flag[2] =
 // max relative change bits of the last sweep.  Clears the stats.
-__global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint32_t it)
+__global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint32_t it,
+                        uint32_t* counter)
 {
     __shared__ int all_ok;
     __shared__ float worst;
@@ -517,6 +558,7 @@ __global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint3
         if (all_ok) flag[0] = 1;
     }
     for (int i = threadIdx.x; i < 2 * kMaxP; i += blockDim.x) stats[i] = 0;
+    if (threadIdx.x == 0) *counter = 0u;
 }
 
 __device__ __forceinline__ uint32_t old_side(const uint32_t* order, uint32_t s)
@@ -635,34 +677,44 @@ __global__ void k_set_last(uint32_t* rows, uint32_t n, const unsigned long long*
 
 inline unsigned blocks_for(size_t n, unsigned b) { return unsigned((n + b - 1) / b); }
 
-int persistent_grid()
+template <typename K>
+int grid_for(K kernel)
 {
-    static int grid = 0;
-    if (!grid) {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        grid = (sms > 0 ? sms : 148) * 6;  // 6 CTAs x 8 warps = 48 warps per SM
-    }
-    return grid;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarps * 32, 0);
+    return std::max(1, sms) * std::max(1, per_sm);
 }
 
 template <typename T>
 void launch_sweep(int P, const GraphView& g, const PanelParams& pp, const T* in, T* out,
-                  uint32_t* stats, const uint32_t* done, cudaStream_t s)
+                  uint32_t* stats, uint32_t* counter, const uint32_t* done, cudaStream_t s)
 {
-    const int grid = persistent_grid();
     if constexpr (sizeof(T) == 4) {
         if (P >= 32) {
             switch (P) {
-            case 32: k_sweep_wide<1><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, done); break;
-            case 64: k_sweep_wide<2><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, done); break;
-            default: k_sweep_wide<4><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, done); break;
+            case 32: {
+                static const int grid = grid_for(k_sweep_wide<32>);
+                k_sweep_wide<32><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, counter, done);
+                break;
+            }
+            case 64: {
+                static const int grid = grid_for(k_sweep_wide<64>);
+                k_sweep_wide<64><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, counter, done);
+                break;
+            }
+            default: {
+                static const int grid = grid_for(k_sweep_wide<128>);
+                k_sweep_wide<128><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, counter, done);
+                break;
+            }
             }
             FCU_LAUNCH("k_sweep_wide");
             return;
         }
     }
+    static const int grid = grid_for(k_sweep<32, T>);
     switch (P) {
     case 1: k_sweep<1, T><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, done); break;
     case 2: k_sweep<2, T><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, done); break;
@@ -675,19 +727,31 @@ void launch_sweep(int P, const GraphView& g, const PanelParams& pp, const T* in,
 }
 
 void launch_defect(int P, const GraphView& g, const PanelParams& pp, const __nv_bfloat16* in,
-                   __nv_bfloat16* out, float* X, uint32_t* stats, const uint32_t* done,
-                   cudaStream_t s)
+                   __nv_bfloat16* out, float* X, uint32_t* stats, uint32_t* counter,
+                   const uint32_t* done, cudaStream_t s)
 {
-    const int grid = persistent_grid();
     if (P >= 32) {
         switch (P) {
-        case 32: k_defect_wide<1><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, done); break;
-        case 64: k_defect_wide<2><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, done); break;
-        default: k_defect_wide<4><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, done); break;
+        case 32: {
+            static const int grid = grid_for(k_defect_wide<32>);
+            k_defect_wide<32><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, counter, done);
+            break;
+        }
+        case 64: {
+            static const int grid = grid_for(k_defect_wide<64>);
+            k_defect_wide<64><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, counter, done);
+            break;
+        }
+        default: {
+            static const int grid = grid_for(k_defect_wide<128>);
+            k_defect_wide<128><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, counter, done);
+            break;
+        }
         }
         FCU_LAUNCH("k_defect_wide");
         return;
     }
+    static const int grid = grid_for(k_sweep_defect<32>);
     switch (P) {
     case 1: k_sweep_defect<1><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, done); break;
     case 2: k_sweep_defect<2><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, done); break;
@@ -769,6 +833,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
     float* prm = static_cast<float*>(st.q.reserve(cells_max * 4 * 4 + kMaxP * 4));
     uint32_t* stats = static_cast<uint32_t*>(st.colstats.reserve((2 * kMaxP + 16) * 4));
     uint32_t* flag = stats + 2 * kMaxP;
+    uint32_t* counter = flag + 8;
     __nv_bfloat16* dbuf = nullptr;
     if (mixed) dbuf = static_cast<__nv_bfloat16*>(st.half.reserve(cells_max * 2 * 2));
 
@@ -847,12 +912,14 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                     timed_sweep([&] {
                         if (fp64)
                             launch_sweep<double>(P, g, pp, reinterpret_cast<const double*>(in),
-                                                 reinterpret_cast<double*>(out), stats, flag, s);
+                                                 reinterpret_cast<double*>(out), stats, counter,
+                                                 flag, s);
                         else
                             launch_sweep<float>(P, g, pp, reinterpret_cast<const float*>(in),
-                                                reinterpret_cast<float*>(out), stats, flag, s);
+                                                reinterpret_cast<float*>(out), stats, counter,
+                                                flag, s);
                     });
-                    k_check<<<1, kMaxP, 0, s>>>(stats, flag, P, tol, sweep);
+                    k_check<<<1, kMaxP, 0, s>>>(stats, flag, P, tol, sweep, counter);
                     FCU_LAUNCH("k_check");
                     ++launches;
                 }
@@ -869,8 +936,8 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
             float* X = reinterpret_cast<float*>(x0);
             float* Y = reinterpret_cast<float*>(x1);
             while (it < max_it) {
-                timed_sweep([&] { launch_sweep<float>(P, g, pp, X, Y, stats, flag, s); });
-                k_check<<<1, kMaxP, 0, s>>>(stats, flag, P, tol, it);
+                timed_sweep([&] { launch_sweep<float>(P, g, pp, X, Y, stats, counter, flag, s); });
+                k_check<<<1, kMaxP, 0, s>>>(stats, flag, P, tol, it, counter);
                 FCU_LAUNCH("k_check");
                 ++launches;
                 ++it;
@@ -894,11 +961,13 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                     const uint32_t batch = std::min(check_every, max_it - it);
                     uint32_t sub_flag[3];
                     for (uint32_t k = 0; k < batch; ++k) {
-                        timed_sweep([&] { launch_defect(P, g, pp, din, dout, X, stats, flag, s); });
+                        timed_sweep([&] {
+                            launch_defect(P, g, pp, din, dout, X, stats, counter, flag, s);
+                        });
                         std::swap(din, dout);
                         k_check<<<1, kMaxP, 0, s>>>(stats, flag + 3, P,
                                                     std::max(tol, start_change * cycle_drop),
-                                                    it + k);
+                                                    it + k, counter);
                         FCU_LAUNCH("k_check");
                         ++launches;
                     }
@@ -927,7 +996,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
         std::memcpy(&change, &host_flag[2], 4);
         worst_change = std::max(worst_change, change);
         if (!host_flag[0]) all_converged = false;
-        FCU_CHECK(cudaMemsetAsync(flag, 0, 32, s));
+        FCU_CHECK(cudaMemsetAsync(flag, 0, 48, s));
         c0 += uint32_t(P);
     }
     FCU_CHECK(cudaStreamSynchronize(s));

@@ -301,15 +301,17 @@ def run_gpu(args, rank, world, local):
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     achieved = rt["sweep_bytes"] / max(rt["sweep_seconds"], 1e-12) / 1e9
+    panel = min(128, 1 << (B - 1).bit_length())
+    kname = (f"k_defect_wide<{panel}>" if prec == fc.PRECISION_MIXED else f"k_sweep_wide<{panel}>")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None,
-                "kernel": "k_sweep_defect<32>" if prec == fc.PRECISION_MIXED else "k_sweep<32,float>",
-                "avg_sweep_ms": rt["sweep_seconds"] / max(rt["sweeps"], 1) * 1e3,
-                "algorithmic_bytes_per_sweep": rt["sweep_bytes"] / max(rt["sweeps"], 1),
-                "peak_source": "measured" if peaks else "fallback"}
+                "frac": achieved / hbm, "traffic": None, "kernel": kname,
+                "launches_timed": rt["timed_sweeps"],
+                "avg_launch_ms": rt["sweep_seconds"] / max(rt["timed_sweeps"], 1) * 1e3,
+                "algorithmic_bytes_per_launch": rt["sweep_bytes"] / max(rt["timed_sweeps"], 1),
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"}
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "sweep_traffic.json")))
-        roofline["traffic"] = prof.get("bytes_per_sweep")
+        roofline["traffic"] = prof.get(kname)
     except (OSError, ValueError):
         pass
 

@@ -229,8 +229,10 @@ typedef struct {
     double seconds;             /* device time of the solve (CUDA events) */
     uint32_t kernel_launches;   /* kernels the solve launched */
     uint32_t sweeps;            /* sweep kernels run, summed over panels */
-    double sweep_seconds;       /* summed sweep-kernel time (TIME_SWEEPS only) */
+    double sweep_seconds;       /* summed time of the dominant sweep kernel (TIME_SWEEPS) */
     double sweep_bytes;         /* algorithmic HBM bytes of those sweeps */
+    uint32_t timed_sweeps;      /* number of sweeps in sweep_seconds */
+    uint32_t reserved;
 } facetcu_batch_result;
 int facetcu_solve_batched(facetcu_context *ctx, const facetcu_batch_config *config,
                           const float *reflectance, const float *transmittance,

@@ -837,7 +837,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
     __nv_bfloat16* dbuf = nullptr;
     if (mixed) dbuf = static_cast<__nv_bfloat16*>(st.half.reserve(cells_max * 2 * 2));
 
-    uint32_t worst_iterations = 0, corrections = 0, launches = 0, sweeps = 0;
+    uint32_t worst_iterations = 0, corrections = 0, launches = 0, sweeps = 0, timed_sweeps = 0;
     double sweep_seconds = 0.0, sweep_bytes = 0.0;
     const bool timed = (cfg.flags & FACETCU_BATCH_TIME_SWEEPS) != 0u;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -867,19 +867,25 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
         PanelParams pp{prho, ptau, pemis, pdir, psky};
         __nv_bfloat16* d0 = dbuf;
         __nv_bfloat16* d1 = dbuf ? dbuf + cells : nullptr;
-        const double panel_bytes = double(cells) * double(elem) * 2.0 + double(cells) * 16.0;
-        auto timed_sweep = [&](auto&& launch) {
-            if (timed) FCU_CHECK(cudaEventRecord(t0, s));
+        // Per-cell bytes: full sweep = state in + out + rho, tau, emission,
+        // direct; defect sweep = BF16 defect in + out + X read-modify-write +
+        // rho, tau.  Only the dominant kind is timed (defect sweeps in MIXED).
+        const double full_bytes = graph_bytes + double(cells) * (double(elem) * 2.0 + 16.0);
+        const double defect_bytes = graph_bytes + double(cells) * 20.0;
+        auto timed_sweep = [&](bool defect, auto&& launch) {
+            const bool count = timed && (defect == mixed);
+            if (count) FCU_CHECK(cudaEventRecord(t0, s));
             launch();
             ++launches;
             ++sweeps;
-            if (timed) {
+            if (count) {
                 FCU_CHECK(cudaEventRecord(t1, s));
                 FCU_CHECK(cudaEventSynchronize(t1));
                 float ms = 0.0f;
                 cudaEventElapsedTime(&ms, t0, t1);
                 sweep_seconds += double(ms) * 1e-3;
-                sweep_bytes += graph_bytes + panel_bytes;
+                sweep_bytes += defect ? defect_bytes : full_bytes;
+                ++timed_sweeps;
             }
         };
         launches += 4;  // prepare, sky, panel in, panel out
@@ -909,7 +915,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                     const uint32_t sweep = it + k;
                     char* in = (sweep & 1u) ? x1 : x0;
                     char* out = (sweep & 1u) ? x0 : x1;
-                    timed_sweep([&] {
+                    timed_sweep(false, [&] {
                         if (fp64)
                             launch_sweep<double>(P, g, pp, reinterpret_cast<const double*>(in),
                                                  reinterpret_cast<double*>(out), stats, counter,
@@ -936,7 +942,9 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
             float* X = reinterpret_cast<float*>(x0);
             float* Y = reinterpret_cast<float*>(x1);
             while (it < max_it) {
-                timed_sweep([&] { launch_sweep<float>(P, g, pp, X, Y, stats, counter, flag, s); });
+                timed_sweep(false, [&] {
+                    launch_sweep<float>(P, g, pp, X, Y, stats, counter, flag, s);
+                });
                 k_check<<<1, kMaxP, 0, s>>>(stats, flag, P, tol, it, counter);
                 FCU_LAUNCH("k_check");
                 ++launches;
@@ -961,7 +969,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                     const uint32_t batch = std::min(check_every, max_it - it);
                     uint32_t sub_flag[3];
                     for (uint32_t k = 0; k < batch; ++k) {
-                        timed_sweep([&] {
+                        timed_sweep(true, [&] {
                             launch_defect(P, g, pp, din, dout, X, stats, counter, flag, s);
                         });
                         std::swap(din, dout);
@@ -1009,6 +1017,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
         result->sweeps = sweeps;
         result->sweep_seconds = sweep_seconds;
         result->sweep_bytes = sweep_bytes;
+        result->timed_sweeps = timed_sweeps;
         result->iterations = worst_iterations;
         result->residual_corrections = corrections;
         result->converged = all_converged ? 1u : 0u;

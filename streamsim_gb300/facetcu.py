@@ -96,7 +96,8 @@ class BatchResult(C.Structure):
                 ("converged", C.c_uint32), ("max_relative_change", C.c_float),
                 ("seconds", C.c_double), ("kernel_launches", C.c_uint32),
                 ("sweeps", C.c_uint32), ("sweep_seconds", C.c_double),
-                ("sweep_bytes", C.c_double)]
+                ("sweep_bytes", C.c_double), ("timed_sweeps", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -74,3 +74,20 @@ def test_host_direction_helpers_match_reference(oracle, reference):
     for zen, az in [(30, 135), (0, 0), (75, 290), (45.5, 12.25), (89.9, 359.0)]:
         assert np.array_equal(facetcu.sun_direction(zen, az).view(np.uint32),
                               reference.sun_direction(zen, az).view(np.uint32))
+
+
+def test_cpp_wrapper_compiles_and_maps_errors(tmp_path, lib):
+    """include/facetcu.hpp keeps the reference's exception classes."""
+    import os
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = tmp_path / "wrapper_check"
+    libdir = os.path.join(root, "streamsim_gb300")
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(root, "include"),
+                    os.path.join(root, "tests", "cpp", "wrapper_check.cpp"), "-L", libdir,
+                    "-lfacetcu", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr

@@ -248,6 +248,39 @@ int facetcu_solve_batched_device(facetcu_context *ctx, const facetcu_batch_confi
                                  const float *direct_geometry, const float *initial,
                                  float *radiosity, facetcu_batch_result *result);
 
+/* ---- allocation-free solve (no counterpart in the reference) ------------- */
+/* facetcu_solve without any device allocation, for callers that cannot
+ * allocate GPU memory themselves or through us: host frameworks and plugin
+ * hosts that own the whole device-memory budget and hand it out from their
+ * own pool, and latency-critical loops that must not pay the implicit device
+ * synchronisation of cudaMalloc/cudaFree.  The caller passes the graph,
+ * optics and output in memory the current device can read and write;
+ * the sweep's working memory (one radiosity buffer and the per-sweep max|dB|
+ * slots) is a fixed array compiled into the library, about 4.2 MB per GPU
+ * that loads it, kept until the process exits.
+ *   row_offsets[surface_count + 1], edges[row_offsets[surface_count]],
+ *   denominators[surface_count], sky_counts[surface_count], optics and
+ *   radiosity[surface_count]: device-accessible; surface_count even,
+ *   <= FACETCU_NOALLOC_MAX_SURFACES (else FACETCU_OVERFLOW_ERROR);
+ *   1 <= iterations <= FACETCU_NOALLOC_MAX_ITERATIONS.
+ * Semantics are those of facetcu_solve (B starts at 0, `iterations`
+ * sweeps); the result is written to `radiosity`.  Work is queued on
+ * `stream` (a cudaStream_t; NULL = the default stream) of the current
+ * device; when max_delta is non-NULL the call waits for the stream and
+ * stores the last sweep's max|dB|, otherwise it returns once the work is
+ * queued.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the one array: calls whose
+ * work overlaps on a GPU (other threads or streams) race and must be
+ * serialised by the caller.  Inputs are not read back for validation. */
+#define FACETCU_NOALLOC_MAX_SURFACES 1048576u
+#define FACETCU_NOALLOC_MAX_ITERATIONS 4096u
+int facetcu_solve_noalloc(const uint32_t *row_offsets, const facetcu_csr_edge *edges,
+                          const uint32_t *denominators, const uint32_t *sky_counts,
+                          uint32_t surface_count, const facetcu_surface_optics *optics,
+                          float sky_radiosity, uint32_t iterations, float relaxation,
+                          float *radiosity, float *max_delta, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

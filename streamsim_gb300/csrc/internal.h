@@ -163,6 +163,12 @@ bool graph_pack(DeviceGraph& g, Workspace& ws, cudaStream_t s);
 void jacobi_plain_sweep(const DeviceGraph& g, const facetcu_surface_optics* d_optics,
                         float sky, float relaxation, const float* d_in, float* d_out,
                         uint32_t* d_max_delta_bits, cudaStream_t s);
+// The same sweep on raw device pointers (used by facetcu_solve_noalloc).
+void jacobi_plain_sweep_raw(uint32_t surfaces, const uint32_t* rows, const facetcu_csr_edge* edges,
+                            const uint32_t* denom, const uint32_t* skyc,
+                            const facetcu_surface_optics* d_optics, float sky, float relaxation,
+                            const float* d_in, float* d_out, uint32_t* d_max_delta_bits,
+                            cudaStream_t s);
 void incident_irradiance(const DeviceGraph& g, const facetcu_surface_optics* d_optics,
                          float sky, const float* d_radiosity, float* d_out, cudaStream_t s);
 

@@ -85,6 +85,20 @@ void jacobi_plain_sweep(const DeviceGraph& g, const facetcu_surface_optics* d_op
     FCU_LAUNCH("k_jacobi_plain");
 }
 
+void jacobi_plain_sweep_raw(uint32_t surfaces, const uint32_t* rows, const facetcu_csr_edge* edges,
+                            const uint32_t* denom, const uint32_t* skyc,
+                            const facetcu_surface_optics* d_optics, float sky, float relaxation,
+                            const float* d_in, float* d_out, uint32_t* d_max_delta_bits,
+                            cudaStream_t s)
+{
+    const uint32_t facets = surfaces / 2u;
+    if (!facets) return;
+    k_jacobi_plain<<<(facets + 63) / 64, 64, 0, s>>>(facets, rows, edges, denom, skyc, d_optics,
+                                                      sky, relaxation, d_in, d_out,
+                                                      d_max_delta_bits);
+    FCU_LAUNCH("k_jacobi_plain");
+}
+
 void incident_irradiance(const DeviceGraph& g, const facetcu_surface_optics* d_optics, float sky,
                          const float* d_radiosity, float* d_out, cudaStream_t s)
 {

@@ -139,8 +139,12 @@ SIGNATURES = {
                                                  C.POINTER(GraphDiagnostics),
                                                  C.POINTER(C.c_uint64)]),
     "facetcu_hemisphere_sunlit": (C.c_int, [_ctx, C.POINTER(Direction), _u32, _u32, _vp, _vp]),
+    "facetcu_solve_noalloc": (C.c_int, [_vp, _vp, _vp, _vp, _u32, _vp, C.c_float, _u32, C.c_float,
+                                        _vp, C.POINTER(C.c_float), _vp]),
 }
 OPTIONAL_SIGNATURES = {}
+NOALLOC_MAX_SURFACES = 1048576
+NOALLOC_MAX_ITERATIONS = 4096
 
 _LIB = None
 

@@ -309,11 +309,17 @@ def run_gpu(args, rank, world, local):
                 "avg_launch_ms": rt["sweep_seconds"] / max(rt["timed_sweeps"], 1) * 1e3,
                 "algorithmic_bytes_per_launch": rt["sweep_bytes"] / max(rt["timed_sweeps"], 1),
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"}
+    # DRAM bytes per launch of the same kernel from one ncu capture
+    # (profiles/k_defect_wide_config2.md); only valid for this workload.
     try:
-        prof = json.load(open(os.path.join(ROOT, "profiles", "sweep_traffic.json")))
-        roofline["traffic"] = prof.get(kname)
+        for line in open(os.path.join(ROOT, "profiles", "sweep_traffic.txt")):
+            name, value = line.split()
+            if name == kname and not args.quick and args.bands == 64:
+                roofline["traffic"] = float(value)
     except (OSError, ValueError):
         pass
+    roofline["l2_gather_bytes_per_launch"] = float(w["vf"]["directed_edges"]) * \
+        (panel * (2 if prec == fc.PRECISION_MIXED else 4))
 
     # end to end through the host-buffer C ABI (pinned buffers, copies timed)
     pin = {k: torch.from_numpy(np.ascontiguousarray(w[k])).pin_memory()

@@ -12,7 +12,11 @@ The view-factor graph is built once before timing (hemisphere ray casting,
 512 rays per facet side, top-K 256 when available, else the reference's
 40-direction global-line raster); a step is one complete 64-band solve from
 optics to converged radiosity (max relative change < 1e-6, the config-1 stop
-rule), with every input already resident in HBM.  L2 is flushed (a 512 MB
+rule), with every input already resident in HBM.  With the shipped MLP
+weights (streamsim_gb300/data/mlp_warm_start.npy, trained on other forest
+seeds by streamsim_gb300/train_mlp.py) the step includes the learned warm
+start: one FP32 sweep, the 12 features per side, the network and the
+combine, all inside the timed region.  L2 is flushed (a 512 MB
 write) between timed steps.
 
 `--impl reference` times the reference's own CPU Jacobi (solveCpu,
@@ -52,6 +56,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--quick", action="store_true", help="config-1 scene, for smoke timing")
+    p.add_argument("--warm-start", default="auto", choices=["auto", "mlp", "none"],
+                   help="auto: the shipped MLP weights when present and bands == 64")
     return p.parse_args()
 
 
@@ -240,6 +246,11 @@ def run_gpu(args, rank, world, local):
     S = sc.surface_count
     B = args.bands
     prec = fc.PRECISION_MIXED if args.precision == "mixed" else fc.PRECISION_FP32
+    use_mlp = args.warm_start == "mlp" or (args.warm_start == "auto" and B == 64 and
+                                           os.path.exists(fc.WARM_START_WEIGHTS))
+    if use_mlp:
+        m.mlpLoad()
+    warm = fc.WARM_MLP if use_mlp else fc.WARM_NONE
 
     # FP64 truth of the same graph (not timed)
     truth, tres = m.solveBatched(w["rho"], w["tau"], w["sky"], w["beam"], w["dgeo"],
@@ -252,12 +263,16 @@ def run_gpu(args, rank, world, local):
     out = torch.empty((B, S), dtype=torch.float32, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.ExternalStream(m.stream(), device=dev)
-    cfg = fc.BatchConfig(B, 1, prec, fc.WARM_NONE, 2000, args.tolerance, 0, 0)
+    cfg = fc.BatchConfig(B, 1, prec, warm, 2000, args.tolerance, 0, 0)
 
     def step(c=cfg):
         return m.solveBatchedDevice(c, t["rho"].data_ptr(), t["tau"].data_ptr(), None,
                                     t["sky"].data_ptr(), t["beam"].data_ptr(),
                                     t["dgeo"].data_ptr(), None, out.data_ptr())
+
+    cold = None
+    if use_mlp:  # the same solve from zero, untimed, for its sweep count
+        cold = step(fc.BatchConfig(B, 1, prec, fc.WARM_NONE, 2000, args.tolerance, 0, 0))
 
     for _ in range(args.warmup):
         flush.fill_(1.0)
@@ -291,8 +306,7 @@ def run_gpu(args, rank, world, local):
     value = units * world / step_s
 
     # sweep-kernel roofline: one extra solve with per-sweep CUDA events
-    cfg_t = fc.BatchConfig(B, 1, prec, fc.WARM_NONE, 2000, args.tolerance, 0,
-                           fc.BATCH_TIME_SWEEPS)
+    cfg_t = fc.BatchConfig(B, 1, prec, warm, 2000, args.tolerance, 0, fc.BATCH_TIME_SWEEPS)
     rt = step(cfg_t)
     peaks = {}
     try:
@@ -390,6 +404,10 @@ def run_gpu(args, rank, world, local):
             "max_rel_err_vs_fp64": err, "iterations": res["iterations"],
             "residual_corrections": res["residual_corrections"],
             "fp64_truth_iterations": tres["iterations"],
+            "warm_start": {"kind": "mlp" if use_mlp else "none",
+                           "iterations_from_zero": cold["iterations"] if cold else None,
+                           "weights": "streamsim_gb300/data/mlp_warm_start.npy"
+                           if use_mlp else None},
             "roofline": roofline, "e2e": e2e, "gpu_launches": int(np.mean(launches)),
             "clocks": clocks.summary(), "plain_fp32": plain,
             "speedup_vs_plain_fp32": (value / plain["value"]) if plain else None,

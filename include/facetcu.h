@@ -208,7 +208,8 @@ enum {
 };
 enum {
     FACETCU_WARM_NONE = 0,          /* start from B = 0 */
-    FACETCU_WARM_GIVEN = 1          /* start from `initial` (R * S floats) */
+    FACETCU_WARM_GIVEN = 1,         /* start from `initial` (R * S floats) */
+    FACETCU_WARM_MLP = 2            /* start from the context's trained MLP (64 bands) */
 };
 typedef struct {
     uint32_t band_count;
@@ -247,6 +248,51 @@ int facetcu_solve_batched_device(facetcu_context *ctx, const facetcu_batch_confi
                                  const float *emission, const float *sky, const float *beam,
                                  const float *direct_geometry, const float *initial,
                                  float *radiosity, facetcu_batch_result *result);
+
+/* ---- learned warm start (no counterpart in the reference) --------------- */
+/* MLP 12 -> 128 -> 128 -> 64 with GELU, BF16 weights (FP32 master copy,
+ * FP32 accumulation), trained by the library's own forward, backward and
+ * Adam kernels.  Per sun and side its 12 inputs are the first-order
+ * radiosity (one sweep from B = 0) of bands 0, 9, ..., 63 divided by
+ * sky_b + beam_b, the reflectance and transmittance of band 32, the
+ * sky-view fraction sky_s / denom_s and the y (up) component of the side
+ * normal; its 64 outputs predict (B_b - B1_b) / (sky_b + beam_b), the
+ * multiple-scattering part of every band.  FACETCU_WARM_MLP starts the
+ * batched solve from B1 + prediction; the iteration then runs to the same
+ * tolerance as without it, so the network only changes the sweep count.
+ * Parameters: 26,432 floats, W1[128x12], b1[128], W2[128x128], b2[128],
+ * W3[64x128], b3[64] (row-major, [out][in]). */
+typedef struct {
+    uint32_t steps;
+    uint32_t batch;
+    float learning_rate;
+    uint32_t seed;
+} facetcu_mlp_train_config;
+int facetcu_mlp_parameter_count(uint32_t *count);
+int facetcu_mlp_reset(facetcu_context *ctx, uint32_t seed);
+int facetcu_mlp_get_parameters(facetcu_context *ctx, float *parameters);
+int facetcu_mlp_set_parameters(facetcu_context *ctx, const float *parameters);
+/* Forward pass of n samples (host arrays): x[n * 12] -> y[n * 64]. */
+int facetcu_mlp_forward(facetcu_context *ctx, const float *x, uint32_t n, float *y);
+/* Mean-squared loss over n x 64 outputs and its FP32 gradient with respect
+ * to the parameters (same order), for x[n * 12] and target[n * 64];
+ * n <= 2^21 (FACETCU_OVERFLOW_ERROR above). */
+int facetcu_mlp_loss_and_gradient(facetcu_context *ctx, const float *x, const float *target,
+                                  uint32_t n, float *loss, float *gradient);
+/* Adam training on n device-resident samples (x[n * 12], target[n * 64]):
+ * `steps` minibatches of `batch` rows (<= 2^21) drawn with replacement
+ * (counter-based hash of seed, step, row). */
+int facetcu_mlp_train_device(facetcu_context *ctx, const float *x, const float *target,
+                             uint64_t n, const facetcu_mlp_train_config *config,
+                             float *final_loss);
+/* Training samples of the current graph and a 64-band batch problem (device
+ * pointers as in facetcu_solve_batched_device, converged radiosity
+ * [R][S]): features[(k * S + s) * 12], targets[(k * S + s) * 64]. */
+int facetcu_mlp_samples_device(facetcu_context *ctx, const facetcu_batch_config *config,
+                               const float *reflectance, const float *transmittance,
+                               const float *emission, const float *sky, const float *beam,
+                               const float *direct_geometry, const float *converged,
+                               float *features, float *targets);
 
 /* ---- allocation-free solve (no counterpart in the reference) ------------- */
 /* facetcu_solve without any device allocation, for callers that cannot

@@ -47,6 +47,9 @@ struct facetcu_context {
 
     Lbvh bvh;
     bool bvh_ready = false;
+    mlp::Net net;
+    mlp::Scratch mlp_scratch;
+    DeviceBuffer mlp_io, warm_b1, warm_x, warm_y, warm_x0;
     DeviceBuffer samples_uv, samples_dir, fraction;
 };
 
@@ -346,8 +349,18 @@ int facetcu_destroy(facetcu_context* ctx)
     ctx->stream = nullptr;
     ctx->facets = 0;
     for (DeviceBuffer* b : {&ctx->bvh.nodes, &ctx->bvh.tri, &ctx->bvh.parent, &ctx->bvh.flags,
-                            &ctx->samples_uv, &ctx->samples_dir, &ctx->fraction})
+                            &ctx->samples_uv, &ctx->samples_dir, &ctx->fraction, &ctx->mlp_io,
+                            &ctx->warm_b1, &ctx->warm_x, &ctx->warm_y, &ctx->warm_x0,
+                            &ctx->net.params, &ctx->net.bf16, &ctx->net.adam_m, &ctx->net.adam_v,
+                            &ctx->net.grad})
         b->release();
+    for (DeviceBuffer* b : {&ctx->mlp_scratch.z1, &ctx->mlp_scratch.a1, &ctx->mlp_scratch.z2,
+                            &ctx->mlp_scratch.a2, &ctx->mlp_scratch.y, &ctx->mlp_scratch.dy,
+                            &ctx->mlp_scratch.da, &ctx->mlp_scratch.dz, &ctx->mlp_scratch.part,
+                            &ctx->mlp_scratch.lossp, &ctx->mlp_scratch.idx, &ctx->mlp_scratch.xb,
+                            &ctx->mlp_scratch.tb})
+        b->release();
+    ctx->net.ready = false;
     ctx->bvh_ready = false;
     ctx->vertices_host.clear();
     ctx->bounds_override = false;
@@ -841,7 +854,9 @@ void validate_batch(const facetcu_batch_config* cfg)
     if (cfg->band_count == 0 || cfg->sun_count == 0)
         throw Error(FACETCU_INVALID_ARGUMENT, "band_count and sun_count must be positive");
     if (cfg->precision > 2u) throw Error(FACETCU_INVALID_ARGUMENT, "unknown precision");
-    if (cfg->warm_start > FACETCU_WARM_GIVEN) throw Error(FACETCU_INVALID_ARGUMENT, "unknown warm start");
+    if (cfg->warm_start > FACETCU_WARM_MLP) throw Error(FACETCU_INVALID_ARGUMENT, "unknown warm start");
+    if (cfg->warm_start == FACETCU_WARM_MLP && cfg->band_count != uint32_t(mlp::kOutputs))
+        throw Error(FACETCU_INVALID_ARGUMENT, "the MLP warm start needs 64 bands");
     if (!std::isfinite(cfg->tolerance) || cfg->tolerance < 0.0f)
         throw Error(FACETCU_INVALID_ARGUMENT, "tolerance must be finite and non-negative");
     if (uint64_t(cfg->band_count) * cfg->sun_count > (1ull << 31))
@@ -871,8 +886,40 @@ int run_batched(facetcu_context* ctx, const facetcu_batch_config* cfg, const flo
     FCU_CHECK(cudaEventCreate(&e0));
     FCU_CHECK(cudaEventCreate(&e1));
     FCU_CHECK(cudaEventRecord(e0, ctx->stream));
-    const int rc = batched_solve(ctx->graph, p, *cfg, initial, out, ctx->batch, ctx->ws, ctx->stream,
-                                 result);
+    int rc;
+    if (cfg->warm_start == FACETCU_WARM_MLP) {
+        // first-order sweep, features, network, B1 + prediction as the start
+        const uint32_t S = p.S, R = p.bands * p.suns;
+        float* b1 = static_cast<float*>(ctx->warm_b1.reserve(size_t(R) * S * 4));
+        float* x = static_cast<float*>(ctx->warm_x.reserve(size_t(p.suns) * S * mlp::kInputs * 4));
+        float* y = static_cast<float*>(ctx->warm_y.reserve(size_t(p.suns) * S * mlp::kOutputs * 4));
+        float* x0 = static_cast<float*>(ctx->warm_x0.reserve(size_t(R) * S * 4));
+        facetcu_batch_config first = *cfg;
+        first.precision = FACETCU_PRECISION_FP32;
+        first.warm_start = FACETCU_WARM_NONE;
+        first.maximum_iterations = 1;
+        first.flags = 0;
+        facetcu_batch_result r1{};
+        batched_solve(ctx->graph, p, first, nullptr, b1, ctx->batch, ctx->ws, ctx->stream, &r1);
+        mlp::features(b1, S, p.bands, p.suns, p.rho, p.tau, p.sky, p.beam,
+                      ctx->graph.denominators.as<uint32_t>(), ctx->graph.sky.as<uint32_t>(),
+                      ctx->vertices.as<facetcu_vertex>(), x, ctx->stream);
+        mlp::infer(ctx->net, x, size_t(p.suns) * S, ctx->mlp_scratch, y, ctx->stream);
+        mlp::warm_combine(b1, y, S, p.bands, p.suns, p.sky, p.beam, x0, ctx->stream);
+        facetcu_batch_config rest = *cfg;
+        rest.warm_start = FACETCU_WARM_GIVEN;
+        rc = batched_solve(ctx->graph, p, rest, x0, out, ctx->batch, ctx->ws, ctx->stream, result);
+        if (result) {
+            result->iterations += 1;
+            result->sweeps += 1;
+            // features + combine, and per inference chunk 3 GEMMs + the bias add
+            const size_t chunks = (size_t(p.suns) * S + mlp::kInferChunk - 1) / mlp::kInferChunk;
+            result->kernel_launches += r1.kernel_launches + 2 + 4 * uint32_t(chunks);
+        }
+    } else {
+        rc = batched_solve(ctx->graph, p, *cfg, initial, out, ctx->batch, ctx->ws, ctx->stream,
+                           result);
+    }
     FCU_CHECK(cudaEventRecord(e1, ctx->stream));
     FCU_CHECK(cudaEventSynchronize(e1));
     float ms = 0.0f;
@@ -903,6 +950,8 @@ int facetcu_solve_batched_device(facetcu_context* ctx, const facetcu_batch_confi
             throw Error(FACETCU_INVALID_ARGUMENT, "reflectance, transmittance, sky, beam and output are required");
         if (cfg->warm_start == FACETCU_WARM_GIVEN && !initial)
             throw Error(FACETCU_INVALID_ARGUMENT, "warm_start = GIVEN needs an initial radiosity");
+        if (cfg->warm_start == FACETCU_WARM_MLP && !ctx->net.ready)
+            throw Error(FACETCU_LOGIC_ERROR, "the MLP warm start needs trained parameters");
         return run_batched(ctx, cfg, reflectance, transmittance, emission, sky, beam,
                            direct_geometry, initial, radiosity, result);
     });
@@ -921,6 +970,8 @@ int facetcu_solve_batched(facetcu_context* ctx, const facetcu_batch_config* cfg,
             throw Error(FACETCU_INVALID_ARGUMENT, "reflectance, transmittance, sky, beam and output are required");
         if (cfg->warm_start == FACETCU_WARM_GIVEN && !initial)
             throw Error(FACETCU_INVALID_ARGUMENT, "warm_start = GIVEN needs an initial radiosity");
+        if (cfg->warm_start == FACETCU_WARM_MLP && !ctx->net.ready)
+            throw Error(FACETCU_LOGIC_ERROR, "the MLP warm start needs trained parameters");
         const size_t S = ctx->graph.surfaces, B = cfg->band_count, K = cfg->sun_count;
         const size_t R = B * K;
         for (size_t i = 0; i < B * S; ++i) {
@@ -962,6 +1013,163 @@ int facetcu_solve_batched(facetcu_context* ctx, const facetcu_batch_config* cfg,
         FCU_CHECK(cudaMemcpyAsync(radiosity, d_out, n_rs * 4, cudaMemcpyDeviceToHost, s));
         FCU_CHECK(cudaStreamSynchronize(s));
         return rc;
+    });
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int facetcu_mlp_parameter_count(uint32_t* count)
+{
+    if (!count) return FACETCU_INVALID_ARGUMENT;
+    *count = uint32_t(mlp::kParameterCount);
+    return FACETCU_OK;
+}
+
+int facetcu_mlp_reset(facetcu_context* ctx, uint32_t seed)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "mlpReset()");
+        mlp::init_params(ctx->net, seed, ctx->stream);
+        FCU_CHECK(cudaStreamSynchronize(ctx->stream));
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_mlp_get_parameters(facetcu_context* ctx, float* parameters)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "mlpGetParameters()");
+        if (!ctx->net.ready) throw Error(FACETCU_LOGIC_ERROR, "the MLP has no parameters yet");
+        if (!parameters) throw Error(FACETCU_INVALID_ARGUMENT, "parameters is null");
+        FCU_CHECK(cudaMemcpyAsync(parameters, ctx->net.params.ptr, mlp::kParameterCount * 4,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+        FCU_CHECK(cudaStreamSynchronize(ctx->stream));
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_mlp_set_parameters(facetcu_context* ctx, const float* parameters)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "mlpSetParameters()");
+        if (!parameters) throw Error(FACETCU_INVALID_ARGUMENT, "parameters is null");
+        for (int i = 0; i < mlp::kParameterCount; ++i)
+            if (!std::isfinite(parameters[i]))
+                throw Error(FACETCU_INVALID_ARGUMENT, "MLP parameters must be finite");
+        mlp::set_params(ctx->net, parameters, ctx->stream);
+        FCU_CHECK(cudaStreamSynchronize(ctx->stream));
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_mlp_forward(facetcu_context* ctx, const float* x, uint32_t n, float* y)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "mlpForward()");
+        if (!ctx->net.ready) throw Error(FACETCU_LOGIC_ERROR, "the MLP has no parameters yet");
+        if (!x || !y || n == 0) throw Error(FACETCU_INVALID_ARGUMENT, "x, y and n are required");
+        cudaStream_t s = ctx->stream;
+        float* dx = static_cast<float*>(
+            ctx->mlp_io.reserve(size_t(n) * (mlp::kInputs + mlp::kOutputs) * 4));
+        float* dy = dx + size_t(n) * mlp::kInputs;
+        FCU_CHECK(cudaMemcpyAsync(dx, x, size_t(n) * mlp::kInputs * 4, cudaMemcpyHostToDevice, s));
+        mlp::infer(ctx->net, dx, n, ctx->mlp_scratch, dy, s);
+        FCU_CHECK(cudaMemcpyAsync(y, dy, size_t(n) * mlp::kOutputs * 4, cudaMemcpyDeviceToHost, s));
+        FCU_CHECK(cudaStreamSynchronize(s));
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_mlp_loss_and_gradient(facetcu_context* ctx, const float* x, const float* target,
+                                  uint32_t n, float* loss, float* gradient)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "mlpLossAndGradient()");
+        if (!ctx->net.ready) throw Error(FACETCU_LOGIC_ERROR, "the MLP has no parameters yet");
+        if (!x || !target || n == 0) throw Error(FACETCU_INVALID_ARGUMENT, "x, target and n are required");
+        if (n > mlp::kMaxRows) throw Error(FACETCU_OVERFLOW_ERROR, "at most 2^21 rows per gradient");
+        cudaStream_t s = ctx->stream;
+        float* dx = static_cast<float*>(
+            ctx->mlp_io.reserve(size_t(n) * (mlp::kInputs + mlp::kOutputs) * 4));
+        float* dt = dx + size_t(n) * mlp::kInputs;
+        FCU_CHECK(cudaMemcpyAsync(dx, x, size_t(n) * mlp::kInputs * 4, cudaMemcpyHostToDevice, s));
+        FCU_CHECK(cudaMemcpyAsync(dt, target, size_t(n) * mlp::kOutputs * 4, cudaMemcpyHostToDevice, s));
+        const double l = mlp::loss_and_grad(ctx->net, dx, dt, int(n), ctx->mlp_scratch, s, true);
+        if (loss) *loss = float(l);
+        if (gradient)
+            FCU_CHECK(cudaMemcpyAsync(gradient, ctx->net.grad.ptr, mlp::kParameterCount * 4,
+                                      cudaMemcpyDeviceToHost, s));
+        FCU_CHECK(cudaStreamSynchronize(s));
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_mlp_train_device(facetcu_context* ctx, const float* x, const float* target, uint64_t n,
+                             const facetcu_mlp_train_config* config, float* final_loss)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "mlpTrain()");
+        if (!x || !target || n == 0 || !config || config->batch == 0 || config->steps == 0)
+            throw Error(FACETCU_INVALID_ARGUMENT, "samples and a training config are required");
+        if (n >= (1ull << 32)) throw Error(FACETCU_OVERFLOW_ERROR, "at most 2^32 training samples");
+        if (config->batch > mlp::kMaxRows)
+            throw Error(FACETCU_OVERFLOW_ERROR, "at most 2^21 samples per training batch");
+        if (!std::isfinite(config->learning_rate) || config->learning_rate <= 0.0f)
+            throw Error(FACETCU_INVALID_ARGUMENT, "learning_rate must be positive");
+        if (!ctx->net.ready) mlp::init_params(ctx->net, config->seed, ctx->stream);
+        const double l = mlp::train(ctx->net, x, target, n, config->steps, config->batch,
+                                    config->learning_rate, config->seed, ctx->mlp_scratch,
+                                    ctx->stream);
+        if (final_loss) *final_loss = float(l);
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_mlp_samples_device(facetcu_context* ctx, const facetcu_batch_config* cfg,
+                               const float* reflectance, const float* transmittance,
+                               const float* emission, const float* sky, const float* beam,
+                               const float* direct_geometry, const float* converged,
+                               float* features, float* targets)
+{
+    return guarded(ctx, [&] {
+        require_graph(ctx, "mlpSamples()");
+        validate_batch(cfg);
+        if (cfg->band_count != uint32_t(mlp::kOutputs))
+            throw Error(FACETCU_INVALID_ARGUMENT, "MLP samples need 64 bands");
+        if (!reflectance || !transmittance || !sky || !beam || !converged || !features || !targets)
+            throw Error(FACETCU_INVALID_ARGUMENT, "inputs and outputs are required");
+        BatchProblem p{};
+        p.vertices = ctx->vertices.as<facetcu_vertex>();
+        for (int a = 0; a < 3; ++a) {
+            p.lo[a] = ctx->bmin[a];
+            p.hi[a] = ctx->bmax[a];
+        }
+        p.S = ctx->graph.surfaces;
+        p.bands = cfg->band_count;
+        p.suns = cfg->sun_count;
+        p.rho = reflectance;
+        p.tau = transmittance;
+        p.emis = emission;
+        p.sky = sky;
+        p.beam = beam;
+        p.dgeo = direct_geometry;
+        const uint32_t S = p.S, R = p.bands * p.suns;
+        float* b1 = static_cast<float*>(ctx->warm_b1.reserve(size_t(R) * S * 4));
+        facetcu_batch_config first = *cfg;
+        first.precision = FACETCU_PRECISION_FP32;
+        first.warm_start = FACETCU_WARM_NONE;
+        first.maximum_iterations = 1;
+        first.flags = 0;
+        facetcu_batch_result r1{};
+        batched_solve(ctx->graph, p, first, nullptr, b1, ctx->batch, ctx->ws, ctx->stream, &r1);
+        mlp::features(b1, S, p.bands, p.suns, p.rho, p.tau, p.sky, p.beam,
+                      ctx->graph.denominators.as<uint32_t>(), ctx->graph.sky.as<uint32_t>(),
+                      ctx->vertices.as<facetcu_vertex>(), features, ctx->stream);
+        mlp::targets(converged, b1, S, p.bands, p.suns, p.sky, p.beam, targets, ctx->stream);
+        FCU_CHECK(cudaStreamSynchronize(ctx->stream));
+        return FACETCU_OK;
     });
 }
 

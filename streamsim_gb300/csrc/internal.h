@@ -218,4 +218,38 @@ void hemisphere_sunlit(const facetcu_vertex* d_vertices, uint32_t facets, const 
                        const float* d_uv, uint32_t samples, uint32_t sets, float3 sun,
                        float* d_fraction, cudaStream_t s);
 
+// ---- warm-start MLP (mlp.cu) -----------------------------------------------
+namespace mlp {
+constexpr int kInputs = 12, kOutputs = 64;
+constexpr int kParameterCount = 128 * 12 + 128 + 128 * 128 + 128 + 64 * 128 + 64;
+struct Net {
+    DeviceBuffer params, bf16, adam_m, adam_v, grad;
+    bool ready = false;
+    uint32_t steps_done = 0;
+};
+struct Scratch {
+    DeviceBuffer z1, a1, z2, a2, y, dy, da, dz, part, lossp, idx, xb, tb;
+};
+void init_params(Net& net, uint32_t seed, cudaStream_t s);
+void set_params(Net& net, const float* host, cudaStream_t s);
+// Rows per forward pass: kMaxRows keeps the GEMM grid (64 rows per CTA in
+// y) under 65,535 CTAs; inference is chunked at kInferChunk rows.
+constexpr size_t kMaxRows = size_t(1) << 21;
+constexpr size_t kInferChunk = size_t(1) << 19;
+void forward_full(Net& net, const float* X, int n, Scratch& sc, float* Y, cudaStream_t s);
+void infer(Net& net, const float* X, size_t n, Scratch& sc, float* Y, cudaStream_t s);
+double loss_and_grad(Net& net, const float* X, const float* T, int n, Scratch& sc, cudaStream_t s,
+                     bool want_loss);
+void adam_step(Net& net, float lr, cudaStream_t s);
+double train(Net& net, const float* X, const float* T, uint64_t n, uint32_t steps, uint32_t batch,
+             float lr, uint32_t seed, Scratch& sc, cudaStream_t s);
+void features(const float* B1, uint32_t S, uint32_t bands, uint32_t suns, const float* rho,
+              const float* tau, const float* sky, const float* beam, const uint32_t* denom,
+              const uint32_t* skyc, const facetcu_vertex* V, float* X, cudaStream_t s);
+void warm_combine(const float* B1, const float* Y, uint32_t S, uint32_t bands, uint32_t suns,
+                  const float* sky, const float* beam, float* x0, cudaStream_t s);
+void targets(const float* B, const float* B1, uint32_t S, uint32_t bands, uint32_t suns,
+             const float* sky, const float* beam, float* T, cudaStream_t s);
+}  // namespace mlp
+
 }  // namespace facetcu

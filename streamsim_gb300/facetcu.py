@@ -32,6 +32,7 @@ PRECISION_MIXED = 1
 PRECISION_FP64 = 2
 WARM_NONE = 0
 WARM_GIVEN = 1
+WARM_MLP = 2
 BATCH_TIME_SWEEPS = 1
 
 
@@ -91,6 +92,11 @@ class BatchConfig(C.Structure):
                 ("panel_width", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class MlpTrainConfig(C.Structure):
+    _fields_ = [("steps", C.c_uint32), ("batch", C.c_uint32), ("learning_rate", C.c_float),
+                ("seed", C.c_uint32)]
+
+
 class BatchResult(C.Structure):
     _fields_ = [("iterations", C.c_uint32), ("residual_corrections", C.c_uint32),
                 ("converged", C.c_uint32), ("max_relative_change", C.c_float),
@@ -142,7 +148,23 @@ SIGNATURES = {
     "facetcu_solve_noalloc": (C.c_int, [_vp, _vp, _vp, _vp, _u32, _vp, C.c_float, _u32, C.c_float,
                                         _vp, C.POINTER(C.c_float), _vp]),
 }
+SIGNATURES.update({
+    "facetcu_mlp_parameter_count": (C.c_int, [C.POINTER(_u32)]),
+    "facetcu_mlp_reset": (C.c_int, [_ctx, _u32]),
+    "facetcu_mlp_get_parameters": (C.c_int, [_ctx, _vp]),
+    "facetcu_mlp_set_parameters": (C.c_int, [_ctx, _vp]),
+    "facetcu_mlp_forward": (C.c_int, [_ctx, _vp, _u32, _vp]),
+    "facetcu_mlp_loss_and_gradient": (C.c_int, [_ctx, _vp, _vp, _u32, C.POINTER(C.c_float), _vp]),
+    "facetcu_mlp_train_device": (C.c_int, [_ctx, _vp, _vp, C.c_uint64, C.POINTER(MlpTrainConfig),
+                                           C.POINTER(C.c_float)]),
+    "facetcu_mlp_samples_device": (C.c_int, [_ctx, C.POINTER(BatchConfig)] + [_vp] * 9),
+})
 OPTIONAL_SIGNATURES = {}
+MLP_INPUTS = 12
+MLP_OUTPUTS = 64
+MLP_PARAMETERS = 26432
+WARM_START_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data",
+                                  "mlp_warm_start.npy")
 NOALLOC_MAX_SURFACES = 1048576
 NOALLOC_MAX_ITERATIONS = 4096
 
@@ -391,9 +413,10 @@ class FacetrtCuda:
     def solveBatched(self, reflectance, transmittance, sky, beam, direct_geometry=None,
                      emission=None, precision=PRECISION_FP32, tolerance=1e-6,
                      maximum_iterations=1000, initial=None, panel_width=0, raise_on_nonconvergence=True,
-                     flags=0):
+                     flags=0, warm_start=None):
         """reflectance/transmittance/emission: (bands, S); sky, beam: (bands,);
-        direct_geometry: (suns, S).  Returns radiosity (suns*bands, S) and the result dict."""
+        direct_geometry: (suns, S).  Returns radiosity (suns*bands, S) and the result dict.
+        warm_start: None (WARM_GIVEN when `initial` is given, else WARM_NONE) or WARM_MLP."""
         rho = _f32(reflectance)
         tau = _f32(transmittance)
         bands = rho.shape[0]
@@ -405,8 +428,10 @@ class FacetrtCuda:
         emis = None if emission is None else _f32(emission)
         dgeo = None if direct_geometry is None else _f32(direct_geometry).reshape(-1, S)
         suns = 1 if dgeo is None else dgeo.shape[0]
-        cfg = BatchConfig(bands, suns, precision, WARM_GIVEN if initial is not None else WARM_NONE,
-                          maximum_iterations, tolerance, panel_width, flags)
+        if warm_start is None:
+            warm_start = WARM_GIVEN if initial is not None else WARM_NONE
+        cfg = BatchConfig(bands, suns, precision, warm_start, maximum_iterations, tolerance,
+                          panel_width, flags)
         init = None if initial is None else _f32(initial)
         if init is not None and init.size != suns * bands * S:
             raise ValueError("initial radiosity must hold suns * bands * 2F values")
@@ -419,6 +444,56 @@ class FacetrtCuda:
             return out, res.as_dict()
         self._check(rc)
         return out, res.as_dict()
+
+    # -- learned warm start -------------------------------------------------
+    def mlpReset(self, seed=1):
+        self._check(self.lib.facetcu_mlp_reset(self.h, seed))
+
+    def mlpLoad(self, path=None):
+        """Load warm-start weights (a .npy of 26,432 float32; default: the
+        weights shipped with the package, trained by train_mlp.py)."""
+        self.mlpSetParameters(np.load(path or WARM_START_WEIGHTS))
+
+    def mlpParameters(self):
+        p = np.zeros(MLP_PARAMETERS, np.float32)
+        self._check(self.lib.facetcu_mlp_get_parameters(self.h, _ptr(p)))
+        return p
+
+    def mlpSetParameters(self, params):
+        p = _f32(params)
+        if p.size != MLP_PARAMETERS:
+            raise ValueError("MLP parameter vector must hold 26,432 floats")
+        self._check(self.lib.facetcu_mlp_set_parameters(self.h, _ptr(p)))
+
+    def mlpForward(self, x):
+        x = _f32(x).reshape(-1, MLP_INPUTS)
+        y = np.zeros((len(x), MLP_OUTPUTS), np.float32)
+        self._check(self.lib.facetcu_mlp_forward(self.h, _ptr(x), len(x), _ptr(y)))
+        return y
+
+    def mlpLossAndGradient(self, x, target):
+        x = _f32(x).reshape(-1, MLP_INPUTS)
+        t = _f32(target).reshape(-1, MLP_OUTPUTS)
+        if len(t) != len(x):
+            raise ValueError("x and target must have the same number of rows")
+        loss = C.c_float()
+        g = np.zeros(MLP_PARAMETERS, np.float32)
+        self._check(self.lib.facetcu_mlp_loss_and_gradient(self.h, _ptr(x), _ptr(t), len(x),
+                                                           C.byref(loss), _ptr(g)))
+        return loss.value, g
+
+    def mlpTrainDevice(self, x_ptr, t_ptr, n, steps, batch, learning_rate=1e-3, seed=1):
+        cfg = MlpTrainConfig(steps, batch, learning_rate, seed)
+        loss = C.c_float()
+        self._check(self.lib.facetcu_mlp_train_device(self.h, x_ptr, t_ptr, n, C.byref(cfg),
+                                                      C.byref(loss)))
+        return loss.value
+
+    def mlpSamplesDevice(self, cfg, rho_ptr, tau_ptr, emis_ptr, sky_ptr, beam_ptr, dgeo_ptr,
+                         converged_ptr, features_ptr, targets_ptr):
+        self._check(self.lib.facetcu_mlp_samples_device(
+            self.h, C.byref(cfg), rho_ptr, tau_ptr, emis_ptr, sky_ptr, beam_ptr, dgeo_ptr,
+            converged_ptr, features_ptr, targets_ptr))
 
     def solveBatchedDevice(self, cfg, rho_ptr, tau_ptr, emis_ptr, sky_ptr, beam_ptr, dgeo_ptr,
                            init_ptr, out_ptr):

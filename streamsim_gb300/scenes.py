@@ -203,15 +203,13 @@ def band_optics(scene, bands=64, leaf=(0.04, 0.48), soil=(0.12, 0.30), leaf_tau_
     lr = leaf[0] + (leaf[1] - leaf[0]) * t
     sr = soil[0] + (soil[1] - soil[0]) * t
     nleaf = scene.leaf_count - scene.trunk_count
-    rho_f = np.empty((bands, F))
-    tau_f = np.zeros((bands, F))
-    rho_f[:, :nleaf] = lr[:, None]
-    tau_f[:, :nleaf] = (leaf_tau_ratio * lr)[:, None]
-    rho_f[:, nleaf:scene.leaf_count] = lr[:, None]
-    rho_f[:, scene.leaf_count:] = sr[:, None]
-    rho = np.repeat(rho_f, 2, axis=1).astype(np.float32)
-    tau = np.repeat(tau_f, 2, axis=1).astype(np.float32)
-    return rho, tau
+    # material per side: 0 leaf, 1 trunk, 2 soil; one (bands, 3) table each
+    material = np.full(2 * F, 2, np.intp)
+    material[:2 * nleaf] = 0
+    material[2 * nleaf:2 * scene.leaf_count] = 1
+    rho_t = np.stack([lr, lr, sr], 1).astype(np.float32)
+    tau_t = np.stack([leaf_tau_ratio * lr, np.zeros(bands), np.zeros(bands)], 1).astype(np.float32)
+    return rho_t[:, material], tau_t[:, material]
 
 
 def reference_optics(scene, sunlit, sun, beam=700.0, leaf_rho=0.10, leaf_tau=0.05,

@@ -12,11 +12,11 @@ The view-factor graph is built once before timing (hemisphere ray casting,
 512 rays per facet side, top-K 256 when available, else the reference's
 40-direction global-line raster); a step is one complete 64-band solve from
 optics to converged radiosity (max relative change < 1e-6, the config-1 stop
-rule), with every input already resident in HBM.  With the shipped MLP
-weights (streamsim_gb300/data/mlp_warm_start.npy, trained on other forest
-seeds by streamsim_gb300/train_mlp.py) the step includes the learned warm
-start: one FP32 sweep, the 12 features per side, the network and the
-combine, all inside the timed region.  L2 is flushed (a 512 MB
+rule), with every input already resident in HBM.  With --warm-start mlp
+the step includes the learned warm start (streamsim_gb300/data/
+mlp_warm_start.npy, trained on other forest seeds by
+streamsim_gb300/train_mlp.py): one FP32 sweep, the 12 features per side,
+the network and the combine, all inside the timed region.  L2 is flushed (a 512 MB
 write) between timed steps.
 
 `--impl reference` times the reference's own CPU Jacobi (solveCpu,
@@ -56,8 +56,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--quick", action="store_true", help="config-1 scene, for smoke timing")
-    p.add_argument("--warm-start", default="auto", choices=["auto", "mlp", "none"],
-                   help="auto: the shipped MLP weights when present and bands == 64")
+    p.add_argument("--warm-start", default="none", choices=["auto", "mlp", "none"],
+                   help="mlp: the shipped MLP weights; auto: those when present and bands == 64")
     return p.parse_args()
 
 

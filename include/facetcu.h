@@ -327,6 +327,101 @@ int facetcu_solve_noalloc(const uint32_t *row_offsets, const facetcu_csr_edge *e
                           float sky_radiosity, uint32_t iterations, float relaxation,
                           float *radiosity, float *max_delta, void *stream);
 
+/* ---- scene files, optics and the eFacetRT process flow ------------------ */
+/* Scene facts loadTreeWithSoil returns (Scene, facetrtcore.cpp:148-166). */
+typedef struct {
+    uint32_t facet_count;
+    uint32_t leaf_facet_count; /* facets [0, leaf) are the object, the rest ground */
+    float minimum[3];
+    float maximum[3];
+} facetcu_scene_info;
+/* loadTreeWithSoil (facetrtcore.cpp:361-473): OBJ positions and faces (fan
+ * triangulated, degenerate triangles dropped), Y shifted so the lowest
+ * vertex is at 0, and a 48 x 48 soil grid at y = -0.01 reaching half the
+ * object's extent beyond it, unless an `o STREAMSIM_TERRAIN` block marks the
+ * ground.  Host only, no GPU.  Call with vertices = material_indices = NULL
+ * for `info`, then with arrays for capacity_facets >= info.facet_count facets
+ * (3 vertices, one material index per facet: 0 object, 1 ground).  Errors
+ * (FACETCU_RUNTIME_ERROR with the reference's message) are read with
+ * facetcu_host_last_error(). */
+int facetcu_load_tree_with_soil(const char *path, facetcu_vertex *vertices,
+                                uint32_t *material_indices, uint32_t capacity_facets,
+                                facetcu_scene_info *info);
+/* makeOptics (facetrtcore.cpp:500-522): rho 0.10 / 0.20, tau 0.05 / 0 for
+ * object / ground sides, D = sunlit * max(0, n_side . sun) * 700.  Host only. */
+int facetcu_make_optics(const facetcu_vertex *vertices, uint32_t facet_count,
+                        uint32_t leaf_facet_count, const float *sunlit,
+                        const facetcu_direction *sun, facetcu_surface_optics *optics);
+/* planckRadiance (facetrtcore.cpp:524-536): W m-2 sr-1 um-1; wavelength in
+ * nm when above 50, else in um; evaluated in double. */
+float facetcu_planck_radiance(float wavelength, float temperature);
+/* The message of the last failing host-only call on this thread. */
+const char *facetcu_host_last_error(void);
+/* runFacetRTCore (facetrtcore.h:5-7, facetrtcore.cpp:3116-3161) for an OBJ
+ * scene: loadTreeWithSoil, the runGpu sequence (:1621-1780) on this library
+ * (40-direction graph at 1024 x 1024, sun raster at 30/135 deg, makeOptics,
+ * 64-sweep solve, diffuse solve, lightEnhancement) and writeWebResult
+ * (:1782-1840).  Prints `PROGRESS\t<int>\t<text>` lines and
+ * `RESULT\t<path>` to stdout; on failure `facetrt: <message>` to stderr and
+ * returns 1 (0 on success).  output_file NULL or "" writes facetrt.json next
+ * to the input.  shader_directory is accepted and unused.  project.json
+ * inputs are refused (scene and material ingestion is not built). */
+int facetcu_run_facetrt_core(const char *input_path, const char *shader_directory,
+                             const char *output_file);
+
+/* ---- spectral optics and the band loop ----------------------------------- */
+/* SurfaceParameters (facetrtcore.cpp:106-138): the fields the optics read. */
+typedef struct {
+    const float *reflectance;   /* per band; the last value repeats (bandValue :538-544) */
+    uint32_t reflectance_count; /* 0: 0.10 for object facets, 0.20 for ground */
+    const float *transmittance;
+    uint32_t transmittance_count; /* 0: 0.05 object, 0 ground */
+    float tir_reflectance;
+    float tir_transmittance;
+    float sunlit_temperature; /* K */
+    float shaded_temperature; /* K */
+} facetcu_surface_parameters;
+/* FacetRTParameters (facetrtcore.cpp:140-146) and the Scene fields
+ * makeSpectralOptics reads (:148-166). */
+typedef struct {
+    const float *wavelengths; /* nm; a band is optical when <= 2500 nm (values <= 2.5 are um) */
+    uint32_t band_count;
+    facetcu_surface_parameters object; /* for object facets without a material */
+    facetcu_surface_parameters ground; /* for ground facets without a material */
+    const facetcu_surface_parameters *materials; /* Scene::materials */
+    uint32_t material_count;
+    const uint32_t *material_indices; /* per facet, or NULL */
+    const float *texture_factors;     /* per facet reflectance factor, or NULL (1) */
+    uint32_t leaf_facet_count;
+    float background_angular_strength; /* Hapke blend of ground sides, [0, 1] */
+    float sky_temperature;             /* K, sky radiance of thermal bands */
+    uint32_t accelerated_solver;       /* FacetRTParameters::acceleratedSolver */
+} facetcu_spectral_parameters;
+/* makeSpectralOptics (facetrtcore.cpp:1057-1126) for one band on the
+ * context's geometry; sunlit[2F] and optics[2F] are host arrays. */
+int facetcu_spectral_optics(facetcu_context *ctx, const facetcu_spectral_parameters *parameters,
+                            const float *sunlit, const facetcu_direction *sun, uint32_t band,
+                            facetcu_surface_optics *optics);
+typedef struct {
+    uint32_t iterations;    /* band 0's SolveResult::iterations */
+    float max_delta;        /* band 0's SolveResult::maxDelta */
+    uint32_t thermal_bands; /* bands that are not optical */
+    uint32_t batched_sweeps; /* sweeps of the batched solve of bands 1.. */
+    double seconds;
+} facetcu_band_result;
+/* The spectral band loop of runGpu (facetrtcore.cpp:1677-1773) on the
+ * context's graph: optics of every band on the device, band 0 through the
+ * reference-semantics solver (64 sweeps, or solveAccelerated's rule when
+ * accelerated_solver), bands 1.. in one batched FP32 solve (64 sweeps; to a
+ * max relative change of 1e-6 when accelerated_solver, with no band-to-band
+ * warm start), optical bands converted to apparent reflectance
+ * clamp(B / (700 max(0, sun.y) + 50), 0, 1), and lightEnhancement from a
+ * direct-free solve of band 0 when it is optical (else zeros).
+ * band_radiosity[band_count][2F] and light_enhancement[2F] are host arrays. */
+int facetcu_solve_bands(facetcu_context *ctx, const facetcu_spectral_parameters *parameters,
+                        const float *sunlit, const facetcu_direction *sun, float *band_radiosity,
+                        float *light_enhancement, facetcu_band_result *result);
+
 #ifdef __cplusplus
 }
 #endif

@@ -327,8 +327,51 @@ class Reference:
         L.ref_run_cpu_obj.argtypes = [C.c_char_p, C.c_uint32, C.c_void_p, C.c_void_p,
                                       C.c_void_p, u32p, f32p]
 
+        L.ref_planck.restype = C.c_float
+        L.ref_planck.argtypes = [C.c_float, C.c_float]
+        L.ref_make_spectral_optics.argtypes = ([C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                                C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                                C.c_uint32, C.c_float, C.c_float, C.c_void_p,
+                                                C.c_float, C.c_float, C.c_uint32, C.c_void_p])
+
     def error(self):
         return self.lib.ref_last_error().decode()
+
+    def planck(self, wavelength, temperature):
+        return float(self.lib.ref_planck(wavelength, temperature))
+
+    @staticmethod
+    def _pack_surface(m):
+        r = np.asarray(m.reflectance, np.float32).ravel()
+        t = np.asarray(m.transmittance, np.float32).ravel()
+        head = [r.size, t.size, m.tir_reflectance, m.tir_transmittance, m.sunlit_temperature,
+                m.shaded_temperature]
+        return np.concatenate([np.asarray(head, np.float32), r, t])
+
+    def make_spectral_optics(self, vertices, leaf_count, sunlit, zenith, azimuth, wavelengths,
+                             band, object_surface, ground, materials=(), material_indices=None,
+                             texture_factors=None, strength=0.0, sky_temperature=250.0):
+        """makeSpectralOptics (facetrtcore.cpp:1057-1126) for one band.
+        Surfaces are any objects with reflectance, transmittance,
+        tir_reflectance, tir_transmittance, sunlit_temperature and
+        shaded_temperature attributes."""
+        vertices = np.ascontiguousarray(vertices, np.float32)
+        sunlit = np.ascontiguousarray(sunlit, np.float32)
+        wl = np.ascontiguousarray(wavelengths, np.float32)
+        F = len(vertices) // 3
+        packed = np.concatenate([self._pack_surface(m)
+                                 for m in [object_surface, ground, *materials]])
+        mi = None if material_indices is None else np.ascontiguousarray(material_indices,
+                                                                        np.uint32)
+        tex = None if texture_factors is None else np.ascontiguousarray(texture_factors,
+                                                                       np.float32)
+        out = np.zeros((2 * F, 4), np.float32)
+        self.lib.ref_make_spectral_optics(
+            vertices.ctypes.data, F, leaf_count, None if mi is None else mi.ctypes.data,
+            None if tex is None else tex.ctypes.data, packed.ctypes.data, len(materials),
+            wl.ctypes.data, wl.size, strength, sky_temperature, sunlit.ctypes.data, zenith,
+            azimuth, band, out.ctypes.data)
+        return out
 
     def hemisphere_directions(self):
         out = np.zeros((40, 3), np.float32)

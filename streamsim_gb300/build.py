@@ -1,7 +1,7 @@
 """Build libfacetcu.so (CUDA, sm_103a) in-tree with nvcc.
 
 Translation units are compiled in parallel and linked into
-streamsim_gb300/libfacetcu.so.  raster.cu and hemi.cu are compiled with
+streamsim_gb300/libfacetcu.so.  raster.cu, hemi.cu, lbvh.cu and spectral.cu are compiled with
 -fmad=false because their float results must round exactly like the
 reference's CPU code (no fused multiply-add); host code is compiled with
 -ffp-contract=off for the same reason.
@@ -16,8 +16,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfacetcu.so")
+CLI_SRC = os.path.join(HERE, "cli", "facetcu_main.cpp")
+CLI = os.path.join(HERE, "facetcu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-EXACT_FP = {"raster.cu", "hemi.cu", "lbvh.cu"}
+EXACT_FP = {"raster.cu", "hemi.cu", "lbvh.cu", "spectral.cu"}
 
 
 def nvcc():
@@ -54,7 +56,23 @@ def _stale():
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     deps.append(os.path.join(HERE, "..", "include", "facetcu.h"))
     deps.append(os.path.abspath(__file__))
+    deps.append(CLI_SRC)
+    if not os.path.exists(CLI) or os.path.getmtime(CLI) < t:
+        return True
     return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_cli():
+    """The `facetcu` executable (the eFacetRT process seam), linked to
+    libfacetcu.so next to it."""
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-std=c++17", "-O2", "-I", os.path.join(HERE, "..", "include"), CLI_SRC,
+           "-L", HERE, "-lfacetcu", "-Wl,-rpath,$ORIGIN", "-o", CLI + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CLI build failed:\n{r.stderr}")
+    os.replace(CLI + ".tmp", CLI)
+    return CLI
 
 
 def build(force=False, jobs=None):
@@ -71,6 +89,7 @@ def build(force=False, jobs=None):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     return LIB
 
 

@@ -8,6 +8,7 @@
 // -ffp-contract=off.
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <limits>
@@ -51,6 +52,8 @@ struct facetcu_context {
     mlp::Scratch mlp_scratch;
     DeviceBuffer mlp_io, warm_b1, warm_x, warm_y, warm_x0;
     DeviceBuffer samples_uv, samples_dir, fraction;
+    spectral::Tables spec;
+    DeviceBuffer spec_io;
 };
 
 namespace {
@@ -1169,6 +1172,196 @@ int facetcu_mlp_samples_device(facetcu_context* ctx, const facetcu_batch_config*
                       ctx->vertices.as<facetcu_vertex>(), features, ctx->stream);
         mlp::targets(converged, b1, S, p.bands, p.suns, p.sky, p.beam, targets, ctx->stream);
         FCU_CHECK(cudaStreamSynchronize(ctx->stream));
+        return FACETCU_OK;
+    });
+}
+
+
+// ---- spectral optics and the band loop ---------------------------------------
+}  // extern "C"
+
+namespace {
+
+void validate_surface(const facetcu_surface_parameters& m)
+{
+    if ((m.reflectance_count && !m.reflectance) || (m.transmittance_count && !m.transmittance))
+        throw Error(FACETCU_INVALID_ARGUMENT, "a surface's band values are missing");
+}
+
+void validate_spectral(const facetcu_context* ctx, const facetcu_spectral_parameters* p,
+                       const float* sunlit, const facetcu_direction* sun)
+{
+    if (!p || !sunlit || !sun)
+        throw Error(FACETCU_INVALID_ARGUMENT, "parameters, sunlit and sun are required");
+    if (!p->wavelengths || p->band_count == 0)
+        throw Error(FACETCU_INVALID_ARGUMENT, "at least one wavelength is required");
+    for (uint32_t b = 0; b < p->band_count; ++b)
+        if (!std::isfinite(p->wavelengths[b]) || p->wavelengths[b] <= 0.0f)
+            throw Error(FACETCU_INVALID_ARGUMENT, "wavelengths must be finite and positive");
+    if (p->material_count && !p->materials)
+        throw Error(FACETCU_INVALID_ARGUMENT, "material_count > 0 needs materials");
+    validate_surface(p->object);
+    validate_surface(p->ground);
+    for (uint32_t m = 0; m < p->material_count; ++m) validate_surface(p->materials[m]);
+    if (p->leaf_facet_count > ctx->facets)
+        throw Error(FACETCU_INVALID_ARGUMENT, "leaf_facet_count exceeds the facet count");
+    if (!std::isfinite(sun->x) || !std::isfinite(sun->y) || !std::isfinite(sun->z))
+        throw Error(FACETCU_INVALID_ARGUMENT, "sun direction must be finite");
+}
+
+struct SpectralIO {
+    uint32_t* material = nullptr;
+    float *texture = nullptr, *sunlit = nullptr, *dgeo = nullptr, *rho = nullptr,
+          *tau = nullptr, *emis = nullptr, *out = nullptr, *sky = nullptr, *beam = nullptr;
+    facetcu_surface_optics* aos = nullptr;
+};
+
+// Device inputs for `bands` bands: tables, materials, texture, sunlit, dgeo.
+SpectralIO spectral_inputs(facetcu_context* ctx, const facetcu_spectral_parameters& p,
+                           const float* sunlit, const facetcu_direction& sun, uint32_t bands)
+{
+    cudaStream_t st = ctx->stream;
+    const size_t F = ctx->facets, S = 2 * F, nb = p.band_count;
+    ctx->spec.build(p, st);
+    auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t bytes = al(F * 4) * 2 + al(S * 4) * 2 + al(size_t(bands) * S * 4) * 4 +
+                         al(nb * 4) * 2 + al(S * 16);
+    char* c = static_cast<char*>(ctx->spec_io.reserve(bytes));
+    SpectralIO io;
+    auto take = [&](size_t b) {
+        char* r = c;
+        c += al(b);
+        return r;
+    };
+    io.material = p.material_indices ? reinterpret_cast<uint32_t*>(take(F * 4)) : nullptr;
+    io.texture = p.texture_factors ? reinterpret_cast<float*>(take(F * 4)) : nullptr;
+    io.sunlit = reinterpret_cast<float*>(take(S * 4));
+    io.dgeo = reinterpret_cast<float*>(take(S * 4));
+    io.rho = reinterpret_cast<float*>(take(size_t(bands) * S * 4));
+    io.tau = reinterpret_cast<float*>(take(size_t(bands) * S * 4));
+    io.emis = reinterpret_cast<float*>(take(size_t(bands) * S * 4));
+    io.out = reinterpret_cast<float*>(take(size_t(bands) * S * 4));
+    io.sky = reinterpret_cast<float*>(take(nb * 4));
+    io.beam = reinterpret_cast<float*>(take(nb * 4));
+    io.aos = reinterpret_cast<facetcu_surface_optics*>(take(S * 16));
+    if (io.material)
+        FCU_CHECK(cudaMemcpyAsync(io.material, p.material_indices, F * 4, cudaMemcpyHostToDevice, st));
+    if (io.texture)
+        FCU_CHECK(cudaMemcpyAsync(io.texture, p.texture_factors, F * 4, cudaMemcpyHostToDevice, st));
+    FCU_CHECK(cudaMemcpyAsync(io.sunlit, sunlit, S * 4, cudaMemcpyHostToDevice, st));
+    FCU_CHECK(cudaMemcpyAsync(io.sky, ctx->spec.sky.data(), nb * 4, cudaMemcpyHostToDevice, st));
+    FCU_CHECK(cudaMemcpyAsync(io.beam, ctx->spec.beam.data(), nb * 4, cudaMemcpyHostToDevice, st));
+    spectral::direct_geometry(uint32_t(F), ctx->vertices.as<facetcu_vertex>(), sun, io.sunlit,
+                              io.dgeo, st);
+    return io;
+}
+
+void nested(facetcu_context* ctx, int rc)
+{
+    if (rc != FACETCU_OK) throw Error(rc, ctx->last_error);
+}
+
+}  // namespace
+
+extern "C" {
+
+int facetcu_spectral_optics(facetcu_context* ctx, const facetcu_spectral_parameters* parameters,
+                            const float* sunlit, const facetcu_direction* sun, uint32_t band,
+                            facetcu_surface_optics* optics)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "spectralOptics()");
+        if (!ctx->facets) throw Error(FACETCU_LOGIC_ERROR, "spectralOptics() needs geometry");
+        validate_spectral(ctx, parameters, sunlit, sun);
+        if (!optics) throw Error(FACETCU_INVALID_ARGUMENT, "optics is required");
+        if (band >= parameters->band_count) throw Error(FACETCU_INVALID_ARGUMENT, "band out of range");
+        const facetcu_spectral_parameters& p = *parameters;
+        const size_t S = 2 * size_t(ctx->facets);
+        SpectralIO io = spectral_inputs(ctx, p, sunlit, *sun, 1);
+        spectral::optics(ctx->spec, p, ctx->facets, ctx->vertices.as<facetcu_vertex>(), io.material,
+                         io.texture, *sun, io.sunlit, band, 1, io.rho, io.tau, io.emis, ctx->stream);
+        spectral::pack(S, io.rho, io.tau, io.emis, io.dgeo, ctx->spec.beam[band], io.aos, ctx->stream);
+        FCU_CHECK(cudaMemcpyAsync(optics, io.aos, S * 16, cudaMemcpyDeviceToHost, ctx->stream));
+        FCU_CHECK(cudaStreamSynchronize(ctx->stream));
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_solve_bands(facetcu_context* ctx, const facetcu_spectral_parameters* parameters,
+                        const float* sunlit, const facetcu_direction* sun, float* band_radiosity,
+                        float* light_enhancement, facetcu_band_result* result)
+{
+    return guarded(ctx, [&] {
+        require_graph(ctx, "solveBands()");
+        validate_spectral(ctx, parameters, sunlit, sun);
+        if (!band_radiosity || !light_enhancement)
+            throw Error(FACETCU_INVALID_ARGUMENT, "band_radiosity and light_enhancement are required");
+        const auto t0 = std::chrono::steady_clock::now();
+        const facetcu_spectral_parameters& p = *parameters;
+        const uint32_t nb = p.band_count;
+        const size_t S = ctx->graph.surfaces;
+        if (S != 2 * size_t(ctx->facets))
+            throw Error(FACETCU_LOGIC_ERROR, "the graph does not belong to the current geometry");
+        cudaStream_t st = ctx->stream;
+        SpectralIO io = spectral_inputs(ctx, p, sunlit, *sun, nb);
+        spectral::optics(ctx->spec, p, ctx->facets, ctx->vertices.as<facetcu_vertex>(), io.material,
+                         io.texture, *sun, io.sunlit, 0, nb, io.rho, io.tau, io.emis, st);
+        const bool accel = p.accelerated_solver != 0;
+        // band 0 through the reference-semantics solver (it carries the
+        // SolveResult of facetrt.json and the direct-light enhancement)
+        std::vector<facetcu_surface_optics> o0(S);
+        spectral::pack(S, io.rho, io.tau, io.emis, io.dgeo, ctx->spec.beam[0], io.aos, st);
+        FCU_CHECK(cudaMemcpyAsync(o0.data(), io.aos, S * 16, cudaMemcpyDeviceToHost, st));
+        FCU_CHECK(cudaStreamSynchronize(st));
+        auto solve_one = [&](const std::vector<facetcu_surface_optics>& o, float* out,
+                             uint32_t* it, float* md) {
+            if (accel)
+                nested(ctx, facetcu_solve_accelerated(ctx, o.data(), S, ctx->spec.sky[0], nullptr,
+                                                      64, 8, 1.0e-4f, 1.0f, out, it, md));
+            else
+                nested(ctx, facetcu_solve(ctx, o.data(), S, ctx->spec.sky[0], 64, 1.0f, out, it, md));
+        };
+        facetcu_band_result r{};
+        solve_one(o0, band_radiosity, &r.iterations, &r.max_delta);
+        if (nb > 1) {
+            facetcu_batch_config cfg{};
+            cfg.band_count = nb - 1;
+            cfg.sun_count = 1;
+            cfg.precision = FACETCU_PRECISION_FP32;
+            cfg.warm_start = FACETCU_WARM_NONE;
+            cfg.maximum_iterations = accel ? 2000u : 64u;
+            cfg.tolerance = accel ? 1.0e-6f : 0.0f;
+            facetcu_batch_result br{};
+            const int rc = facetcu_solve_batched_device(ctx, &cfg, io.rho + S, io.tau + S,
+                                                        io.emis + S, io.sky + 1, io.beam + 1,
+                                                        io.dgeo, nullptr, io.out + S, &br);
+            if (rc != FACETCU_NOT_CONVERGED || accel) nested(ctx, rc);
+            r.batched_sweeps = br.sweeps;
+        }
+        FCU_CHECK(cudaMemcpyAsync(io.out, band_radiosity, S * 4, cudaMemcpyHostToDevice, st));
+        const float cosz = std::max(0.0f, sun->y);
+        const float ref = 700.0f * cosz + 100.0f * 0.5f;
+        if (ref > 1.0e-8f)
+            spectral::apparent(io.out, S, nb, ctx->spec.optical_dev, ref, st);
+        FCU_CHECK(cudaMemcpyAsync(band_radiosity, io.out, size_t(nb) * S * 4,
+                                  cudaMemcpyDeviceToHost, st));
+        FCU_CHECK(cudaStreamSynchronize(st));
+        for (uint32_t b = 0; b < nb; ++b) r.thermal_bands += ctx->spec.optical[b] ? 0u : 1u;
+        std::fill(light_enhancement, light_enhancement + S, 0.0f);
+        if (ctx->spec.optical[0]) {
+            for (auto& o : o0) o.direct_irradiance = 0.0f;
+            std::vector<float> diffuse(S);
+            uint32_t it = 0;
+            float md = 0.0f;
+            solve_one(o0, diffuse.data(), &it, &md);
+            for (size_t s = 0; s < S; ++s) {
+                float d = diffuse[s];
+                if (ref > 1.0e-8f) d = std::clamp(d / ref, 0.0f, 1.0f);
+                light_enhancement[s] = std::max(0.0f, band_radiosity[s] - d);
+            }
+        }
+        r.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (result) *result = r;
         return FACETCU_OK;
     });
 }

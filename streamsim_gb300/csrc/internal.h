@@ -252,4 +252,30 @@ void targets(const float* B, const float* B1, uint32_t S, uint32_t bands, uint32
              const float* sky, const float* beam, float* T, cudaStream_t s);
 }  // namespace mlp
 
+// ---- spectral optics (spectral.cu) ----------------------------------------
+namespace spectral {
+bool optical_wavelength(float wavelength);
+// Per-material, per-band scalars and per-band flags for one parameter set.
+struct Tables {
+    DeviceBuffer dev;
+    float4* table = nullptr;   // [(slot*2 + object)*bands + b] = {rho, tau, Planck sun, shade}
+    float2* tir = nullptr;     // [slot] = {tir rho, tir tau}
+    uint8_t* thermal = nullptr;      // [b] wavelength > 2500 (makeSpectralOptics' test)
+    uint8_t* optical_dev = nullptr;  // [b] isOpticalWavelength
+    std::vector<float> sky, beam;    // per band
+    std::vector<uint8_t> optical;
+    void build(const facetcu_spectral_parameters& p, cudaStream_t s);
+};
+void optics(const Tables& t, const facetcu_spectral_parameters& p, uint32_t F,
+            const facetcu_vertex* V, const uint32_t* material, const float* texture,
+            facetcu_direction sun, const float* sunlit, uint32_t b0, uint32_t bcount, float* rho,
+            float* tau, float* emis, cudaStream_t s);
+void direct_geometry(uint32_t F, const facetcu_vertex* V, facetcu_direction sun,
+                     const float* sunlit, float* dgeo, cudaStream_t s);
+void pack(size_t S, const float* rho, const float* tau, const float* emis, const float* dgeo,
+          float beam, facetcu_surface_optics* out, cudaStream_t s);
+void apparent(float* B, size_t S, uint32_t bands, const uint8_t* optical, float ref,
+              cudaStream_t s);
+}  // namespace spectral
+
 }  // namespace facetcu

@@ -109,6 +109,36 @@ class BatchResult(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class SceneInfo(C.Structure):
+    _fields_ = [("facet_count", C.c_uint32), ("leaf_facet_count", C.c_uint32),
+                ("minimum", C.c_float * 3), ("maximum", C.c_float * 3)]
+
+
+class SurfaceParameters(C.Structure):
+    _fields_ = [("reflectance", C.c_void_p), ("reflectance_count", C.c_uint32),
+                ("transmittance", C.c_void_p), ("transmittance_count", C.c_uint32),
+                ("tir_reflectance", C.c_float), ("tir_transmittance", C.c_float),
+                ("sunlit_temperature", C.c_float), ("shaded_temperature", C.c_float)]
+
+
+class SpectralParameters(C.Structure):
+    _fields_ = [("wavelengths", C.c_void_p), ("band_count", C.c_uint32),
+                ("object", SurfaceParameters), ("ground", SurfaceParameters),
+                ("materials", C.c_void_p), ("material_count", C.c_uint32),
+                ("material_indices", C.c_void_p), ("texture_factors", C.c_void_p),
+                ("leaf_facet_count", C.c_uint32), ("background_angular_strength", C.c_float),
+                ("sky_temperature", C.c_float), ("accelerated_solver", C.c_uint32)]
+
+
+class BandResult(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("max_delta", C.c_float),
+                ("thermal_bands", C.c_uint32), ("batched_sweeps", C.c_uint32),
+                ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _vp = C.c_void_p
 _u32 = C.c_uint32
 _ctx = C.c_void_p
@@ -158,6 +188,17 @@ SIGNATURES.update({
     "facetcu_mlp_train_device": (C.c_int, [_ctx, _vp, _vp, C.c_uint64, C.POINTER(MlpTrainConfig),
                                            C.POINTER(C.c_float)]),
     "facetcu_mlp_samples_device": (C.c_int, [_ctx, C.POINTER(BatchConfig)] + [_vp] * 9),
+})
+SIGNATURES.update({
+    "facetcu_load_tree_with_soil": (C.c_int, [C.c_char_p, _vp, _vp, _u32, C.POINTER(SceneInfo)]),
+    "facetcu_make_optics": (C.c_int, [_vp, _u32, _u32, _vp, C.POINTER(Direction), _vp]),
+    "facetcu_planck_radiance": (C.c_float, [C.c_float, C.c_float]),
+    "facetcu_host_last_error": (C.c_char_p, []),
+    "facetcu_run_facetrt_core": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p]),
+    "facetcu_spectral_optics": (C.c_int, [_ctx, C.POINTER(SpectralParameters), _vp,
+                                          C.POINTER(Direction), _u32, _vp]),
+    "facetcu_solve_bands": (C.c_int, [_ctx, C.POINTER(SpectralParameters), _vp,
+                                      C.POINTER(Direction), _vp, _vp, C.POINTER(BandResult)]),
 })
 OPTIONAL_SIGNATURES = {}
 MLP_INPUTS = 12
@@ -209,6 +250,105 @@ def sun_direction(zenith_deg, azimuth_deg):
     """sunDirection (facetrtcore.cpp:491-498), computed by the library."""
     d = load().facetcu_sun_direction(zenith_deg, azimuth_deg)
     return np.array([d.x, d.y, d.z], np.float32)
+
+
+def _host_check(rc):
+    if rc != OK:
+        msg = (load().facetcu_host_last_error() or b"").decode()
+        raise (ValueError if rc == INVALID_ARGUMENT else RuntimeError)(msg)
+
+
+def load_tree_with_soil(path):
+    """loadTreeWithSoil: (vertices (3F, 6) float32, material per facet,
+    leaf facet count, minimum (3,), maximum (3,))."""
+    lib = load()
+    info = SceneInfo()
+    _host_check(lib.facetcu_load_tree_with_soil(os.fsencode(path), None, None, 0, C.byref(info)))
+    F = info.facet_count
+    v = np.zeros((3 * F, 6), np.float32)
+    mat = np.zeros(F, np.uint32)
+    _host_check(lib.facetcu_load_tree_with_soil(os.fsencode(path), _ptr(v), _ptr(mat), F,
+                                                C.byref(info)))
+    return (v, mat, info.leaf_facet_count, np.array(info.minimum[:], np.float32),
+            np.array(info.maximum[:], np.float32))
+
+
+def make_optics(vertices, leaf_facet_count, sunlit, sun):
+    """makeOptics: (2F, 4) float32 [rho, tau, e, D]."""
+    v = _f32(vertices).reshape(-1, 6)
+    F = len(v) // 3
+    lit = _f32(sunlit)
+    if lit.size != 2 * F:
+        raise ValueError("sunlit must hold 2 values per facet")
+    out = np.zeros((2 * F, 4), np.float32)
+    d = Direction(*[float(x) for x in np.ravel(sun)[:3]])
+    _host_check(load().facetcu_make_optics(_ptr(v), F, leaf_facet_count, _ptr(lit), C.byref(d),
+                                           _ptr(out)))
+    return out
+
+
+def planck_radiance(wavelength, temperature):
+    return float(load().facetcu_planck_radiance(wavelength, temperature))
+
+
+def run_facetrt_core(input_path, output_file=None):
+    """runFacetRTCore: 0 on success, 1 on failure (messages on stdout/stderr)."""
+    out = os.fsencode(output_file) if output_file else None
+    return int(load().facetcu_run_facetrt_core(os.fsencode(input_path), None, out))
+
+
+class Surface:
+    """SurfaceParameters: per-band reflectance/transmittance lists (empty =
+    the reference's object/ground fallback), thermal-IR values and the
+    sunlit/shaded temperatures."""
+
+    def __init__(self, reflectance=(), transmittance=(), tir_reflectance=0.03,
+                 tir_transmittance=0.0, sunlit_temperature=300.0, shaded_temperature=296.0):
+        self.reflectance = np.asarray(reflectance, np.float32).ravel()
+        self.transmittance = np.asarray(transmittance, np.float32).ravel()
+        self.tir_reflectance = tir_reflectance
+        self.tir_transmittance = tir_transmittance
+        self.sunlit_temperature = sunlit_temperature
+        self.shaded_temperature = shaded_temperature
+
+    def struct(self):
+        return SurfaceParameters(_ptr(self.reflectance) if self.reflectance.size else None,
+                                 self.reflectance.size,
+                                 _ptr(self.transmittance) if self.transmittance.size else None,
+                                 self.transmittance.size, self.tir_reflectance,
+                                 self.tir_transmittance, self.sunlit_temperature,
+                                 self.shaded_temperature)
+
+
+def ground_surface():
+    """FacetRTParameters::ground's default (facetrtcore.cpp:143)."""
+    return Surface([0.20], [0.0], 0.05, 0.0, 305.0, 295.0)
+
+
+def spectral_parameters(wavelengths, leaf_facet_count, object_surface=None, ground=None,
+                        materials=(), material_indices=None, texture_factors=None,
+                        background_angular_strength=0.0, sky_temperature=250.0,
+                        accelerated=False):
+    """A SpectralParameters struct plus the arrays it points to (keep both)."""
+    keep = {"wl": _f32(wavelengths)}
+    obj = object_surface or Surface([0.10], [0.05])
+    gnd = ground or ground_surface()
+    mats = list(materials)
+    keep["surfaces"] = [obj, gnd] + mats
+    arr = None
+    if mats:
+        arr = (SurfaceParameters * len(mats))(*[m.struct() for m in mats])
+        keep["mats"] = arr
+    if material_indices is not None:
+        keep["mi"] = np.ascontiguousarray(material_indices, np.uint32)
+    if texture_factors is not None:
+        keep["tex"] = _f32(texture_factors)
+    p = SpectralParameters(_ptr(keep["wl"]), keep["wl"].size, obj.struct(), gnd.struct(),
+                           C.cast(arr, C.c_void_p) if arr is not None else None, len(mats),
+                           _ptr(keep["mi"]) if "mi" in keep else None,
+                           _ptr(keep["tex"]) if "tex" in keep else None, leaf_facet_count,
+                           background_angular_strength, sky_temperature, 1 if accelerated else 0)
+    return p, keep
 
 
 def device_count():
@@ -444,6 +584,29 @@ class FacetrtCuda:
             return out, res.as_dict()
         self._check(rc)
         return out, res.as_dict()
+
+    # -- spectral optics and the band loop ------------------------------------
+    def spectralOptics(self, parameters, sunlit, sun, band):
+        """makeSpectralOptics for one band: (2F, 4) float32."""
+        lit = _f32(sunlit)
+        out = np.zeros((lit.size, 4), np.float32)
+        d = Direction(*[float(x) for x in np.ravel(sun)[:3]])
+        self._check(self.lib.facetcu_spectral_optics(self.h, C.byref(parameters), _ptr(lit),
+                                                     C.byref(d), band, _ptr(out)))
+        return out
+
+    def solveBands(self, parameters, sunlit, sun):
+        """The runGpu band loop: (band radiosity (bands, 2F), light
+        enhancement (2F,), result dict)."""
+        lit = _f32(sunlit)
+        bands = np.zeros((parameters.band_count, lit.size), np.float32)
+        enh = np.zeros(lit.size, np.float32)
+        d = Direction(*[float(x) for x in np.ravel(sun)[:3]])
+        res = BandResult()
+        self._check(self.lib.facetcu_solve_bands(self.h, C.byref(parameters), _ptr(lit),
+                                                 C.byref(d), _ptr(bands), _ptr(enh),
+                                                 C.byref(res)))
+        return bands, enh, res.as_dict()
 
     # -- learned warm start -------------------------------------------------
     def mlpReset(self, seed=1):

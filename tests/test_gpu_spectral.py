@@ -1,0 +1,146 @@
+"""makeSpectralOptics and the runGpu band loop on the device against the
+reference's own functions (oracle/_ref) and the CPU solver restatement.
+
+Tolerances: optics bit-identical when the ground's angular strength is 0
+(the reference default; the Hapke terms cancel exactly), within 2e-6
+relative otherwise (CUDA vs C-library transcendentals in the Hapke
+kernel); band radiosity within 1e-5 relative of the CPU solver (FP32 state,
+FP32 vs FP64 gather); the accelerated loop within 1e-4 relative of the
+FP64 fixed point."""
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Graph
+from streamsim_gb300 import facetcu, scenes
+from tests.gpu_helpers import model_for, require_gpu
+
+pytestmark = pytest.mark.gpu
+
+WAVELENGTHS = [450.0, 550.0, 865.0, 1.6, 2500.0, 3000.0, 10000.0, 10.0]
+
+
+@pytest.fixture(scope="module")
+def case():
+    require_gpu()
+    sc = scenes.config1(seed=2, leaves=800, grid=12)
+    m = model_for(sc.vertices, 512, 64)
+    m.buildVisibilityGraph(scenes.hemisphere_directions())
+    sun = scenes.sun_direction(35.0, 120.0)
+    lit = m.computeSunlitFraction(sun)
+    F = sc.facet_count
+    rng = np.random.default_rng(4)
+    mats = [facetcu.Surface([0.05, 0.08, 0.45, 0.30, 0.22], [0.04, 0.06, 0.40], 0.02, 0.01,
+                            301.0, 297.0),
+            facetcu.Surface([], [], 0.05, 0.0, 310.0, 300.0),
+            facetcu.Surface([0.3], [0.9], 0.04, 0.2, 290.0, 285.0)]
+    mi = np.where(np.arange(F) < sc.leaf_count, rng.choice([0, 2, 7], F), 1).astype(np.uint32)
+    mi[sc.leaf_count::5] = 9  # ground facets without a material: FacetRTParameters::ground
+    tex = rng.uniform(0.8, 1.3, F).astype(np.float32)
+    yield dict(scene=sc, model=m, sun=sun, lit=lit, mats=mats, mi=mi, tex=tex,
+               graph=Graph(*m.graph()))
+    m.close()
+
+
+def _params(c, strength=0.0, accelerated=False, wavelengths=WAVELENGTHS):
+    return facetcu.spectral_parameters(
+        wavelengths, c["scene"].leaf_count,
+        object_surface=facetcu.Surface([0.11, 0.12], [0.05], 0.03, 0.0, 300.0, 296.0),
+        ground=facetcu.ground_surface(), materials=c["mats"], material_indices=c["mi"],
+        texture_factors=c["tex"], background_angular_strength=strength, sky_temperature=250.0,
+        accelerated=accelerated)
+
+
+def _ref_optics(reference, c, band, strength, wavelengths=WAVELENGTHS):
+    return reference.make_spectral_optics(
+        c["scene"].vertices, c["scene"].leaf_count, c["lit"], 35.0, 120.0, wavelengths, band,
+        facetcu.Surface([0.11, 0.12], [0.05], 0.03, 0.0, 300.0, 296.0), facetcu.ground_surface(),
+        c["mats"], c["mi"], c["tex"], strength, 250.0)
+
+
+def test_spectral_optics_bit_identical_at_default_strength(reference, case):
+    p, keep = _params(case)
+    for b in range(len(WAVELENGTHS)):
+        ours = case["model"].spectralOptics(p, case["lit"], case["sun"], b)
+        theirs = _ref_optics(reference, case, b, 0.0)
+        assert np.array_equal(ours.view(np.uint32), theirs.view(np.uint32)), WAVELENGTHS[b]
+
+
+def test_spectral_optics_with_angular_ground(reference, case):
+    p, keep = _params(case, strength=0.6)
+    for b in range(len(WAVELENGTHS)):
+        ours = case["model"].spectralOptics(p, case["lit"], case["sun"], b)
+        theirs = _ref_optics(reference, case, b, 0.6)
+        assert np.allclose(ours, theirs, rtol=2e-6, atol=1e-7), WAVELENGTHS[b]
+        # object sides have no angular term: exact
+        S_obj = 2 * case["scene"].leaf_count
+        assert np.array_equal(ours[:S_obj], theirs[:S_obj])
+
+
+def _reference_loop(reference, oracle, c, wavelengths):
+    """The band loop of runGpu (facetrtcore.cpp:1677-1773), traditional
+    solver, on the CPU: reference optics, the oracle's 64-sweep solve."""
+    ref_irr = 700.0 * max(0.0, float(c["sun"][1])) + 50.0
+    out = []
+    for b, wl in enumerate(wavelengths):
+        o = _ref_optics(reference, c, b, 0.0, wavelengths)
+        optical = (wl * 1000.0 if wl <= 2.5 else wl) <= 2500.0
+        sky = 50.0 if optical else reference.planck(wl, 250.0)
+        B, md = oracle.solve(c["graph"], o, sky, 64)
+        if optical:
+            B = np.clip(B / np.float32(ref_irr), 0.0, 1.0)
+        out.append(B)
+        if b == 0:
+            o[:, 3] = 0.0
+            Bd, _ = oracle.solve(c["graph"], o, sky, 64)
+            if optical:
+                Bd = np.clip(Bd / np.float32(ref_irr), 0.0, 1.0)
+            enh = np.maximum(0.0, out[0] - Bd)
+            md0 = md
+    return np.array(out), enh, md0
+
+
+def test_band_loop_matches_cpu_band_loop(reference, oracle, case):
+    p, keep = _params(case)
+    bands, enh, res = case["model"].solveBands(p, case["lit"], case["sun"])
+    ref_bands, ref_enh, md0 = _reference_loop(reference, oracle, case, WAVELENGTHS)
+    assert res["iterations"] == 64 and res["batched_sweeps"] == 64
+    assert res["thermal_bands"] == 3
+    for b in range(len(WAVELENGTHS)):
+        scale = np.maximum(np.abs(ref_bands[b]), 1e-6 * np.abs(ref_bands[b]).max())
+        assert np.max(np.abs(bands[b] - ref_bands[b]) / scale) < 1e-5, WAVELENGTHS[b]
+    assert np.max(np.abs(enh - ref_enh)) < 1e-5
+    assert abs(res["max_delta"] - md0) <= 1e-3 * max(md0, 1e-6) + 1e-6
+
+
+def test_band_loop_thermal_first_band_has_no_enhancement(reference, oracle, case):
+    wl = [10000.0, 550.0]
+    p, keep = _params(case, wavelengths=wl)
+    bands, enh, res = case["model"].solveBands(p, case["lit"], case["sun"])
+    assert np.all(enh == 0.0) and res["thermal_bands"] == 1
+    ref_bands, _, _ = _reference_loop(reference, oracle, case, wl)
+    assert np.allclose(bands, ref_bands, rtol=1e-5, atol=1e-6)
+
+
+def test_accelerated_band_loop_reaches_the_fixed_point(reference, oracle, case):
+    p, keep = _params(case, accelerated=True)
+    bands, enh, res = case["model"].solveBands(p, case["lit"], case["sun"])
+    ref_irr = 700.0 * max(0.0, float(case["sun"][1])) + 50.0
+    for b, wl in enumerate(WAVELENGTHS):
+        o = _ref_optics(reference, case, b, 0.0)
+        optical = (wl * 1000.0 if wl <= 2.5 else wl) <= 2500.0
+        sky = 50.0 if optical else reference.planck(wl, 250.0)
+        B64, _ = oracle.solve_f64(case["graph"], o, sky)
+        if optical:
+            B64 = np.clip(B64 / ref_irr, 0.0, 1.0)
+        scale = np.maximum(np.abs(B64), 1e-3 * np.abs(B64).max())
+        assert np.max(np.abs(bands[b] - B64) / scale) < 1e-4, wl
+    assert res["iterations"] <= 64
+
+
+def test_band_loop_argument_checks(case):
+    p, keep = _params(case)
+    with pytest.raises(ValueError):
+        case["model"].spectralOptics(p, case["lit"], case["sun"], len(WAVELENGTHS))
+    bad, keep2 = _params(case, wavelengths=[550.0, float("nan")])
+    with pytest.raises(ValueError):
+        case["model"].solveBands(bad, case["lit"], case["sun"])

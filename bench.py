@@ -327,9 +327,9 @@ def run_gpu(args, rank, world, local):
     # (profiles/k_defect_wide_config2.md); only valid for this workload.
     try:
         for line in open(os.path.join(ROOT, "profiles", "sweep_traffic.txt")):
-            name, value = line.split()
+            name, dram_bytes = line.split()
             if name == kname and not args.quick and args.bands == 64:
-                roofline["traffic"] = float(value)
+                roofline["traffic"] = float(dram_bytes)
     except (OSError, ValueError):
         pass
     roofline["l2_gather_bytes_per_launch"] = float(w["vf"]["directed_edges"]) * \

@@ -910,7 +910,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
         uint32_t host_flag[3] = {0, 0, 0};
         if (!mixed) {
             while (it < max_it) {
-                const uint32_t batch = std::min(check_every, max_it - it);
+                const uint32_t batch = std::min(timed ? 1u : check_every, max_it - it);
                 for (uint32_t k = 0; k < batch; ++k) {
                     const uint32_t sweep = it + k;
                     char* in = (sweep & 1u) ? x1 : x0;
@@ -932,7 +932,10 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                 it += batch;
                 FCU_CHECK(cudaMemcpyAsync(host_flag, flag, 12, cudaMemcpyDeviceToHost, s));
                 FCU_CHECK(cudaStreamSynchronize(s));
-                if (host_flag[0]) break;
+                if (host_flag[0]) {
+                    sweeps -= it - host_flag[1];  // launched after the done flag: no work
+                    break;
+                }
             }
             cur = int(host_flag[1] & 1u);
         } else {
@@ -965,12 +968,17 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                 __nv_bfloat16* din = d0;
                 __nv_bfloat16* dout = d1;
                 bool cycle_done = false;
+                // The defect sweeps read the cycle's own done flag (flag + 3):
+                // once k_check has seen the target drop, the remaining sweeps
+                // of the batch return at once and leave X and the defect
+                // buffers untouched.  Timed runs check after every sweep so
+                // that no such empty launch is timed.
                 while (!cycle_done && it < max_it) {
-                    const uint32_t batch = std::min(check_every, max_it - it);
+                    const uint32_t batch = std::min(timed ? 1u : check_every, max_it - it);
                     uint32_t sub_flag[3];
                     for (uint32_t k = 0; k < batch; ++k) {
                         timed_sweep(true, [&] {
-                            launch_defect(P, g, pp, din, dout, X, stats, counter, flag, s);
+                            launch_defect(P, g, pp, din, dout, X, stats, counter, flag + 3, s);
                         });
                         std::swap(din, dout);
                         k_check<<<1, kMaxP, 0, s>>>(stats, flag + 3, P,
@@ -984,6 +992,8 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                     FCU_CHECK(cudaStreamSynchronize(s));
                     if (sub_flag[0]) {
                         cycle_done = true;
+                        sweeps -= it - sub_flag[1];  // skipped after the target drop
+                        it = sub_flag[1];
                         FCU_CHECK(cudaMemsetAsync(flag + 3, 0, 12, s));
                     }
                 }

@@ -316,7 +316,7 @@ def run_gpu(args, rank, world, local):
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     achieved = rt["sweep_bytes"] / max(rt["sweep_seconds"], 1e-12) / 1e9
     panel = min(128, 1 << (B - 1).bit_length())
-    kname = (f"k_defect_wide<{panel}>" if prec == fc.PRECISION_MIXED else f"k_sweep_wide<{panel}>")
+    kname = (f"k_step_i8<{panel}>" if prec == fc.PRECISION_MIXED else f"k_sweep_wide<{panel}>")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": None, "kernel": kname,
                 "launches_timed": rt["timed_sweeps"],
@@ -333,7 +333,7 @@ def run_gpu(args, rank, world, local):
     except (OSError, ValueError):
         pass
     roofline["l2_gather_bytes_per_launch"] = float(w["vf"]["directed_edges"]) * \
-        (panel * (2 if prec == fc.PRECISION_MIXED else 4))
+        (panel * (1 if prec == fc.PRECISION_MIXED else 4))
 
     # end to end through the host-buffer C ABI (pinned buffers, copies timed)
     pin = {k: torch.from_numpy(np.ascontiguousarray(w[k])).pin_memory()
@@ -394,7 +394,7 @@ def run_gpu(args, rank, world, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16+f32" if prec == fc.PRECISION_MIXED else "f32",
+            "dtype": "i8+f32" if prec == fc.PRECISION_MIXED else "f32",
             "data": "synthetic (seeded scene generator, no dataset)",
             "config": {"workload": workload_name(args, w), "facets": sc.facet_count,
                        "sides": S, "bands": B, "suns": 1,

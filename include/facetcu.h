@@ -203,7 +203,7 @@ int facetcu_incident_irradiance(facetcu_context *ctx, const float *radiosity,
  * (radiosity[r*S + s]). */
 enum {
     FACETCU_PRECISION_FP32 = 0,     /* FP32 gather */
-    FACETCU_PRECISION_MIXED = 1,    /* BF16 defect gather + FP32 residual correction */
+    FACETCU_PRECISION_MIXED = 1,    /* FP32 state and residual; int8 steps (BF16 defects below 32 columns) */
     FACETCU_PRECISION_FP64 = 2      /* FP64 state and gather (reference truth) */
 };
 enum {

@@ -346,7 +346,8 @@ int facetcu_destroy(facetcu_context* ctx)
                             &ctx->rad_b, &ctx->residual, &ctx->host_io, &ctx->scratch,
                             &ctx->sun_total, &ctx->sun_visible, &ctx->batch.x0, &ctx->batch.x1,
                             &ctx->batch.half, &ctx->batch.colstats, &ctx->batch.q,
-                            &ctx->batch.corr, &ctx->batch_inputs})
+                            &ctx->batch.corr, &ctx->batch.i8, &ctx->batch_inputs, &ctx->spec_io,
+                            &ctx->spec.dev})
         b->release();
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     ctx->stream = nullptr;

@@ -25,10 +25,12 @@
 // Precision modes:
 //   FP32  — panel and gather in FP32;
 //   FP64  — the same sweep in double (the truth the 1e-4 bar is checked on);
-//   MIXED — defect iteration: an FP32 sweep gives d = B' - B; then
-//           d <- K d runs with d stored in BF16 (half the gather bytes),
-//           accumulated in FP32 and added to the FP32 panel; every cycle
-//           restarts from a fresh FP32 sweep (the FP32 residual correction).
+//   MIXED — FP32 state with low-precision corrections.  Panels of 32 or
+//           more columns: an FP32 sweep, then residual-tracked int8 steps
+//           (per-column scale, exact int32 gather sums, FP32 residual; see
+//           k_step_i8), then a verifying FP32 sweep.  Narrower panels:
+//           defect cycles, d <- K d with d stored in BF16 and accumulated in
+//           FP32, each cycle restarted from a fresh FP32 sweep.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -172,7 +174,56 @@ template <> struct Vec16<true> {  // 8 x BF16
 
 // acc[k] += sum over edges e of side s of count_e * X[n_e][col0 + k], where
 // col0 = (lane % L) * CPL; valid in every lane after the fold (lanes of the
-// same sub-index hold the same sums).
+// same sub-index hold the same sums).  kGatherU vector loads per lane are in
+// flight at once (raw 16-byte words, unpacked at the multiply-add), and with
+// kPrefetch the next 32-edge chunk's packed edges are loaded while the
+// current chunk is gathered.
+#ifndef FCU_GATHER_U
+#define FCU_GATHER_U 8
+#endif
+#ifndef FCU_PREFETCH
+#define FCU_PREFETCH 1
+#endif
+#ifndef FCU_MIN_BLOCKS
+#define FCU_MIN_BLOCKS 3
+#endif
+constexpr int kGatherU = FCU_GATHER_U;
+constexpr bool kPrefetch = FCU_PREFETCH != 0;
+constexpr int kMinBlocks = FCU_MIN_BLOCKS;
+
+__device__ __forceinline__ void edge_word(const uint32_t* __restrict__ packed,
+                                          const facetcu_csr_edge* __restrict__ edges, uint32_t e,
+                                          uint32_t& nb, float& c)
+{
+    if (packed) {
+        const uint32_t p = __ldg(packed + e);
+        nb = p & kNeighborMask;
+        c = float(p >> 22);
+    } else {
+        const uint2 w = __ldg(reinterpret_cast<const uint2*>(edges) + e);
+        nb = w.x;
+        c = float(w.y);
+    }
+}
+
+template <bool kBF16>
+__device__ __forceinline__ void unpack16(const uint4& q, float* v)
+{
+    if constexpr (kBF16) {
+        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            v[2 * i] = __uint_as_float(w[i] << 16);
+            v[2 * i + 1] = __uint_as_float(w[i] & 0xFFFF0000u);
+        }
+    } else {
+        v[0] = __uint_as_float(q.x);
+        v[1] = __uint_as_float(q.y);
+        v[2] = __uint_as_float(q.z);
+        v[3] = __uint_as_float(q.w);
+    }
+}
+
 template <int P, bool kBF16>
 __device__ __forceinline__ void gather_split(const uint32_t* __restrict__ rows,
                                              const uint32_t* __restrict__ packed,
@@ -182,26 +233,27 @@ __device__ __forceinline__ void gather_split(const uint32_t* __restrict__ rows,
     constexpr int CPL = Vec16<kBF16>::kCols;
     constexpr int L = P / CPL;  // lanes per row = 16-byte vectors per row
     constexpr int G = 32 / L;   // edges per load instruction
-    constexpr int U = 4;
+    constexpr int U = kGatherU;
     const int grp = lane / L, sub = lane % L;
+    const uint4* __restrict__ X16 = reinterpret_cast<const uint4*>(X);
     const uint32_t start = __ldg(rows + s), end = __ldg(rows + s + 1);
+    uint32_t nbn = 0;
+    float cn = 0.0f;
+    if (kPrefetch && start + uint32_t(lane) < end) edge_word(packed, edges, start + lane, nbn, cn);
     for (uint32_t base = start; base < end; base += 32) {
         const uint32_t n = min(32u, end - base);
         uint32_t nbv = 0;
         float cv = 0.0f;
-        if (uint32_t(lane) < n) {
-            if (packed) {
-                const uint32_t p = __ldg(packed + base + lane);
-                nbv = p & kNeighborMask;
-                cv = float(p >> 22);
-            } else {
-                const uint2 e = __ldg(reinterpret_cast<const uint2*>(edges) + base + lane);
-                nbv = e.x;
-                cv = float(e.y);
-            }
+        if constexpr (kPrefetch) {
+            nbv = nbn;
+            cv = cn;
+            const uint32_t next = base + 32u + uint32_t(lane);
+            if (next < end) edge_word(packed, edges, next, nbn, cn);
+        } else if (uint32_t(lane) < n) {
+            edge_word(packed, edges, base + lane, nbv, cv);
         }
         for (uint32_t j = 0; j < n; j += G * U) {
-            float v[U][CPL];
+            uint4 q[U];
             float c[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
@@ -210,17 +262,19 @@ __device__ __forceinline__ void gather_split(const uint32_t* __restrict__ rows,
                 const uint32_t nb = __shfl_sync(0xffffffffu, nbv, src);
                 c[u] = __shfl_sync(0xffffffffu, cv, src);
                 if (idx < n) {
-                    Vec16<kBF16>::load(X, size_t(nb) * L + sub, v[u]);
+                    q[u] = __ldg(X16 + size_t(nb) * L + sub);
                 } else {
                     c[u] = 0.0f;
-#pragma unroll
-                    for (int k = 0; k < CPL; ++k) v[u][k] = 0.0f;
+                    q[u] = make_uint4(0u, 0u, 0u, 0u);
                 }
             }
 #pragma unroll
-            for (int u = 0; u < U; ++u)
+            for (int u = 0; u < U; ++u) {
+                float v[CPL];
+                unpack16<kBF16>(q[u], v);
 #pragma unroll
-                for (int k = 0; k < CPL; ++k) acc[k] += c[u] * v[u][k];
+                for (int k = 0; k < CPL; ++k) acc[k] += c[u] * v[k];
+            }
         }
     }
 #pragma unroll
@@ -294,7 +348,7 @@ __device__ __forceinline__ void publish_stats(const float* md, const float* mb, 
 
 // One full FP32 sweep B_out = Q + K B_in over a wide panel.
 template <int P>
-__global__ void __launch_bounds__(kWarps * 32, 3) k_sweep_wide(GraphView g, PanelParams pp,
+__global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_sweep_wide(GraphView g, PanelParams pp,
                                                             const float* __restrict__ Bin,
                                                             float* __restrict__ Bout,
                                                             uint32_t* stats, uint32_t* counter,
@@ -363,7 +417,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_sweep_wide(GraphView g, Pane
 // Defect sweep over a wide panel: d_out = K d_in (BF16 in and out, FP32
 // accumulation), X += d_out.  Stats: max|d_out|, max|X|.
 template <int P>
-__global__ void __launch_bounds__(kWarps * 32, 3) k_defect_wide(GraphView g, PanelParams pp,
+__global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_defect_wide(GraphView g, PanelParams pp,
                                                              const __nv_bfloat16* __restrict__ Din,
                                                              __nv_bfloat16* __restrict__ Dout,
                                                              float* __restrict__ X, uint32_t* stats,
@@ -440,6 +494,276 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_defect_wide(GraphView g, Pan
         }
     }
     publish_cols<CPL>(md, mb, col0, owner, P, stats);
+}
+
+// ---- residual-tracked int8 steps (MIXED, wide panels) --------------------
+// State per cell: X (FP32 iterate), R = T(X) - X (FP32, its Jacobi
+// residual) and Q = round(R / sigma) (int8, one scale sigma per column, not
+// yet applied).  One step applies the quantized residual and updates the
+// residual by exactly what was applied:
+//   delta = sigma_in * Q_in,  X += delta,  R += K delta - delta,
+//   Q_out = round(R / sigma_out),  sigma_out = max|R_in| / 127,
+// where K delta comes from gathering the int8 neighbour rows (count * q
+// summed exactly in int32).  R stays the true residual of X up to FP32
+// rounding, so the int8 rounding only perturbs the step: max|R| contracts by
+// about c + (1 + c) / 254 per step (c the spectral radius of K), as with a
+// BF16 defect, while each gathered neighbour row is half as wide and no
+// periodic FP32 correction sweep is needed.  |R_out| < max|R_in| because
+// c < 1, so Q_out fits in [-127, 127] (clamped all the same).
+
+__device__ __forceinline__ void edge_word_i(const uint32_t* __restrict__ packed,
+                                            const facetcu_csr_edge* __restrict__ edges,
+                                            uint32_t e, uint32_t& nb, int& c)
+{
+    if (packed) {
+        const uint32_t w = __ldg(packed + e);
+        nb = w & kNeighborMask;
+        c = int(w >> 22);
+    } else {
+        const uint2 w = __ldg(reinterpret_cast<const uint2*>(edges) + e);
+        nb = w.x;
+        c = int(w.y);
+    }
+}
+
+// Sign-extended byte k of w (PTX prmt with the sign-replicate selector bit).
+template <int k>
+__device__ __forceinline__ int sbyte(uint32_t w)
+{
+    constexpr uint32_t sel = uint32_t(k) | ((uint32_t(k) | 8u) << 4) | ((uint32_t(k) | 8u) << 8) |
+                             ((uint32_t(k) | 8u) << 12);
+    uint32_t d;
+    asm("prmt.b32 %0, %1, 0, %2;" : "=r"(d) : "r"(w), "n"(sel));
+    return int(d);
+}
+
+// acc[0..16) += sum over edges of side s of count * Q[n][sub * 16 + k]; the
+// G lane groups each take every G-th edge (partial sums).  Eight 16-byte
+// loads per lane are in flight per round; the next round's packed edges are
+// prefetched.
+template <int P>
+__device__ __forceinline__ void gather_i8(const uint32_t* __restrict__ rows,
+                                          const uint32_t* __restrict__ packed,
+                                          const facetcu_csr_edge* __restrict__ edges, uint32_t s,
+                                          const int8_t* __restrict__ Q, int lane, int* acc)
+{
+    constexpr int L = P / 16;              // lanes per row, 16 bytes each
+    constexpr int G = 32 / L;              // edges per load instruction
+    constexpr int W = G >= 4 ? G / 4 : 1;  // packed words per lane per round
+    constexpr int E = 32 * W;              // edges per round
+    constexpr int U = E / G;               // loads per lane per round
+    const int grp = lane / L, sub = lane % L;
+    const uint4* __restrict__ Q16 = reinterpret_cast<const uint4*>(Q);
+    const uint32_t start = __ldg(rows + s), end = __ldg(rows + s + 1);
+    uint32_t nbn[W];
+    int cn[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        nbn[w] = 0u;
+        cn[w] = 0;
+        const uint32_t e = start + uint32_t(w * 32 + lane);
+        if (e < end) edge_word_i(packed, edges, e, nbn[w], cn[w]);
+    }
+    for (uint32_t base = start; base < end; base += E) {
+        uint32_t nbv[W];
+        int cv[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            nbv[w] = nbn[w];
+            cv[w] = cn[w];
+            nbn[w] = 0u;
+            cn[w] = 0;
+            const uint32_t e = base + uint32_t(E + w * 32 + lane);
+            if (e < end) edge_word_i(packed, edges, e, nbn[w], cn[w]);
+        }
+        uint4 q[U];
+        int c[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int src = (u * G + grp) & 31;
+            const uint32_t nb = __shfl_sync(0xffffffffu, nbv[(u * G) >> 5], src);
+            c[u] = __shfl_sync(0xffffffffu, cv[(u * G) >> 5], src);
+            if (base + uint32_t(u * G + grp) < end) {
+                q[u] = __ldg(Q16 + size_t(nb) * L + sub);
+            } else {
+                q[u] = make_uint4(0u, 0u, 0u, 0u);
+                c[u] = 0;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t wd[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                acc[4 * i + 0] += c[u] * sbyte<0>(wd[i]);
+                acc[4 * i + 1] += c[u] * sbyte<1>(wd[i]);
+                acc[4 * i + 2] += c[u] * sbyte<2>(wd[i]);
+                acc[4 * i + 3] += c[u] * sbyte<3>(wd[i]);
+            }
+        }
+    }
+}
+
+// Sum the G groups' partial sums and scatter: afterwards a[0 .. 16 / G) of
+// lane (grp, sub) are the totals of columns sub * 16 + i8_offset<G>(grp) + i.
+template <int G, int L>
+__device__ __forceinline__ void reduce_scatter_i8(int* a, int lane)
+{
+    const int grp = lane / L;
+#pragma unroll
+    for (int lvl = 0; (1 << lvl) < G; ++lvl) {
+        const bool hi = ((grp >> lvl) & 1) != 0;
+        const int half = 16 >> (lvl + 1);
+#pragma unroll
+        for (int i = 0; i < half; ++i) {
+            const int send = hi ? a[i] : a[i + half];
+            const int keep = hi ? a[i + half] : a[i];
+            a[i] = keep + __shfl_xor_sync(0xffffffffu, send, L << lvl);
+        }
+    }
+}
+
+template <int G>
+__device__ __forceinline__ int i8_offset(int grp)
+{
+    int off = 0;
+#pragma unroll
+    for (int lvl = 0; (1 << lvl) < G; ++lvl) off += ((grp >> lvl) & 1) * (16 >> (lvl + 1));
+    return off;
+}
+
+template <int N> struct VecN;
+template <> struct VecN<1> {
+    static __device__ __forceinline__ void ld(const float* p, float* v) { v[0] = *p; }
+    static __device__ __forceinline__ void st(float* p, const float* v) { *p = v[0]; }
+    static __device__ __forceinline__ void ldq(const int8_t* p, int* v) { v[0] = *p; }
+    static __device__ __forceinline__ void stq(int8_t* p, const int* v) { *p = int8_t(v[0]); }
+};
+template <> struct VecN<2> {
+    static __device__ __forceinline__ void ld(const float* p, float* v)
+    {
+        const float2 q = *reinterpret_cast<const float2*>(p);
+        v[0] = q.x;
+        v[1] = q.y;
+    }
+    static __device__ __forceinline__ void st(float* p, const float* v)
+    {
+        *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+    }
+    static __device__ __forceinline__ void ldq(const int8_t* p, int* v)
+    {
+        const char2 q = *reinterpret_cast<const char2*>(p);
+        v[0] = q.x;
+        v[1] = q.y;
+    }
+    static __device__ __forceinline__ void stq(int8_t* p, const int* v)
+    {
+        *reinterpret_cast<char2*>(p) = make_char2(char(v[0]), char(v[1]));
+    }
+};
+template <> struct VecN<4> {
+    static __device__ __forceinline__ void ld(const float* p, float* v) { load4(p, v); }
+    static __device__ __forceinline__ void st(float* p, const float* v) { store4(p, v); }
+    static __device__ __forceinline__ void ldq(const int8_t* p, int* v)
+    {
+        const char4 q = *reinterpret_cast<const char4*>(p);
+        v[0] = q.x;
+        v[1] = q.y;
+        v[2] = q.z;
+        v[3] = q.w;
+    }
+    static __device__ __forceinline__ void stq(int8_t* p, const int* v)
+    {
+        *reinterpret_cast<char4*>(p) = make_char4(char(v[0]), char(v[1]), char(v[2]), char(v[3]));
+    }
+};
+
+template <int P>
+__global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_step_i8(
+    GraphView g, PanelParams pp, const int8_t* __restrict__ Qin, int8_t* __restrict__ Qout,
+    float* __restrict__ X, float* __restrict__ R, const float* __restrict__ sig_in,
+    const float* __restrict__ sig_out, uint32_t* stats, uint32_t* counter, const uint32_t* done)
+{
+    if (*done) return;
+    constexpr int L = P / 16, G = 32 / L, NC = P / 32;
+    const int lane = threadIdx.x & 31;
+    const int col0 = (lane % L) * 16 + i8_offset<G>(lane / L);
+    float si[NC], inv_so[NC], md[NC], mb[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        si[k] = sig_in[col0 + k];
+        const float so = sig_out[col0 + k];
+        inv_so[k] = so > 0.0f ? 1.0f / so : 0.0f;
+        md[k] = 0.0f;
+        mb[k] = 0.0f;
+    }
+    const uint32_t chunks = (g.facets + kChunk - 1) / kChunk;
+    for (uint32_t ch = next_chunk(counter, lane); ch < chunks; ch = next_chunk(counter, lane)) {
+        const uint32_t fe = min(g.facets, (ch + 1) * kChunk);
+        for (uint32_t f = ch * kChunk; f < fe; ++f) {
+            float h[2][NC];
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                const uint32_t s = 2u * f + side;
+                int acc[16];
+#pragma unroll
+                for (int k = 0; k < 16; ++k) acc[k] = 0;
+                gather_i8<P>(g.rows, g.packed, g.edges, s, Qin, lane, acc);
+                reduce_scatter_i8<G, L>(acc, lane);
+                const uint32_t d = __ldg(g.denom + s);
+                const float inv = d ? 1.0f / float(d) : 0.0f;
+#pragma unroll
+                for (int k = 0; k < NC; ++k) h[side][k] = float(acc[k]) * si[k] * inv;
+            }
+            const size_t i0 = size_t(2u * f) * P + col0, i1 = i0 + P;
+            float r0[NC], r1[NC], t0[NC], t1[NC], x0[NC], x1[NC], e0[NC], e1[NC];
+            int q0[NC], q1[NC];
+            VecN<NC>::ld(pp.rho + i0, r0);
+            VecN<NC>::ld(pp.rho + i1, r1);
+            VecN<NC>::ld(pp.tau + i0, t0);
+            VecN<NC>::ld(pp.tau + i1, t1);
+            VecN<NC>::ld(X + i0, x0);
+            VecN<NC>::ld(X + i1, x1);
+            VecN<NC>::ld(R + i0, e0);
+            VecN<NC>::ld(R + i1, e1);
+            VecN<NC>::ldq(Qin + i0, q0);
+            VecN<NC>::ldq(Qin + i1, q1);
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                const float kd0 = r0[k] * h[0][k] + t0[k] * h[1][k];
+                const float kd1 = r1[k] * h[1][k] + t1[k] * h[0][k];
+                const float dl0 = si[k] * float(q0[k]), dl1 = si[k] * float(q1[k]);
+                x0[k] += dl0;
+                x1[k] += dl1;
+                e0[k] = e0[k] - dl0 + kd0;
+                e1[k] = e1[k] - dl1 + kd1;
+                q0[k] = max(-127, min(127, __float2int_rn(e0[k] * inv_so[k])));
+                q1[k] = max(-127, min(127, __float2int_rn(e1[k] * inv_so[k])));
+                md[k] = fmaxf(md[k], fmaxf(fabsf(e0[k]), fabsf(e1[k])));
+                mb[k] = fmaxf(mb[k], fmaxf(fabsf(x0[k]), fabsf(x1[k])));
+            }
+            VecN<NC>::st(X + i0, x0);
+            VecN<NC>::st(X + i1, x1);
+            VecN<NC>::st(R + i0, e0);
+            VecN<NC>::st(R + i1, e1);
+            VecN<NC>::stq(Qout + i0, q0);
+            VecN<NC>::stq(Qout + i1, q1);
+        }
+    }
+    publish_cols<NC>(md, mb, col0, true, P, stats);
+}
+
+// R = Y - X and Q = round(R / sigma) for the first int8 step (X unchanged).
+__global__ void k_init_i8(const float* __restrict__ X, const float* __restrict__ Y,
+                          float* __restrict__ R, int8_t* __restrict__ Q,
+                          const float* __restrict__ sig, size_t n, int P)
+{
+    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float r = Y[i] - X[i];
+    const float sg = sig[i % size_t(P)];
+    R[i] = r;
+    Q[i] = int8_t(sg > 0.0f ? max(-127, min(127, __float2int_rn(r / sg))) : 0);
 }
 
 // Narrow-panel sweep (FP32 or FP64 state; also used for the FP64 truth).
@@ -532,9 +856,11 @@ __global__ void k_defect_init(const float* Bold, const float* Bnew, __nv_bfloat1
 
 // Convergence check after sweep `it` (0-based): every column must satisfy
 // max|dB| <= tol * max|B|.  flag[0] = done, flag[1] = sweeps run, flag[2] =
-// max relative change bits of the last sweep.  Clears the stats.
+// max relative change bits of the last sweep.  Clears the stats.  With
+// scale_a / scale_b, also stores max|dB| / 127 per column there (the int8
+// step scales).
 __global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint32_t it,
-                        uint32_t* counter)
+                        uint32_t* counter, float* scale_a = nullptr, float* scale_b = nullptr)
 {
     __shared__ int all_ok;
     __shared__ float worst;
@@ -550,6 +876,9 @@ __global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint3
         const float rel = mb > 0.0f ? md / mb : (md > 0.0f ? INFINITY : 0.0f);
         if (!(md <= tol * mb) && !(md == 0.0f)) atomicExch(&all_ok, 0);
         atomicMax(reinterpret_cast<int*>(&worst), __float_as_int(rel));
+        // int8 step scales: sigma = max|R| / 127 for the column
+        if (scale_a && !already) scale_a[threadIdx.x] = md / 127.0f;
+        if (scale_b && !already) scale_b[threadIdx.x] = md / 127.0f;
     }
     __syncthreads();
     if (threadIdx.x == 0 && !already) {
@@ -763,6 +1092,33 @@ void launch_defect(int P, const GraphView& g, const PanelParams& pp, const __nv_
     FCU_LAUNCH("k_sweep_defect");
 }
 
+void launch_step_i8(int P, const GraphView& g, const PanelParams& pp, const int8_t* qin,
+                    int8_t* qout, float* X, float* R, const float* sin, const float* sout,
+                    uint32_t* stats, uint32_t* counter, const uint32_t* done, cudaStream_t s)
+{
+    switch (P) {
+    case 32: {
+        static const int grid = grid_for(k_step_i8<32>);
+        k_step_i8<32><<<grid, kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin, sout, stats,
+                                                   counter, done);
+        break;
+    }
+    case 64: {
+        static const int grid = grid_for(k_step_i8<64>);
+        k_step_i8<64><<<grid, kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin, sout, stats,
+                                                   counter, done);
+        break;
+    }
+    default: {
+        static const int grid = grid_for(k_step_i8<128>);
+        k_step_i8<128><<<grid, kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin, sout, stats,
+                                                    counter, done);
+        break;
+    }
+    }
+    FCU_LAUNCH("k_step_i8");
+}
+
 // Panel widths: power of two, at most `cap` (128 for FP32/BF16 with a
 // packed graph, 32 otherwise), at least the remaining columns when fewer.
 int panel_width(uint32_t remaining, uint32_t requested, uint32_t cap)
@@ -831,11 +1187,22 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
     char* x0 = static_cast<char*>(st.x0.reserve(cells_max * elem));
     char* x1 = static_cast<char*>(st.x1.reserve(cells_max * elem));
     float* prm = static_cast<float*>(st.q.reserve(cells_max * 4 * 4 + kMaxP * 4));
-    uint32_t* stats = static_cast<uint32_t*>(st.colstats.reserve((2 * kMaxP + 16) * 4));
+    uint32_t* stats = static_cast<uint32_t*>(st.colstats.reserve((4 * kMaxP + 16) * 4));
     uint32_t* flag = stats + 2 * kMaxP;
     uint32_t* counter = flag + 8;
+    float* sig = reinterpret_cast<float*>(flag + 16);  // two slots of kMaxP int8 step scales
+    // MIXED: wide panels run int8 steps (two int8 panels + the FP32
+    // residual), narrow ones BF16 defect cycles (two BF16 panels).
+    const bool wide_mixed = mixed && Pmax >= 32;
     __nv_bfloat16* dbuf = nullptr;
+    int8_t* qbuf = nullptr;
+    float* rbuf = nullptr;
+    // (a trailing panel of fewer than 32 columns takes the BF16 path)
     if (mixed) dbuf = static_cast<__nv_bfloat16*>(st.half.reserve(cells_max * 2 * 2));
+    if (wide_mixed) {
+        qbuf = static_cast<int8_t*>(st.i8.reserve(cells_max * 2));
+        rbuf = static_cast<float*>(st.corr.reserve(cells_max * 4));
+    }
 
     uint32_t worst_iterations = 0, corrections = 0, launches = 0, sweeps = 0, timed_sweeps = 0;
     double sweep_seconds = 0.0, sweep_bytes = 0.0;
@@ -870,8 +1237,10 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
         // Per-cell bytes: full sweep = state in + out + rho, tau, emission,
         // direct; defect sweep = BF16 defect in + out + X read-modify-write +
         // rho, tau.  Only the dominant kind is timed (defect sweeps in MIXED).
+        // int8 step: own Q in + Q out (1 + 1), X and R read-modify-write
+        // (8 + 8), rho and tau (8) per cell.
         const double full_bytes = graph_bytes + double(cells) * (double(elem) * 2.0 + 16.0);
-        const double defect_bytes = graph_bytes + double(cells) * 20.0;
+        const double defect_bytes = graph_bytes + double(cells) * (P >= 32 ? 26.0 : 20.0);
         auto timed_sweep = [&](bool defect, auto&& launch) {
             const bool count = timed && (defect == mixed);
             if (count) FCU_CHECK(cudaEventRecord(t0, s));
@@ -938,6 +1307,71 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                 }
             }
             cur = int(host_flag[1] & 1u);
+        } else if (P >= 32) {
+            // FP32 sweep; then residual-tracked int8 steps until max|R| <=
+            // tol/4 max|X|; then the FP32 sweep again verifies max|dB| <=
+            // tol max|B| (and restarts the steps in the rare case it does
+            // not hold).  The int8 rounding leaves a residual of about the
+            // same absolute size on every side, where a Jacobi iterate's
+            // residual shrinks with the side's radiosity; the steps are
+            // therefore run a factor 4 (two steps) below the tolerance so
+            // that dim sides meet the same relative accuracy.
+            const float step_tol = tol * 0.25f;
+            float* X = reinterpret_cast<float*>(x0);
+            float* Y = reinterpret_cast<float*>(x1);
+            int8_t* qb[2] = {qbuf, qbuf + cells};
+            float* slot[2] = {sig, sig + kMaxP};
+            while (it < max_it) {
+                timed_sweep(false, [&] {
+                    launch_sweep<float>(P, g, pp, X, Y, stats, counter, flag, s);
+                });
+                k_check<<<1, kMaxP, 0, s>>>(stats, flag, P, tol, it, counter, slot[0], slot[1]);
+                FCU_LAUNCH("k_check");
+                launches += 1;
+                ++it;
+                ++corrections;
+                FCU_CHECK(cudaMemcpyAsync(host_flag, flag, 12, cudaMemcpyDeviceToHost, s));
+                FCU_CHECK(cudaStreamSynchronize(s));
+                if (host_flag[0] || it >= max_it) {
+                    std::swap(X, Y);  // the newest iterate is the FP32 sweep's
+                    break;
+                }
+                k_init_i8<<<blocks_for(cells, 256), 256, 0, s>>>(X, Y, rbuf, qb[0], slot[0], cells,
+                                                                 P);
+                FCU_LAUNCH("k_init_i8");
+                ++launches;
+                uint32_t j = 0;
+                bool steps_done = false;
+                while (!steps_done && it < max_it) {
+                    const uint32_t batch = std::min(timed ? 1u : check_every, max_it - it);
+                    for (uint32_t k = 0; k < batch; ++k, ++j) {
+                        const float* sin = slot[j & 1u];
+                        const float* sout = slot[(j + 1) & 1u];
+                        timed_sweep(true, [&] {
+                            launch_step_i8(P, g, pp, qb[j & 1u], qb[(j + 1) & 1u], X, rbuf, sin,
+                                           sout, stats, counter, flag + 3, s);
+                        });
+                        // slot j & 1 (sigma of the panel just consumed) takes
+                        // max|R_new| / 127 for the step after next
+                        k_check<<<1, kMaxP, 0, s>>>(stats, flag + 3, P, step_tol, it + k,
+                                                    counter, slot[j & 1u], nullptr);
+                        FCU_LAUNCH("k_check");
+                        ++launches;
+                    }
+                    it += batch;
+                    uint32_t sub_flag[3];
+                    FCU_CHECK(cudaMemcpyAsync(sub_flag, flag + 3, 12, cudaMemcpyDeviceToHost, s));
+                    FCU_CHECK(cudaStreamSynchronize(s));
+                    if (sub_flag[0]) {
+                        steps_done = true;
+                        sweeps -= it - sub_flag[1];  // launched after the target: no work
+                        it = sub_flag[1];
+                        FCU_CHECK(cudaMemsetAsync(flag + 3, 0, 12, s));
+                    }
+                }
+            }
+            cur = X == reinterpret_cast<float*>(x0) ? 0 : 1;
+            host_flag[1] = it;
         } else {
             // FP32 sweep, then BF16 defect sweeps until the defect has shrunk
             // by `cycle_drop`, then a fresh FP32 sweep (residual correction).

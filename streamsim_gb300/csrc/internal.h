@@ -191,6 +191,7 @@ struct BatchState {
     DeviceBuffer colstats;      // per-column max|dB|, max|B| bits
     DeviceBuffer q;             // source term per panel
     DeviceBuffer corr;          // residual / correction panel
+    DeviceBuffer i8;            // int8 step panels (two)
 };
 int batched_solve(const DeviceGraph& g, const BatchProblem& p, const facetcu_batch_config& cfg,
                   const float* d_initial, float* d_out, BatchState& st, Workspace& ws,

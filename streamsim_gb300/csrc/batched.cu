@@ -146,31 +146,8 @@ __device__ __forceinline__ Acc gather_narrow(const GraphView& g, uint32_t s, con
 // G = 32 / L edges per load instruction (e.g. P = 64 BF16: 8 lanes per
 // 128-byte row, 4 edges at once); the G partial sums are folded with
 // shuffles at the end of the row and the first L lanes own the result.
-template <bool kBF16> struct Vec16;
-template <> struct Vec16<false> {  // 4 x FP32
-    static constexpr int kCols = 4;
-    static __device__ __forceinline__ void load(const void* X, size_t idx16, float* v)
-    {
-        const float4 q = __ldg(reinterpret_cast<const float4*>(X) + idx16);
-        v[0] = q.x;
-        v[1] = q.y;
-        v[2] = q.z;
-        v[3] = q.w;
-    }
-};
-template <> struct Vec16<true> {  // 8 x BF16
-    static constexpr int kCols = 8;
-    static __device__ __forceinline__ void load(const void* X, size_t idx16, float* v)
-    {
-        const uint4 q = __ldg(reinterpret_cast<const uint4*>(X) + idx16);
-        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            v[2 * i] = __uint_as_float(w[i] << 16);
-            v[2 * i + 1] = __uint_as_float(w[i] & 0xFFFF0000u);
-        }
-    }
-};
+// Columns per 16-byte vector: 4 FP32 or 8 BF16.
+template <bool kBF16> constexpr int kVecCols = kBF16 ? 8 : 4;
 
 // acc[k] += sum over edges e of side s of count_e * X[n_e][col0 + k], where
 // col0 = (lane % L) * CPL; valid in every lane after the fold (lanes of the
@@ -230,7 +207,7 @@ __device__ __forceinline__ void gather_split(const uint32_t* __restrict__ rows,
                                              const facetcu_csr_edge* __restrict__ edges,
                                              uint32_t s, const void* X, int lane, float* acc)
 {
-    constexpr int CPL = Vec16<kBF16>::kCols;
+    constexpr int CPL = kVecCols<kBF16>;
     constexpr int L = P / CPL;  // lanes per row = 16-byte vectors per row
     constexpr int G = 32 / L;   // edges per load instruction
     constexpr int U = kGatherU;
@@ -408,88 +385,6 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_sweep_wide(GraphVie
                 }
                 store4(Bout + i0, b0);
                 store4(Bout + i1, b1);
-            }
-        }
-    }
-    publish_cols<CPL>(md, mb, col0, owner, P, stats);
-}
-
-// Defect sweep over a wide panel: d_out = K d_in (BF16 in and out, FP32
-// accumulation), X += d_out.  Stats: max|d_out|, max|X|.
-template <int P>
-__global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_defect_wide(GraphView g, PanelParams pp,
-                                                             const __nv_bfloat16* __restrict__ Din,
-                                                             __nv_bfloat16* __restrict__ Dout,
-                                                             float* __restrict__ X, uint32_t* stats,
-                                                             uint32_t* counter,
-                                                             const uint32_t* done)
-{
-    if (*done) return;
-    constexpr int CPL = 8;
-    constexpr int L = P / CPL;
-    const int lane = threadIdx.x & 31;
-    const bool owner = lane < L;
-    const int col0 = (lane % L) * CPL;
-    float md[CPL], mb[CPL];
-#pragma unroll
-    for (int k = 0; k < CPL; ++k) {
-        md[k] = 0.0f;
-        mb[k] = 0.0f;
-    }
-    const uint32_t chunks = (g.facets + kChunk - 1) / kChunk;
-    for (uint32_t ch = next_chunk(counter, lane); ch < chunks; ch = next_chunk(counter, lane)) {
-        const uint32_t fe = min(g.facets, (ch + 1) * kChunk);
-        for (uint32_t f = ch * kChunk; f < fe; ++f) {
-            float h[2][CPL];
-#pragma unroll
-            for (int side = 0; side < 2; ++side) {
-                const uint32_t s = 2u * f + side;
-                float acc[CPL];
-#pragma unroll
-                for (int k = 0; k < CPL; ++k) acc[k] = 0.0f;
-                gather_split<P, true>(g.rows, g.packed, g.edges, s, Din, lane, acc);
-                const uint32_t d = __ldg(g.denom + s);
-                const float inv = d ? 1.0f / float(d) : 0.0f;
-#pragma unroll
-                for (int k = 0; k < CPL; ++k) h[side][k] = acc[k] * inv;
-            }
-            if (owner) {
-                const size_t i0 = size_t(2u * f) * P + col0, i1 = i0 + P;
-                float r0[CPL], r1[CPL], t0[CPL], t1[CPL], x0[CPL], x1[CPL];
-#pragma unroll
-                for (int q = 0; q < CPL; q += 4) {
-                    load4(pp.rho + i0 + q, r0 + q);
-                    load4(pp.rho + i1 + q, r1 + q);
-                    load4(pp.tau + i0 + q, t0 + q);
-                    load4(pp.tau + i1 + q, t1 + q);
-                    load4(X + i0 + q, x0 + q);
-                    load4(X + i1 + q, x1 + q);
-                }
-                uint32_t w0[CPL / 2], w1[CPL / 2];
-#pragma unroll
-                for (int k = 0; k < CPL; k += 2) {
-                    float d0[2], d1[2];
-#pragma unroll
-                    for (int m = 0; m < 2; ++m) {
-                        d0[m] = r0[k + m] * h[0][k + m] + t0[k + m] * h[1][k + m];
-                        d1[m] = r1[k + m] * h[1][k + m] + t1[k + m] * h[0][k + m];
-                        x0[k + m] += d0[m];
-                        x1[k + m] += d1[m];
-                        md[k + m] = fmaxf(md[k + m], fmaxf(fabsf(d0[m]), fabsf(d1[m])));
-                        mb[k + m] = fmaxf(mb[k + m], fmaxf(fabsf(x0[k + m]), fabsf(x1[k + m])));
-                    }
-                    w0[k / 2] = uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(d0[0]))) |
-                                (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(d0[1]))) << 16);
-                    w1[k / 2] = uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(d1[0]))) |
-                                (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(d1[1]))) << 16);
-                }
-#pragma unroll
-                for (int q = 0; q < CPL; q += 4) {
-                    store4(X + i0 + q, x0 + q);
-                    store4(X + i1 + q, x1 + q);
-                }
-                *reinterpret_cast<uint4*>(Dout + i0) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
-                *reinterpret_cast<uint4*>(Dout + i1) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
             }
         }
     }
@@ -1055,31 +950,13 @@ void launch_sweep(int P, const GraphView& g, const PanelParams& pp, const T* in,
     FCU_LAUNCH("k_sweep");
 }
 
+// BF16 defect sweep; only panels narrower than 32 columns take this path
+// (wider MIXED panels run k_step_i8).
 void launch_defect(int P, const GraphView& g, const PanelParams& pp, const __nv_bfloat16* in,
                    __nv_bfloat16* out, float* X, uint32_t* stats, uint32_t* counter,
                    const uint32_t* done, cudaStream_t s)
 {
-    if (P >= 32) {
-        switch (P) {
-        case 32: {
-            static const int grid = grid_for(k_defect_wide<32>);
-            k_defect_wide<32><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, counter, done);
-            break;
-        }
-        case 64: {
-            static const int grid = grid_for(k_defect_wide<64>);
-            k_defect_wide<64><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, counter, done);
-            break;
-        }
-        default: {
-            static const int grid = grid_for(k_defect_wide<128>);
-            k_defect_wide<128><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, counter, done);
-            break;
-        }
-        }
-        FCU_LAUNCH("k_defect_wide");
-        return;
-    }
+    (void)counter;
     static const int grid = grid_for(k_sweep_defect<32>);
     switch (P) {
     case 1: k_sweep_defect<1><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, X, stats, done); break;

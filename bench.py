@@ -56,6 +56,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--quick", action="store_true", help="config-1 scene, for smoke timing")
+    p.add_argument("--config", default="c2", choices=["c2", "c3"],
+                   help="c2: the headline workload; c3: 150-tree forest, 256 suns x 64 bands "
+                        "(16,384 right-hand sides, outputs kept on the device)")
     p.add_argument("--warm-start", default="none", choices=["auto", "mlp", "none"],
                    help="mlp: the shipped MLP weights; auto: those when present and bands == 64")
     return p.parse_args()
@@ -417,6 +420,124 @@ def run_gpu(args, rank, world, local):
     m.close()
 
 
+def run_c3(args, rank, world, local):
+    """Batched right-hand sides at scale: the 150-tree forest (479,600
+    facets, 959,200 sides) against 256 suns (zenith 0-75 deg x azimuth
+    0-360 deg, 16 x 16 grid) x 64 bands = 16,384 RHS.  The 62.9 GB of output
+    stays on the device; MIXED and batched FP32 are timed on the full set,
+    the error against FP64 on suns 0 and 255 (128 columns)."""
+    import itertools
+
+    import torch
+
+    from streamsim_gb300 import facetcu as fc
+    from streamsim_gb300 import scenes
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    sc = scenes.config3(seed=0)
+    S = sc.surface_count
+    m = fc.FacetrtCuda()
+    m.initialize(args.raster, args.raster, 1024)
+    m.setGeometry(sc.vertices)
+    uv, dirs = scenes.hemisphere_samples(args.rays, 32, seed=7)
+    t0 = time.perf_counter()
+    diag, dropped = m.buildHemisphereGraph(uv, dirs, args.rays, args.top_k, 32)
+    build_s = time.perf_counter() - t0
+    suv, _ = scenes.hemisphere_samples(256, 32, seed=8)
+    suns = list(itertools.product(np.linspace(0.0, 75.0, 16), np.linspace(0.0, 360.0, 16,
+                                                                           endpoint=False)))
+    dgeo = np.empty((len(suns), S), np.float32)
+    t0 = time.perf_counter()
+    for i, (zen, az) in enumerate(suns):
+        sun = scenes.sun_direction(zen, az)
+        dgeo[i] = scenes.direct_geometry(sc, m.hemisphereSunlit(sun, suv, 256, 32), sun)
+    sun_s = time.perf_counter() - t0
+    B = args.bands
+    rho, tau = scenes.band_optics(sc, B)
+    sky = np.full(B, 100.0, np.float32)
+    beam = np.full(B, 800.0, np.float32)
+    R = B * len(suns)
+    t = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+         for k, v in (("rho", rho), ("tau", tau), ("sky", sky), ("beam", beam), ("dgeo", dgeo))}
+    out = torch.empty((R, S), dtype=torch.float32, device=dev)
+    stream = torch.cuda.ExternalStream(m.stream(), device=dev)
+    torch.cuda.synchronize()
+
+    def solve(prec, flags=0):
+        cfg = fc.BatchConfig(B, len(suns), prec, fc.WARM_NONE, 2000, args.tolerance, 0, flags)
+        return m.solveBatchedDevice(cfg, t["rho"].data_ptr(), t["tau"].data_ptr(), None,
+                                    t["sky"].data_ptr(), t["beam"].data_ptr(),
+                                    t["dgeo"].data_ptr(), None, out.data_ptr())
+
+    # FP64 truth of suns 0 and 255 (the error check; not timed)
+    pick = [0, len(suns) - 1]
+    truth, _ = m.solveBatched(rho, tau, sky, beam, dgeo[pick], precision=fc.PRECISION_FP64,
+                              tolerance=1e-12, maximum_iterations=4000)
+    rows = np.concatenate([np.arange(B) + k * B for k in pick])
+
+    def error():
+        got = out[torch.from_numpy(rows).to(dev)].cpu().numpy()
+        scale = np.maximum(np.abs(truth), 1e-6 * np.abs(truth).max())
+        return float(np.max(np.abs(got - truth) / scale))
+
+    def timed(prec, steps, warmup):
+        for _ in range(warmup):
+            res = solve(prec)
+        times = []
+        with ClockSampler(local) as clocks:
+            for _ in range(steps):
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                res = solve(prec)
+                e1.record(stream)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1) / 1e3)
+        return float(np.mean(times)), res, clocks.summary()
+
+    step_s, res, clocks = timed(fc.PRECISION_MIXED, args.steps, args.warmup)
+    err = error()
+    fp32_s, res32, _ = timed(fc.PRECISION_FP32, 1, 0)
+    err32 = error()
+    rt = solve(fc.PRECISION_MIXED, fc.BATCH_TIME_SWEEPS)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = rt["sweep_bytes"] / max(rt["sweep_seconds"], 1e-12) / 1e9
+    units = sc.facet_count * R
+    line = {
+        "metric": METRIC, "value": units / step_s, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "i8+f32",
+        "data": "synthetic (seeded scene generator, no dataset)",
+        "config": {"workload": f"config3 forest: {sc.facet_count:,} facets, {B} bands x "
+                               f"{len(suns)} suns = {R:,} RHS, view factors: hemisphere",
+                   "facets": sc.facet_count, "sides": S, "bands": B, "suns": len(suns),
+                   "precision": "mixed", "tolerance": args.tolerance,
+                   "view_factors": {"rays_per_side": args.rays, "top_k": args.top_k,
+                                    "directed_edges": int(diag["directed_edge_count"]),
+                                    "build_s": build_s, "sun_rasters_s": sun_s},
+                   "l2": "inputs and outputs far larger than L2 (no flush needed)"},
+        "max_rel_err_vs_fp64": err, "error_columns": "suns 0 and 255 x 64 bands",
+        "iterations": res["iterations"], "residual_corrections": res["residual_corrections"],
+        "batched_fp32": {"value": units / fp32_s, "ms_per_step": fp32_s * 1e3,
+                         "iterations": res32["iterations"], "max_rel_err_vs_fp64": err32},
+        "speedup_vs_batched_fp32": fp32_s / step_s,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "kernel": "k_step_i8<128>",
+                     "launches_timed": rt["timed_sweeps"],
+                     "avg_launch_ms": rt["sweep_seconds"] / max(rt["timed_sweeps"], 1) * 1e3},
+        "e2e": None, "gpu_launches": int(res["kernel_launches"]), "clocks": clocks,
+    }
+    print(json.dumps(line))
+    m.close()
+
+
 def run_reference(args, rank, world, local):
     if rank != 0:
         return
@@ -445,6 +566,8 @@ def main():
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, local)
+    elif args.config == "c3":
+        run_c3(args, rank, world, local)
     else:
         run_gpu(args, rank, world, local)
     if world > 1:

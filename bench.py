@@ -464,8 +464,9 @@ def run_c3(args, rank, world, local):
     stream = torch.cuda.ExternalStream(m.stream(), device=dev)
     torch.cuda.synchronize()
 
-    def solve(prec, flags=0):
-        cfg = fc.BatchConfig(B, len(suns), prec, fc.WARM_NONE, 2000, args.tolerance, 0, flags)
+    def solve(prec, flags=0, tol=None, maxit=2000):
+        cfg = fc.BatchConfig(B, len(suns), prec, fc.WARM_NONE, maxit,
+                             args.tolerance if tol is None else tol, 0, flags)
         return m.solveBatchedDevice(cfg, t["rho"].data_ptr(), t["tau"].data_ptr(), None,
                                     t["sky"].data_ptr(), t["beam"].data_ptr(),
                                     t["dgeo"].data_ptr(), None, out.data_ptr())
@@ -481,9 +482,9 @@ def run_c3(args, rank, world, local):
         scale = np.maximum(np.abs(truth), 1e-6 * np.abs(truth).max())
         return float(np.max(np.abs(got - truth) / scale))
 
-    def timed(prec, steps, warmup):
+    def timed(prec, steps, warmup, **kw):
         for _ in range(warmup):
-            res = solve(prec)
+            res = solve(prec, **kw)
         times = []
         with ClockSampler(local) as clocks:
             for _ in range(steps):
@@ -491,7 +492,7 @@ def run_c3(args, rank, world, local):
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                res = solve(prec)
+                res = solve(prec, **kw)
                 e1.record(stream)
                 e1.synchronize()
                 times.append(e0.elapsed_time(e1) / 1e3)
@@ -501,6 +502,10 @@ def run_c3(args, rank, world, local):
     err = error()
     fp32_s, res32, _ = timed(fc.PRECISION_FP32, 1, 0)
     err32 = error()
+    # FP32 run to the MIXED steps' own target (a quarter of the tolerance),
+    # capped at 60 sweeps: the FP32 solve that meets the 1e-4 bar
+    fp32t_s, res32t, _ = timed(fc.PRECISION_FP32, 1, 0, tol=args.tolerance * 0.25, maxit=60)
+    err32t = error()
     rt = solve(fc.PRECISION_MIXED, fc.BATCH_TIME_SWEEPS)
     peaks = {}
     try:
@@ -527,7 +532,12 @@ def run_c3(args, rank, world, local):
         "iterations": res["iterations"], "residual_corrections": res["residual_corrections"],
         "batched_fp32": {"value": units / fp32_s, "ms_per_step": fp32_s * 1e3,
                          "iterations": res32["iterations"], "max_rel_err_vs_fp64": err32},
+        "batched_fp32_quarter_tol": {"value": units / fp32t_s, "ms_per_step": fp32t_s * 1e3,
+                                     "iterations": res32t["iterations"],
+                                     "converged": bool(res32t["converged"]),
+                                     "max_rel_err_vs_fp64": err32t},
         "speedup_vs_batched_fp32": fp32_s / step_s,
+        "speedup_vs_batched_fp32_meeting_the_bar": fp32t_s / step_s,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "kernel": "k_step_i8<128>",
                      "launches_timed": rt["timed_sweeps"],

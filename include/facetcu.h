@@ -218,7 +218,8 @@ typedef struct {
     uint32_t warm_start;        /* FACETCU_WARM_* */
     uint32_t maximum_iterations;
     float tolerance;            /* relative change per column */
-    uint32_t panel_width;       /* RHS columns per resident panel (<= 32); 0 = 32 */
+    uint32_t panel_width;       /* RHS columns per resident panel (power of two, <= 128;
+                                   <= 32 in FP64); 0 = the widest that fits */
     uint32_t flags;             /* FACETCU_BATCH_TIME_SWEEPS: time every sweep kernel */
 } facetcu_batch_config;
 #define FACETCU_BATCH_TIME_SWEEPS 1u
@@ -233,7 +234,8 @@ typedef struct {
     double sweep_seconds;       /* summed time of the dominant sweep kernel (TIME_SWEEPS) */
     double sweep_bytes;         /* algorithmic HBM bytes of those sweeps */
     uint32_t timed_sweeps;      /* number of sweeps in sweep_seconds */
-    uint32_t reserved;
+    uint32_t graph_launches;    /* replays of the captured step batch (CUDA graph); their
+                                   kernels are counted in kernel_launches */
 } facetcu_batch_result;
 int facetcu_solve_batched(facetcu_context *ctx, const facetcu_batch_config *config,
                           const float *reflectance, const float *transmittance,

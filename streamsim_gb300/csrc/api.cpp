@@ -349,6 +349,7 @@ int facetcu_destroy(facetcu_context* ctx)
                             &ctx->batch.corr, &ctx->batch.i8, &ctx->batch_inputs, &ctx->spec_io,
                             &ctx->spec.dev})
         b->release();
+    release_graphs(ctx->batch);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     ctx->stream = nullptr;
     ctx->facets = 0;

@@ -661,9 +661,11 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_step_i8(
 // R = Y - X and Q = round(R / sigma) for the first int8 step (X unchanged).
 __global__ void k_init_i8(const float* __restrict__ X, const float* __restrict__ Y,
                           float* __restrict__ R, int8_t* __restrict__ Q,
-                          const float* __restrict__ sig, size_t n, int P)
+                          const float* __restrict__ sig, size_t n, int P, uint32_t* it_dev,
+                          uint32_t it)
 {
     const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i == 0) *it_dev = it;  // sweep index of the first step's check
     if (i >= n) return;
     const float r = Y[i] - X[i];
     const float sg = sig[i % size_t(P)];
@@ -765,10 +767,12 @@ __global__ void k_defect_init(const float* Bold, const float* Bnew, __nv_bfloat1
 // scale_a / scale_b, also stores max|dB| / 127 per column there (the int8
 // step scales).
 __global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint32_t it,
-                        uint32_t* counter, float* scale_a = nullptr, float* scale_b = nullptr)
+                        uint32_t* counter, float* scale_a = nullptr, float* scale_b = nullptr,
+                        uint32_t* it_dev = nullptr)
 {
     __shared__ int all_ok;
     __shared__ float worst;
+    if (it_dev) it = *it_dev;  // the sweep index kept on the device (graph replays)
     if (threadIdx.x == 0) {
         all_ok = 1;
         worst = 0.0f;
@@ -792,7 +796,10 @@ __global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint3
         if (all_ok) flag[0] = 1;
     }
     for (int i = threadIdx.x; i < 2 * kMaxP; i += blockDim.x) stats[i] = 0;
-    if (threadIdx.x == 0) *counter = 0u;
+    if (threadIdx.x == 0) {
+        *counter = 0u;
+        if (it_dev) *it_dev = it + 1;
+    }
 }
 
 __device__ __forceinline__ uint32_t old_side(const uint32_t* order, uint32_t s)
@@ -979,31 +986,99 @@ void launch_defect(int P, const GraphView& g, const PanelParams& pp, const __nv_
     FCU_LAUNCH("k_sweep_defect");
 }
 
+template <int P>
+int step_grid()
+{
+    static const int grid = grid_for(k_step_i8<P>);
+    return grid;
+}
+
 void launch_step_i8(int P, const GraphView& g, const PanelParams& pp, const int8_t* qin,
                     int8_t* qout, float* X, float* R, const float* sin, const float* sout,
                     uint32_t* stats, uint32_t* counter, const uint32_t* done, cudaStream_t s)
 {
     switch (P) {
-    case 32: {
-        static const int grid = grid_for(k_step_i8<32>);
-        k_step_i8<32><<<grid, kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin, sout, stats,
-                                                   counter, done);
+    case 32:
+        k_step_i8<32><<<step_grid<32>(), kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin, sout,
+                                                              stats, counter, done);
         break;
-    }
-    case 64: {
-        static const int grid = grid_for(k_step_i8<64>);
-        k_step_i8<64><<<grid, kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin, sout, stats,
-                                                   counter, done);
+    case 64:
+        k_step_i8<64><<<step_grid<64>(), kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin, sout,
+                                                              stats, counter, done);
         break;
-    }
-    default: {
-        static const int grid = grid_for(k_step_i8<128>);
-        k_step_i8<128><<<grid, kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin, sout, stats,
-                                                    counter, done);
+    default:
+        k_step_i8<128><<<step_grid<128>(), kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin,
+                                                                sout, stats, counter, done);
         break;
-    }
     }
     FCU_LAUNCH("k_step_i8");
+}
+
+// One batch of kStepBatch int8 steps, each followed by its check, as a CUDA
+// graph: the batches of a solve repeat the same launches (the q panels and
+// scales alternate with the step's parity and every batch starts on an even
+// step; the check takes its sweep index from the device counter k_init_i8
+// seeds), so the batch is captured once per panel configuration and replayed.
+constexpr uint32_t kStepBatch = 8;
+
+struct StepGraphKey {
+    int P;
+    GraphView g;
+    PanelParams pp;
+    const int8_t* q0;
+    const int8_t* q1;
+    float* X;
+    float* R;
+    float* slot0;
+    float* slot1;
+    uint32_t* stats;
+    uint32_t* flag;
+    float tol;
+    cudaStream_t stream;
+};
+
+void record_steps(const StepGraphKey& k, cudaStream_t s)
+{
+    int8_t* qb[2] = {const_cast<int8_t*>(k.q0), const_cast<int8_t*>(k.q1)};
+    float* slot[2] = {k.slot0, k.slot1};
+    uint32_t* counter = k.flag + 8;
+    for (uint32_t j = 0; j < kStepBatch; ++j) {
+        launch_step_i8(k.P, k.g, k.pp, qb[j & 1u], qb[(j + 1) & 1u], k.X, k.R, slot[j & 1u],
+                       slot[(j + 1) & 1u], k.stats, counter, k.flag + 3, s);
+        k_check<<<1, kMaxP, 0, s>>>(k.stats, k.flag + 3, k.P, k.tol, 0u, counter, slot[j & 1u],
+                                    nullptr, k.flag + 12);
+        FCU_LAUNCH("k_check");
+    }
+}
+
+cudaGraphExec_t step_graph(BatchState& st, const StepGraphKey& key)
+{
+    if (st.step_graph && std::memcmp(st.step_graph_key, &key, sizeof(key)) == 0)
+        return st.step_graph;
+    release_graphs(st);
+    switch (key.P) {  // size the grids before capture starts
+    case 32: step_grid<32>(); break;
+    case 64: step_grid<64>(); break;
+    default: step_grid<128>(); break;
+    }
+    cudaGraph_t graph = nullptr;
+    FCU_CHECK(cudaStreamBeginCapture(key.stream, cudaStreamCaptureModeThreadLocal));
+    try {
+        record_steps(key, key.stream);
+    } catch (...) {
+        cudaStreamEndCapture(key.stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+    }
+    FCU_CHECK(cudaStreamEndCapture(key.stream, &graph));
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t rc = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    FCU_CHECK(rc);
+    st.step_graph = exec;
+    static_assert(sizeof(StepGraphKey) <= sizeof(st.step_graph_key), "graph key size");
+    std::memcpy(st.step_graph_key, &key, sizeof(key));
+    return exec;
 }
 
 // Panel widths: power of two, at most `cap` (128 for FP32/BF16 with a
@@ -1048,6 +1123,13 @@ void ensure_permuted(DeviceGraph& gr, const BatchProblem& p, Workspace& ws, cuda
 }  // namespace
 
 // Host driver.  Returns FACETCU_OK or FACETCU_NOT_CONVERGED.
+void release_graphs(BatchState& st)
+{
+    if (st.step_graph) cudaGraphExecDestroy(st.step_graph);
+    st.step_graph = nullptr;
+    std::memset(st.step_graph_key, 0, sizeof(st.step_graph_key));
+}
+
 int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu_batch_config& cfg,
                   const float* d_initial, float* d_out, BatchState& st, Workspace& ws,
                   cudaStream_t s, facetcu_batch_result* result)
@@ -1092,6 +1174,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
     }
 
     uint32_t worst_iterations = 0, corrections = 0, launches = 0, sweeps = 0, timed_sweeps = 0;
+    uint32_t graph_launches = 0;
     double sweep_seconds = 0.0, sweep_bytes = 0.0;
     const bool timed = (cfg.flags & FACETCU_BATCH_TIME_SWEEPS) != 0u;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -1224,13 +1307,36 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                     break;
                 }
                 k_init_i8<<<blocks_for(cells, 256), 256, 0, s>>>(X, Y, rbuf, qb[0], slot[0], cells,
-                                                                 P);
+                                                                 P, flag + 12, it);
                 FCU_LAUNCH("k_init_i8");
                 ++launches;
                 uint32_t j = 0;
                 bool steps_done = false;
                 while (!steps_done && it < max_it) {
                     const uint32_t batch = std::min(timed ? 1u : check_every, max_it - it);
+                    if (!timed && batch == kStepBatch) {
+                        // j is even here: the captured parity pattern applies
+                        StepGraphKey key;
+                        std::memset(&key, 0, sizeof(key));  // padding takes part in the compare
+                        key.P = P;
+                        key.g = g;
+                        key.pp = pp;
+                        key.q0 = qb[0];
+                        key.q1 = qb[1];
+                        key.X = X;
+                        key.R = rbuf;
+                        key.slot0 = slot[0];
+                        key.slot1 = slot[1];
+                        key.stats = stats;
+                        key.flag = flag;
+                        key.tol = step_tol;
+                        key.stream = s;
+                        FCU_CHECK(cudaGraphLaunch(step_graph(st, key), s));
+                        launches += 2 * kStepBatch;
+                        sweeps += kStepBatch;
+                        ++graph_launches;
+                        j += kStepBatch;
+                    } else
                     for (uint32_t k = 0; k < batch; ++k, ++j) {
                         const float* sin = slot[j & 1u];
                         const float* sout = slot[(j + 1) & 1u];
@@ -1353,6 +1459,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
         result->residual_corrections = corrections;
         result->converged = all_converged ? 1u : 0u;
         result->max_relative_change = worst_change;
+        result->graph_launches = graph_launches;
     }
     return all_converged ? FACETCU_OK : FACETCU_NOT_CONVERGED;
 }

@@ -192,7 +192,10 @@ struct BatchState {
     DeviceBuffer q;             // source term per panel
     DeviceBuffer corr;          // residual / correction panel
     DeviceBuffer i8;            // int8 step panels (two)
+    cudaGraphExec_t step_graph = nullptr;  // captured batch of int8 steps
+    alignas(8) unsigned char step_graph_key[256] = {};
 };
+void release_graphs(BatchState& st);
 int batched_solve(const DeviceGraph& g, const BatchProblem& p, const facetcu_batch_config& cfg,
                   const float* d_initial, float* d_out, BatchState& st, Workspace& ws,
                   cudaStream_t s, facetcu_batch_result* result);

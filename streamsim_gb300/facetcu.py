@@ -103,7 +103,7 @@ class BatchResult(C.Structure):
                 ("seconds", C.c_double), ("kernel_launches", C.c_uint32),
                 ("sweeps", C.c_uint32), ("sweep_seconds", C.c_double),
                 ("sweep_bytes", C.c_double), ("timed_sweeps", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("graph_launches", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

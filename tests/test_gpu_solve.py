@@ -158,3 +158,22 @@ def test_batched_warm_start_given(c1):
     out2, res2 = c1["model"].solveBatched(rho, tau, sky, beam, dgeo, tolerance=1e-6, initial=out)
     assert res2["iterations"] < res["iterations"] / 3
     assert rel_err(out2, out) < 1e-5
+
+
+def test_mixed_graph_replay_matches_per_sweep_launches(c1):
+    """The int8 step batches replayed from a captured CUDA graph give the
+    same bits as launching every step and check one by one (the sweep-timing
+    mode), on a wide panel and on two panels of different widths."""
+    sc = c1["scene"]
+    for bands, suns in ((64, 1), (32, 3)):
+        rho, tau, _, sky, beam = _bands(sc, c1["lit"], c1["sun"], bands)
+        dgeo = np.stack([scenes.direct_geometry(sc, c1["lit"], scenes.sun_direction(z, 135))
+                         for z in np.linspace(10, 60, suns)])
+        kw = dict(precision=facetcu.PRECISION_MIXED, tolerance=1e-7, maximum_iterations=400,
+                  raise_on_nonconvergence=False)
+        a, ra = c1["model"].solveBatched(rho, tau, sky, beam, dgeo, **kw)
+        b, rb = c1["model"].solveBatched(rho, tau, sky, beam, dgeo,
+                                         flags=facetcu.BATCH_TIME_SWEEPS, **kw)
+        assert ra["graph_launches"] > 0 and rb["graph_launches"] == 0
+        assert ra["iterations"] == rb["iterations"]
+        assert np.array_equal(a, b)

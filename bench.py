@@ -56,9 +56,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--quick", action="store_true", help="config-1 scene, for smoke timing")
-    p.add_argument("--config", default="c2", choices=["c2", "c3"],
+    p.add_argument("--config", default="c2", choices=["c2", "c3", "c5"],
                    help="c2: the headline workload; c3: 150-tree forest, 256 suns x 64 bands "
-                        "(16,384 right-hand sides, outputs kept on the device)")
+                        "(16,384 right-hand sides, outputs kept on the device); c5: 32 scenes "
+                        "of uneven size, 64 bands + a thermal band, as one batch")
     p.add_argument("--warm-start", default="none", choices=["auto", "mlp", "none"],
                    help="mlp: the shipped MLP weights; auto: those when present and bands == 64")
     return p.parse_args()
@@ -548,6 +549,144 @@ def run_c3(args, rank, world, local):
     m.close()
 
 
+def run_c5(args, rank, world, local):
+    """Uneven multi-scene batch with a thermal source: 32 scenes (row crops,
+    forests, urban blocks) with facet counts log-uniform in [20k, 400k],
+    each with its own sun; 64 optical bands plus one thermal band (11 um,
+    emissivity 0.97 leaves / 0.95 soil and walls, facet temperatures
+    U(280, 320) K, sky at 250 K).  Each scene's hemisphere graph is built
+    alone (255 rays per side, so every count fits the packed format of the
+    9.4 M-side union); facetcu_scene_batch joins them into one
+    block-diagonal graph, solved as one batch (one launch per step over all
+    scenes).  Compared with solving the 32 scenes one after another."""
+    import torch
+
+    from streamsim_gb300 import facetcu as fc
+    from streamsim_gb300 import scenes
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    t0 = time.perf_counter()
+    parts = scenes.c5_scenes(32, seed=0)
+    gen_s = time.perf_counter() - t0
+    rays = 255
+    uv, dirs = scenes.hemisphere_samples(rays, 32, seed=7)
+    suv, _ = scenes.hemisphere_samples(256, 32, seed=8)
+    rng = np.random.default_rng(5)
+    models, rho, tau, emis, dgeo = [], [], [], [], []
+    build_s = 0.0
+    for sc in parts:
+        m = fc.FacetrtCuda()
+        m.initialize(256, 256, 64)
+        m.setGeometry(sc.vertices)
+        t1 = time.perf_counter()
+        m.buildHemisphereGraph(uv, dirs, rays, args.top_k, 32)
+        build_s += time.perf_counter() - t1
+        sun = scenes.sun_direction(rng.uniform(0.0, 60.0), rng.uniform(0.0, 360.0))
+        dgeo.append(scenes.direct_geometry(sc, m.hemisphereSunlit(sun, suv, 256, 32), sun))
+        r, t = scenes.band_optics(sc, 64)
+        tr, tt, te = scenes.thermal_optics(sc, rng.uniform(280.0, 320.0, sc.facet_count))
+        rho.append(np.vstack([r, tr]))
+        tau.append(np.vstack([t, tt]))
+        emis.append(np.vstack([np.zeros_like(r), te]))
+        models.append(m)
+    B = 65
+    sky = np.append(np.full(64, 100.0), fc.planck_radiance(11000.0, 250.0)).astype(np.float32)
+    beam = np.append(np.full(64, 800.0), 0.0).astype(np.float32)
+    facets = sum(sc.facet_count for sc in parts)
+    units = facets * B
+    cfg = fc.BatchConfig(B, 1, fc.PRECISION_MIXED, fc.WARM_NONE, 2000, args.tolerance, 0, 0)
+
+    def upload(r, t, e, d):
+        return {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+                for k, v in (("rho", r), ("tau", t), ("emis", e), ("sky", sky), ("beam", beam),
+                             ("dgeo", d))}
+
+    def solve(m, x, out, c=cfg):
+        return m.solveBatchedDevice(c, x["rho"].data_ptr(), x["tau"].data_ptr(),
+                                    x["emis"].data_ptr(), x["sky"].data_ptr(),
+                                    x["beam"].data_ptr(), x["dgeo"].data_ptr(), None,
+                                    out.data_ptr())
+
+    # the 32 scenes one after another, inputs resident
+    alone = [upload(rho[i], tau[i], emis[i], dgeo[i][None, :]) for i in range(len(parts))]
+    outs = [torch.empty((B, parts[i].surface_count), dtype=torch.float32, device=dev)
+            for i in range(len(parts))]
+    torch.cuda.synchronize()
+    for i, m in enumerate(models):
+        solve(m, alone[i], outs[i])
+    seq = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        seq_res = [solve(m, alone[i], outs[i]) for i, m in enumerate(models)]
+        torch.cuda.synchronize()
+        seq.append(time.perf_counter() - t1)
+    seq_s = float(np.mean(seq))
+    del alone, outs
+
+    # one batch
+    batch = fc.FacetrtCuda()
+    batch.initialize(16, 16, 8)
+    offsets, diag = batch.sceneBatch(models)
+    for m in models:
+        m.close()
+    cat = lambda xs: np.ascontiguousarray(np.concatenate(xs, axis=-1))
+    x = upload(cat(rho), cat(tau), cat(emis), cat(dgeo)[None, :])
+    S = int(offsets[-1])
+    out = torch.empty((B, S), dtype=torch.float32, device=dev)
+    stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        res = solve(batch, x, out)
+    times, walls = [], []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            t1 = time.perf_counter()
+            e0.record(stream)
+            res = solve(batch, x, out)
+            e1.record(stream)
+            e1.synchronize()
+            walls.append(time.perf_counter() - t1)
+            times.append(e0.elapsed_time(e1) / 1e3)
+    step_s = float(np.mean(times))
+    wall_s = float(np.mean(walls))
+    got = out.cpu().numpy()
+    truth, tres = batch.solveBatched(cat(rho), cat(tau), sky, beam, cat(dgeo)[None, :],
+                                     emission=cat(emis), precision=fc.PRECISION_FP64,
+                                     tolerance=1e-12, maximum_iterations=4000)
+    scale = np.maximum(np.abs(truth), 1e-6 * np.abs(truth).max(axis=1, keepdims=True))
+    err = float(np.max(np.abs(got - truth) / scale))
+    line = {
+        "metric": METRIC, "value": units / step_s, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "i8+f32",
+        "data": "synthetic (seeded scene generator, no dataset)",
+        "config": {"workload": f"32 scenes (crops, forests, urban), {facets:,} facets in total, "
+                               "64 bands + 1 thermal band, one sun each, as one batch",
+                   "facets": facets, "sides": S,
+                   "scene_facets": [sc.facet_count for sc in parts], "bands": B, "suns": 1,
+                   "precision": "mixed", "tolerance": args.tolerance,
+                   "view_factors": {"rays_per_side": rays, "top_k": args.top_k,
+                                    "directed_edges": int(diag["directed_edge_count"]),
+                                    "build_s_all_scenes": build_s},
+                   "generation_s": gen_s,
+                   "l2": "inputs far larger than L2 (no flush needed)"},
+        "max_rel_err_vs_fp64": err, "iterations": res["iterations"],
+        "graph_launches": res["graph_launches"], "gpu_launches": int(res["kernel_launches"]),
+        "wall_ms_per_step": wall_s * 1e3,
+        "scenes_one_by_one": {"value": units / seq_s, "ms_per_step": seq_s * 1e3,
+                              "gpu_launches": int(sum(r["kernel_launches"] for r in seq_res))},
+        "speedup_vs_one_by_one": seq_s / wall_s,
+        "e2e": None, "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+    batch.close()
+
+
 def run_reference(args, rank, world, local):
     if rank != 0:
         return
@@ -578,6 +717,8 @@ def main():
         run_reference(args, rank, world, local)
     elif args.config == "c3":
         run_c3(args, rank, world, local)
+    elif args.config == "c5":
+        run_c5(args, rank, world, local)
     else:
         run_gpu(args, rank, world, local)
     if world > 1:

@@ -329,6 +329,21 @@ int facetcu_solve_noalloc(const uint32_t *row_offsets, const facetcu_csr_edge *e
                           float sky_radiosity, uint32_t iterations, float relaxation,
                           float *radiosity, float *max_delta, void *stream);
 
+/* ---- scene batches ------------------------------------------------------ */
+/* Makes ctx's geometry and graph the disjoint union of `scene_count` other
+ * contexts, each with a built graph (raster or hemisphere), so that one
+ * batched solve (one launch per sweep) covers scenes of uneven size:
+ * scene i's sides are [side_offsets[i], side_offsets[i+1]) of the union and
+ * its graph block is copied with its neighbour indices offset (no
+ * cross-scene edges).  Scene i's vertices are translated into their own cell
+ * of a grid (only the solver's Morton renumbering sees positions).  Per-side
+ * arrays for the union are the scenes' arrays concatenated in that order.
+ * side_offsets holds scene_count + 1 entries; diagnostics may be NULL.  No
+ * counterpart in the reference (it solves one scene per run). */
+int facetcu_scene_batch(facetcu_context *ctx, facetcu_context *const *scenes,
+                        uint32_t scene_count, uint32_t *side_offsets,
+                        facetcu_graph_diagnostics *diagnostics);
+
 /* ---- scene files, optics and the eFacetRT process flow ------------------ */
 /* Scene facts loadTreeWithSoil returns (Scene, facetrtcore.cpp:148-166). */
 typedef struct {

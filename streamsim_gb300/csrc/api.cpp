@@ -1368,4 +1368,92 @@ int facetcu_solve_bands(facetcu_context* ctx, const facetcu_spectral_parameters*
     });
 }
 
+// ---- scene batches -------------------------------------------------------
+int facetcu_scene_batch(facetcu_context* ctx, facetcu_context* const* scenes,
+                        uint32_t scene_count, uint32_t* side_offsets,
+                        facetcu_graph_diagnostics* diagnostics)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "sceneBatch()");
+        if (!scenes || scene_count == 0)
+            throw Error(FACETCU_INVALID_ARGUMENT, "at least one scene is required");
+        uint64_t facets = 0, nnz = 0;
+        float extent = 0.0f;
+        uint32_t max_count = 0;
+        for (uint32_t i = 0; i < scene_count; ++i) {
+            const facetcu_context* sc = scenes[i];
+            if (!sc || sc == ctx || !sc->graph_ready)
+                throw Error(FACETCU_LOGIC_ERROR,
+                            "every scene of a batch needs its own context with a built graph");
+            if (sc->device != ctx->device)
+                throw Error(FACETCU_INVALID_ARGUMENT, "the scenes of a batch must share a GPU");
+            facets += sc->facets;
+            nnz += sc->graph.nnz;
+            max_count = std::max(max_count, sc->graph.max_count);
+            for (int a = 0; a < 3; ++a) extent = std::max(extent, sc->bmax[a] - sc->bmin[a]);
+        }
+        if (2 * facets > 0xffffffffull || nnz > 0xffffffffull)
+            throw Error(FACETCU_OVERFLOW_ERROR, "the batch exceeds 2^32 sides or edges");
+        // Scene i sits in its own cell of an n x n x n grid (cell = 1.25 x the
+        // largest scene extent): positions matter here only for the solver's
+        // Morton renumbering, which then keeps every scene contiguous.
+        uint32_t n = 1;
+        while (uint64_t(n) * n * n < scene_count) ++n;
+        const float cell = 1.25f * std::max(extent, 1.0f);
+        std::vector<facetcu_vertex> all;
+        all.reserve(size_t(facets) * 3);
+        for (uint32_t i = 0; i < scene_count; ++i) {
+            const facetcu_context* sc = scenes[i];
+            const float off[3] = {float(i % n) * cell - sc->bmin[0],
+                                  float((i / n) % n) * cell - sc->bmin[1],
+                                  float(i / (n * n)) * cell - sc->bmin[2]};
+            for (facetcu_vertex v : sc->vertices_host) {
+                for (int a = 0; a < 3; ++a) v.position[a] += off[a];
+                all.push_back(v);
+            }
+        }
+        nested(ctx, facetcu_set_geometry(ctx, all.data(), all.size()));
+        DeviceGraph& g = ctx->graph;
+        cudaStream_t s = ctx->stream;
+        const uint32_t S = uint32_t(2 * facets);
+        g.surfaces = S;
+        g.nnz = nnz;
+        g.row_offsets.reserve((size_t(S) + 1) * 4);
+        g.edges.reserve(nnz * 8 + 8);
+        g.denominators.reserve(size_t(S) * 4);
+        g.sky.reserve(size_t(S) * 4);
+        uint32_t side = 0;
+        uint64_t edge = 0;
+        for (uint32_t i = 0; i < scene_count; ++i) {
+            const facetcu_context* sc = scenes[i];
+            FCU_CHECK(cudaStreamSynchronize(sc->stream));
+            if (side_offsets) side_offsets[i] = side;
+            graph_append(g, sc->graph, side, edge, s);
+            side += sc->graph.surfaces;
+            edge += sc->graph.nnz;
+        }
+        if (side_offsets) side_offsets[scene_count] = side;
+        const uint32_t last = uint32_t(nnz);
+        FCU_CHECK(cudaMemcpyAsync(g.row_offsets.as<uint32_t>() + S, &last, 4,
+                                  cudaMemcpyHostToDevice, s));
+        g.max_count = max_count;
+        g.packed_valid = false;
+        g.perm_valid = false;
+        float closure = 0.0f;
+        uint32_t sampled = 0;
+        graph_closure(g, &closure, &sampled, ctx->ws, s);
+        graph_pack(g, ctx->ws, s);
+        FCU_CHECK(cudaStreamSynchronize(s));
+        ctx->graph_ready = true;
+        if (diagnostics) {
+            *diagnostics = {};
+            diagnostics->facet_count = uint32_t(facets);
+            diagnostics->surface_count = S;
+            diagnostics->directed_edge_count = uint32_t(nnz);
+            diagnostics->max_closure_error = closure;
+        }
+        return FACETCU_OK;
+    });
+}
+
 }  // extern "C"

@@ -43,7 +43,6 @@ namespace {
 
 constexpr int kWarps = 8;  // warps per CTA
 constexpr int kMaxP = 128;
-constexpr uint32_t kNeighborMask = (1u << 22) - 1u;
 
 struct PanelParams {
     // per side and column, [S][P]
@@ -61,14 +60,15 @@ struct GraphView {
     const uint32_t* denom;
     const uint32_t* skyc;
     uint32_t facets;
+    uint32_t nb_bits;                  // neighbour field of a packed word (count above it)
 };
 
 __device__ __forceinline__ void edge_at(const GraphView& g, uint32_t e, uint32_t& nb, float& c)
 {
     if (g.packed) {
         const uint32_t p = __ldg(g.packed + e);
-        nb = p & kNeighborMask;
-        c = float(p >> 22);
+        nb = p & ((1u << g.nb_bits) - 1u);
+        c = float(p >> g.nb_bits);
     } else {
         const facetcu_csr_edge ed = g.edges[e];
         nb = ed.neighbor;
@@ -170,12 +170,12 @@ constexpr int kMinBlocks = FCU_MIN_BLOCKS;
 
 __device__ __forceinline__ void edge_word(const uint32_t* __restrict__ packed,
                                           const facetcu_csr_edge* __restrict__ edges, uint32_t e,
-                                          uint32_t& nb, float& c)
+                                          uint32_t nb_bits, uint32_t& nb, float& c)
 {
     if (packed) {
         const uint32_t p = __ldg(packed + e);
-        nb = p & kNeighborMask;
-        c = float(p >> 22);
+        nb = p & ((1u << nb_bits) - 1u);
+        c = float(p >> nb_bits);
     } else {
         const uint2 w = __ldg(reinterpret_cast<const uint2*>(edges) + e);
         nb = w.x;
@@ -205,7 +205,8 @@ template <int P, bool kBF16>
 __device__ __forceinline__ void gather_split(const uint32_t* __restrict__ rows,
                                              const uint32_t* __restrict__ packed,
                                              const facetcu_csr_edge* __restrict__ edges,
-                                             uint32_t s, const void* X, int lane, float* acc)
+                                             uint32_t nb_bits, uint32_t s, const void* X,
+                                             int lane, float* acc)
 {
     constexpr int CPL = kVecCols<kBF16>;
     constexpr int L = P / CPL;  // lanes per row = 16-byte vectors per row
@@ -216,7 +217,8 @@ __device__ __forceinline__ void gather_split(const uint32_t* __restrict__ rows,
     const uint32_t start = __ldg(rows + s), end = __ldg(rows + s + 1);
     uint32_t nbn = 0;
     float cn = 0.0f;
-    if (kPrefetch && start + uint32_t(lane) < end) edge_word(packed, edges, start + lane, nbn, cn);
+    if (kPrefetch && start + uint32_t(lane) < end)
+        edge_word(packed, edges, start + lane, nb_bits, nbn, cn);
     for (uint32_t base = start; base < end; base += 32) {
         const uint32_t n = min(32u, end - base);
         uint32_t nbv = 0;
@@ -225,9 +227,9 @@ __device__ __forceinline__ void gather_split(const uint32_t* __restrict__ rows,
             nbv = nbn;
             cv = cn;
             const uint32_t next = base + 32u + uint32_t(lane);
-            if (next < end) edge_word(packed, edges, next, nbn, cn);
+            if (next < end) edge_word(packed, edges, next, nb_bits, nbn, cn);
         } else if (uint32_t(lane) < n) {
-            edge_word(packed, edges, base + lane, nbv, cv);
+            edge_word(packed, edges, base + lane, nb_bits, nbv, cv);
         }
         for (uint32_t j = 0; j < n; j += G * U) {
             uint4 q[U];
@@ -367,7 +369,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_sweep_wide(GraphVie
                 float acc[CPL];
 #pragma unroll
                 for (int k = 0; k < CPL; ++k) acc[k] = 0.0f;
-                gather_split<P, false>(g.rows, g.packed, g.edges, s, Bin, lane, acc);
+                gather_split<P, false>(g.rows, g.packed, g.edges, g.nb_bits, s, Bin, lane, acc);
                 const uint32_t d = __ldg(g.denom + s);
                 const float skyc = float(__ldg(g.skyc + s));
                 float dir[CPL];
@@ -420,12 +422,12 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_sweep_wide(GraphVie
 
 __device__ __forceinline__ void edge_word_i(const uint32_t* __restrict__ packed,
                                             const facetcu_csr_edge* __restrict__ edges,
-                                            uint32_t e, uint32_t& nb, int& c)
+                                            uint32_t e, uint32_t nb_bits, uint32_t& nb, int& c)
 {
     if (packed) {
         const uint32_t w = __ldg(packed + e);
-        nb = w & kNeighborMask;
-        c = int(w >> 22);
+        nb = w & ((1u << nb_bits) - 1u);
+        c = int(w >> nb_bits);
     } else {
         const uint2 w = __ldg(reinterpret_cast<const uint2*>(edges) + e);
         nb = w.x;
@@ -451,7 +453,8 @@ __device__ __forceinline__ int sbyte(uint32_t w)
 template <int P>
 __device__ __forceinline__ void gather_i8(const uint32_t* __restrict__ rows,
                                           const uint32_t* __restrict__ packed,
-                                          const facetcu_csr_edge* __restrict__ edges, uint32_t s,
+                                          const facetcu_csr_edge* __restrict__ edges,
+                                          uint32_t nb_bits, uint32_t s,
                                           const int8_t* __restrict__ Q, int lane, int* acc)
 {
     constexpr int L = P / 16;              // lanes per row, 16 bytes each
@@ -469,7 +472,7 @@ __device__ __forceinline__ void gather_i8(const uint32_t* __restrict__ rows,
         nbn[w] = 0u;
         cn[w] = 0;
         const uint32_t e = start + uint32_t(w * 32 + lane);
-        if (e < end) edge_word_i(packed, edges, e, nbn[w], cn[w]);
+        if (e < end) edge_word_i(packed, edges, e, nb_bits, nbn[w], cn[w]);
     }
     for (uint32_t base = start; base < end; base += E) {
         uint32_t nbv[W];
@@ -481,7 +484,7 @@ __device__ __forceinline__ void gather_i8(const uint32_t* __restrict__ rows,
             nbn[w] = 0u;
             cn[w] = 0;
             const uint32_t e = base + uint32_t(E + w * 32 + lane);
-            if (e < end) edge_word_i(packed, edges, e, nbn[w], cn[w]);
+            if (e < end) edge_word_i(packed, edges, e, nb_bits, nbn[w], cn[w]);
         }
         uint4 q[U];
         int c[U];
@@ -613,7 +616,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_step_i8(
                 int acc[16];
 #pragma unroll
                 for (int k = 0; k < 16; ++k) acc[k] = 0;
-                gather_i8<P>(g.rows, g.packed, g.edges, s, Qin, lane, acc);
+                gather_i8<P>(g.rows, g.packed, g.edges, g.nb_bits, s, Qin, lane, acc);
                 reduce_scatter_i8<G, L>(acc, lane);
                 const uint32_t d = __ldg(g.denom + s);
                 const float inv = d ? 1.0f / float(d) : 0.0f;
@@ -896,8 +899,9 @@ __global__ void k_perm_lengths(const uint32_t* order, uint32_t S, const uint32_t
 
 __global__ void k_perm_copy(const uint32_t* order, const uint32_t* rank, uint32_t S,
                             const uint32_t* rows, const uint32_t* packed, const uint32_t* prows,
-                            uint32_t* ppacked)
+                            uint32_t* ppacked, uint32_t nb_bits)
 {
+    const uint32_t mask = (1u << nb_bits) - 1u;
     const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (s >= S) return;
@@ -905,9 +909,9 @@ __global__ void k_perm_copy(const uint32_t* order, const uint32_t* rank, uint32_
     const uint32_t b = rows[so], n = rows[so + 1] - b, pb = prows[s];
     for (uint32_t i = lane; i < n; i += 32) {
         const uint32_t p = packed[b + i];
-        const uint32_t nb = p & kNeighborMask;
+        const uint32_t nb = p & mask;
         const uint32_t nn = 2u * rank[nb >> 1] + (nb & 1u);
-        ppacked[pb + i] = nn | (p & ~kNeighborMask);
+        ppacked[pb + i] = nn | (p & ~mask);
     }
 }
 
@@ -1081,13 +1085,19 @@ cudaGraphExec_t step_graph(BatchState& st, const StepGraphKey& key)
     return exec;
 }
 
-// Panel widths: power of two, at most `cap` (128 for FP32/BF16 with a
-// packed graph, 32 otherwise), at least the remaining columns when fewer.
+// Panel widths: the widest power of two not above the remaining columns
+// (and `cap`: 128 for FP32/MIXED, 32 for FP64, or the caller's request), so
+// 65 columns run as 64 + 1 rather than one half-empty 128-wide panel; a
+// remainder below 32 columns is covered by one narrow panel.
 int panel_width(uint32_t remaining, uint32_t requested, uint32_t cap)
 {
-    uint32_t p = requested ? std::min(requested, cap) : cap;
+    const uint32_t p = requested ? std::min(requested, cap) : cap;
     uint32_t w = 1;
-    while (w < p && w < remaining) w <<= 1;
+    while (w * 2 <= p && w * 2 <= remaining) w <<= 1;
+    if (w < 32) {
+        w = 1;
+        while (w < p && w < remaining) w <<= 1;
+    }
     return int(std::min(w, cap));
 }
 
@@ -1114,7 +1124,8 @@ void ensure_permuted(DeviceGraph& gr, const BatchProblem& p, Workspace& ws, cuda
     k_set_last<<<1, 1, 0, s>>>(prows, S, total);
     FCU_LAUNCH("k_set_last");
     k_perm_copy<<<blocks_for(size_t(S) * 32, 256), 256, 0, s>>>(
-        order, rank, S, gr.row_offsets.as<uint32_t>(), gr.packed.as<uint32_t>(), prows, ppk);
+        order, rank, S, gr.row_offsets.as<uint32_t>(), gr.packed.as<uint32_t>(), prows, ppk,
+        gr.nb_bits);
     FCU_LAUNCH("k_perm_copy");
     FCU_CHECK(cudaStreamSynchronize(s));
     gr.perm_valid = true;
@@ -1150,6 +1161,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
     g.denom = perm ? gr.p_denom.as<uint32_t>() : gr.denominators.as<uint32_t>();
     g.skyc = perm ? gr.p_sky.as<uint32_t>() : gr.sky.as<uint32_t>();
     g.facets = S / 2u;
+    g.nb_bits = gr.nb_bits;
     const uint32_t cap = fp64 ? 32u : uint32_t(kMaxP);
     const int Pmax = panel_width(R, cfg.panel_width, cap);
     const size_t cells_max = size_t(S) * Pmax;

@@ -82,16 +82,51 @@ __global__ void k_closure(const uint32_t* row_offsets, const facetcu_csr_edge* e
     atomicMax(closure_bits, __float_as_uint(fabsf(c - 1.0f)));
 }
 
-__global__ void k_pack(const facetcu_csr_edge* edges, size_t n, uint32_t* packed)
+__global__ void k_pack(const facetcu_csr_edge* edges, size_t n, uint32_t nb_bits,
+                       uint32_t* packed)
 {
     const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    packed[i] = edges[i].neighbor | (edges[i].count << 22);
+    packed[i] = edges[i].neighbor | (edges[i].count << nb_bits);
 }
 
 inline unsigned grid(size_t n, unsigned b) { return unsigned((n + b - 1) / b); }
 
+// One scene's rows and edges into a block-diagonal union graph.
+__global__ void k_append_rows(const uint32_t* rows, uint32_t S, uint64_t edge_offset,
+                              uint32_t* dst)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < S) dst[i] = uint32_t(rows[i] + edge_offset);
+}
+__global__ void k_append_edges(const facetcu_csr_edge* edges, size_t n, uint32_t side_offset,
+                               facetcu_csr_edge* dst)
+{
+    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = {edges[i].neighbor + side_offset, edges[i].count};
+}
+
 }  // namespace
+
+void graph_append(DeviceGraph& dst, const DeviceGraph& src, uint32_t side_offset,
+                  uint64_t edge_offset, cudaStream_t s)
+{
+    const uint32_t S = src.surfaces;
+    if (!S) return;
+    k_append_rows<<<grid(S, 256), 256, 0, s>>>(src.row_offsets.as<uint32_t>(), S, edge_offset,
+                                                dst.row_offsets.as<uint32_t>() + side_offset);
+    FCU_LAUNCH("k_append_rows");
+    if (src.nnz) {
+        k_append_edges<<<grid(src.nnz, 256), 256, 0, s>>>(
+            src.edges.as<facetcu_csr_edge>(), src.nnz, side_offset,
+            dst.edges.as<facetcu_csr_edge>() + edge_offset);
+        FCU_LAUNCH("k_append_edges");
+    }
+    FCU_CHECK(cudaMemcpyAsync(dst.denominators.as<uint32_t>() + side_offset,
+                              src.denominators.ptr, size_t(S) * 4, cudaMemcpyDeviceToDevice, s));
+    FCU_CHECK(cudaMemcpyAsync(dst.sky.as<uint32_t>() + side_offset, src.sky.ptr, size_t(S) * 4,
+                              cudaMemcpyDeviceToDevice, s));
+}
 
 void graph_from_pairs(uint64_t* d_pairs, size_t n, int side_bits, DeviceGraph& g, Workspace& ws,
                       cudaStream_t s)
@@ -171,10 +206,16 @@ bool graph_pack(DeviceGraph& g, Workspace& ws, cudaStream_t s)
     (void)ws;
     if (g.packed_valid) return true;
     g.perm_valid = false;
-    if (g.surfaces > (1u << 22) || g.max_count >= 1024u) return false;
+    // neighbour in the low nb_bits (at least 22), count above: exact while the
+    // largest count fits the remaining bits (1023 up to 2^22 sides, 511 up
+    // to 2^23, 255 up to 2^24); otherwise the 8-byte edges are used
+    uint32_t bits = 22;
+    while (bits < 25 && (1u << bits) < g.surfaces) ++bits;
+    if ((1u << bits) < g.surfaces || bits > 24 || g.max_count >= (1u << (32 - bits))) return false;
+    g.nb_bits = bits;
     uint32_t* p = static_cast<uint32_t*>(g.packed.reserve((g.nnz + 1) * 4));
     if (g.nnz) {
-        k_pack<<<grid(g.nnz, 256), 256, 0, s>>>(g.edges.as<facetcu_csr_edge>(), g.nnz, p);
+        k_pack<<<grid(g.nnz, 256), 256, 0, s>>>(g.edges.as<facetcu_csr_edge>(), g.nnz, bits, p);
         FCU_LAUNCH("k_pack");
     }
     g.packed_valid = true;

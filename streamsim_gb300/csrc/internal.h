@@ -138,8 +138,9 @@ struct DeviceGraph {
     DeviceBuffer edges;         // nnz * {neighbor, count}
     DeviceBuffer denominators;  // S
     DeviceBuffer sky;           // S
-    DeviceBuffer packed;        // nnz u32: neighbor | count << 22 (batched solver)
+    DeviceBuffer packed;        // nnz u32: neighbor | count << nb_bits (batched solver)
     bool packed_valid = false;
+    uint32_t nb_bits = 22;  // neighbour field width of the packed words
     uint32_t max_count = 0;
     // Morton-ordered copy used by the batched solver: facets renumbered along
     // a Morton curve of their centroids, rows and neighbour ids remapped.
@@ -153,6 +154,8 @@ void graph_from_pairs(uint64_t* d_pairs, size_t pair_count, int side_bits, Devic
                       Workspace& ws, cudaStream_t s);
 // max |(sky + sum counts) / denom - 1| over sides with denom > 0, and the
 // number of sides with denom > 0.
+void graph_append(DeviceGraph& dst, const DeviceGraph& src, uint32_t side_offset,
+                  uint64_t edge_offset, cudaStream_t s);
 void graph_closure(const DeviceGraph& g, float* closure, uint32_t* sampled, Workspace& ws,
                    cudaStream_t s);
 // Build the 4-byte packed edge array (neighbor in 22 bits, count in 10 bits)

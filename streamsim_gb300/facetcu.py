@@ -200,6 +200,7 @@ SIGNATURES.update({
     "facetcu_solve_bands": (C.c_int, [_ctx, C.POINTER(SpectralParameters), _vp,
                                       C.POINTER(Direction), _vp, _vp, C.POINTER(BandResult)]),
 })
+SIGNATURES["facetcu_scene_batch"] = (C.c_int, [_ctx, _vp, _u32, _vp, C.POINTER(GraphDiagnostics)])
 OPTIONAL_SIGNATURES = {}
 MLP_INPUTS = 12
 MLP_OUTPUTS = 64
@@ -584,6 +585,18 @@ class FacetrtCuda:
             return out, res.as_dict()
         self._check(rc)
         return out, res.as_dict()
+
+    # -- scene batches ---------------------------------------------------------
+    def sceneBatch(self, models):
+        """Make this context the disjoint union of other contexts' geometry and
+        graphs; returns the side offsets (len(models) + 1) and diagnostics."""
+        handles = (C.c_void_p * len(models))(*[m.h for m in models])
+        offsets = np.zeros(len(models) + 1, np.uint32)
+        d = GraphDiagnostics()
+        self._check(self.lib.facetcu_scene_batch(self.h, C.cast(handles, C.c_void_p), len(models),
+                                                 _ptr(offsets), C.byref(d)))
+        self.facet_count = int(offsets[-1]) // 2
+        return offsets, {k: getattr(d, k) for k, _ in d._fields_}
 
     # -- spectral optics and the band loop ------------------------------------
     def spectralOptics(self, parameters, sunlit, sun, band):

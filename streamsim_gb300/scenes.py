@@ -15,6 +15,10 @@ Named workloads:
            sphere r ~ U(1.5,3) of 3,000 leaves, edge 0.08 m, normals on the
            sphere) on a 50 x 50 m soil of 20,000 triangles: 203,840 facets.
   config3  the same forest with 150 trees on 80 x 80 m: 479,600 facets.
+  c5_scenes  32 scenes with facet counts log-uniform in [20k, 400k], cycling
+           row crops (0.75 m rows of 0.3 m-wide leaf hedges), forests (the
+           config-2 tree) and urban blocks (5-40 m boxes, faces subdivided
+           into 0.5 m cells), each on its own soil.
 """
 import math
 
@@ -22,10 +26,11 @@ import numpy as np
 
 
 class Scene:
-    def __init__(self, vertices, leaf_count, name, trunk_count=0):
+    def __init__(self, vertices, leaf_count, name, trunk_count=0, walls=False):
         self.vertices = np.ascontiguousarray(vertices, np.float32)
         self.leaf_count = int(leaf_count)
         self.trunk_count = int(trunk_count)
+        self.walls = bool(walls)  # object facets are building walls and roofs
         self.name = name
 
     @property
@@ -122,6 +127,95 @@ def cylinder(base, radius, height, segments=32):
     return A, B, C
 
 
+def quad_grid(origin, u, v, nu, nv):
+    """Triangles of the parallelogram origin + s u + t v (s, t in [0, 1]) in
+    nu x nv cells, facing u x v."""
+    i, j = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    i = i.ravel()[:, None].astype(np.float64)
+    j = j.ravel()[:, None].astype(np.float64)
+    o = np.asarray(origin, np.float64)
+    du = np.asarray(u, np.float64) / nu
+    dv = np.asarray(v, np.float64) / nv
+    p00 = o + i * du + j * dv
+    return (np.concatenate([p00, p00]), np.concatenate([p00 + du, p00 + du + dv]),
+            np.concatenate([p00 + du + dv, p00 + dv]))
+
+
+def box(x0, z0, w, d, h, cell=0.5):
+    """Roof and four walls of a w x d x h box (outward normals), every face
+    subdivided into cells of about `cell` metres."""
+    n = lambda length: max(1, int(math.ceil(length / cell)))
+    faces = [((x0, h, z0), (0, 0, d), (w, 0, 0), n(d), n(w)),          # roof, +y
+             ((x0, 0, z0), (0, 0, d), (0, h, 0), n(d), n(h)),          # -x
+             ((x0 + w, 0, z0), (0, h, 0), (0, 0, d), n(h), n(d)),      # +x
+             ((x0, 0, z0), (0, h, 0), (w, 0, 0), n(h), n(w)),          # -z
+             ((x0, 0, z0 + d), (w, 0, 0), (0, h, 0), n(w), n(h))]      # +z
+    parts = [quad_grid(*f) for f in faces]
+    return tuple(np.concatenate([p[k] for p in parts]) for k in range(3))
+
+
+def row_crops(target, seed=0, leaf_edge=0.05, spacing=0.75, width=0.3):
+    """Hedge rows along x, `spacing` m apart and `width` m wide, of leaf
+    triangles (normals on the upper hemisphere) over a soil plane; about
+    `target` facets (10 % soil)."""
+    rng = np.random.default_rng(seed)
+    nq = max(8, int(round(math.sqrt(0.05 * target))))
+    leaves = max(1, target - 2 * nq * nq)
+    L = float(np.clip(math.sqrt(leaves) / 12.0, 4.0, 60.0))
+    rows = max(2, int(L / spacing))
+    row_z = -L / 2 + spacing / 2 + spacing * rng.integers(0, rows, leaves)
+    height = rng.uniform(0.4, 0.9, rows)[((row_z + L / 2 - spacing / 2) / spacing).round().astype(int)]
+    centres = np.stack([rng.uniform(-L / 2, L / 2, leaves), rng.uniform(0.05, 1.0, leaves) * height,
+                        row_z + rng.uniform(-width / 2, width / 2, leaves)], 1)
+    nrm = uniform_sphere(leaves, rng)
+    nrm[:, 1] = np.abs(nrm[:, 1])
+    leaf = _triangles_to_vertices(*equilateral(centres, nrm, leaf_edge, rng))
+    soil = _triangles_to_vertices(*soil_grid(-L / 2, L / 2, -L / 2, L / 2, nq, nq))
+    return Scene(np.concatenate([leaf, soil]), len(leaf) // 3, f"crops({target}, seed={seed})")
+
+
+def forest_of(target, seed=0):
+    """The config-2 tree (3,000 leaves and a 64-triangle trunk) repeated to
+    about `target` facets over a soil of about 10 % of them."""
+    soil_quads = max(64, int(0.05 * target))
+    trees = max(1, int(round((target - 2 * soil_quads) / 3064)))
+    extent = 10.0 + 6.0 * math.sqrt(trees)
+    return forest(trees, extent, soil_quads, seed, name=f"forest({target}, seed={seed})")
+
+
+def urban(target, seed=0, cell=0.5):
+    """5-40 m boxes on 50 m plots until about `target` facets, on a soil of
+    about 5 % of them."""
+    rng = np.random.default_rng(seed)
+    nq = max(8, int(round(math.sqrt(0.025 * target))))
+    parts = []
+    count = 2 * nq * nq
+    k = 0
+    while count < target or not parts:
+        w, d, h = rng.uniform(5.0, 40.0, 3)
+        b = box(50.0 * (k % 8) + rng.uniform(0, 50 - w), 50.0 * (k // 8) + rng.uniform(0, 50 - d),
+                w, d, h, cell)
+        parts.append(_triangles_to_vertices(*b))
+        count += len(parts[-1]) // 3
+        k += 1
+    walls = np.concatenate(parts)
+    p = walls[:, :3]
+    x0, z0 = p[:, 0].min() - 10, p[:, 2].min() - 10
+    x1, z1 = p[:, 0].max() + 10, p[:, 2].max() + 10
+    soil = _triangles_to_vertices(*soil_grid(x0, x1, z0, z1, nq, nq))
+    return Scene(np.concatenate([walls, soil]), len(walls) // 3, f"urban({target}, seed={seed})",
+                 walls=True)
+
+
+def c5_scenes(count=32, seed=0, lo=20000, hi=400000):
+    """Scenes of uneven size: facet counts log-uniform in [lo, hi], kinds
+    cycling crops, forest, urban."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(math.log(lo), math.log(hi), count)).astype(int)
+    makers = (row_crops, forest_of, urban)
+    return [makers[i % 3](int(n), seed + 1 + i) for i, n in enumerate(sizes)]
+
+
 def config1(seed=0, leaves=2048, grid=32):
     rng = np.random.default_rng(seed)
     centres = np.stack([rng.uniform(-5, 5, leaves), rng.uniform(0.2, 1.5, leaves),
@@ -193,11 +287,21 @@ def direct_geometry(scene, sunlit, sun):
     return (np.asarray(sunlit, np.float32) * cos).astype(np.float32)
 
 
-def band_optics(scene, bands=64, leaf=(0.04, 0.48), soil=(0.12, 0.30), leaf_tau_ratio=0.4):
+def band_optics(scene, bands=64, leaf=(0.04, 0.48), soil=(0.12, 0.30), leaf_tau_ratio=0.4,
+                wall=(0.20, 0.30)):
     """Per-band reflectance/transmittance (bands, S): leaf rho ramps leaf[0] ->
     leaf[1] with tau = leaf_tau_ratio * rho, soil rho soil[0] -> soil[1] and
-    tau = 0; trunk facets take the leaf reflectance with tau = 0.  Both sides
-    of a facet share its material."""
+    tau = 0; trunk facets take the leaf reflectance with tau = 0; walls (urban
+    scenes) ramp wall[0] -> wall[1] with tau = 0.  Both sides of a facet share
+    its material."""
+    if scene.walls:
+        F = scene.facet_count
+        t = np.linspace(0.0, 1.0, bands) if bands > 1 else np.zeros(1)
+        material = np.full(2 * F, 1, np.intp)
+        material[:2 * scene.leaf_count] = 0
+        rho_t = np.stack([wall[0] + (wall[1] - wall[0]) * t,
+                          soil[0] + (soil[1] - soil[0]) * t], 1).astype(np.float32)
+        return rho_t[:, material], np.zeros((bands, 2 * F), np.float32)
     F = scene.facet_count
     t = np.linspace(0.0, 1.0, bands, dtype=np.float64) if bands > 1 else np.zeros(1)
     lr = leaf[0] + (leaf[1] - leaf[0]) * t
@@ -210,6 +314,22 @@ def band_optics(scene, bands=64, leaf=(0.04, 0.48), soil=(0.12, 0.30), leaf_tau_
     rho_t = np.stack([lr, lr, sr], 1).astype(np.float32)
     tau_t = np.stack([leaf_tau_ratio * lr, np.zeros(bands), np.zeros(bands)], 1).astype(np.float32)
     return rho_t[:, material], tau_t[:, material]
+
+
+def thermal_optics(scene, temperature, wavelength_nm=11000.0, leaf_eps=0.97, ground_eps=0.95):
+    """One thermal band: rho = 1 - eps, tau = 0, emission eps * Planck(T) per
+    side (W m-2 sr-1 um-1), leaf emissivity for leaf and trunk facets, the
+    ground one for soil and walls; temperature per facet (K)."""
+    from . import facetcu
+    F = scene.facet_count
+    eps_f = np.full(F, ground_eps)
+    if not scene.walls:
+        eps_f[:scene.leaf_count] = leaf_eps
+    planck = np.array([facetcu.planck_radiance(wavelength_nm, float(t))
+                       for t in np.asarray(temperature, np.float32)])
+    eps = np.repeat(eps_f, 2)
+    rho = (1.0 - eps).astype(np.float32)
+    return rho, np.zeros_like(rho), (eps * np.repeat(planck, 2)).astype(np.float32)
 
 
 def reference_optics(scene, sunlit, sun, beam=700.0, leaf_rho=0.10, leaf_tau=0.05,

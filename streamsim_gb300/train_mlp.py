@@ -34,6 +34,8 @@ def parse(argv=None):
     p.add_argument("--small", action="store_true", help="config-1 scenes (2,048 leaves)")
     p.add_argument("--out", default=None, help="where to write the weights (.npy)")
     p.add_argument("--report", default=None, help="where to write the evaluation (.json)")
+    p.add_argument("--weights", default=None,
+                   help="evaluate these weights (.npy) instead of training")
     return p.parse_args(argv)
 
 
@@ -111,6 +113,34 @@ def evaluate(fc, case, truth, params, tolerance):
     return row
 
 
+def evaluate_only(fc, scenes, args, params, rng):
+    """Cold vs learned start on args.eval unseen seeds (the benchmark's
+    optics on the first, random optics and suns on the rest)."""
+    for _ in range(args.scenes):  # the optics draws of the training scenes
+        random_optics(rng)
+    rows = []
+    for i in range(args.eval):
+        optics = fixed_optics() if i == 0 else random_optics(rng)
+        case = make_case(fc, scenes, 10000 + i, optics, args)
+        truth = solve_truth(fc, case)
+        row = evaluate(fc, case, truth, params, args.tolerance)
+        row["seed"] = 10000 + i
+        rows.append(row)
+        case["model"].close()
+    report = dict(evaluation=rows, tolerance=args.tolerance,
+                  mean_iterations_cold=float(np.mean([r["cold"]["iterations"] for r in rows])),
+                  mean_iterations_mlp=float(np.mean([r["mlp"]["iterations"] for r in rows])),
+                  mean_ms_cold=float(np.mean([r["cold"]["seconds"] for r in rows]) * 1e3),
+                  mean_ms_mlp=float(np.mean([r["mlp"]["seconds"] for r in rows]) * 1e3),
+                  max_err_cold=float(max(r["cold"]["max_rel_err"] for r in rows)),
+                  max_err_mlp=float(max(r["mlp"]["max_rel_err"] for r in rows)))
+    print(json.dumps(report))
+    if args.report:
+        with open(args.report, "w") as f:
+            json.dump(report, f, indent=1)
+    return report
+
+
 def main(argv=None):
     import torch
 
@@ -119,6 +149,8 @@ def main(argv=None):
 
     args = parse(argv)
     rng = np.random.default_rng(20240)
+    if args.weights:
+        return evaluate_only(fc, scenes, args, np.load(args.weights), rng)
     xs, ys = [], []
     t0 = time.perf_counter()
     for i in range(args.scenes):

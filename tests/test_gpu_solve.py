@@ -177,3 +177,47 @@ def test_mixed_graph_replay_matches_per_sweep_launches(c1):
         assert ra["graph_launches"] > 0 and rb["graph_launches"] == 0
         assert ra["iterations"] == rb["iterations"]
         assert np.array_equal(a, b)
+
+
+def test_scene_batch_matches_scenes_solved_alone():
+    """facetcu_scene_batch: three scenes of uneven size (crops, urban, a
+    config-1 field) as one block-diagonal graph.  Its FP64 solve equals each
+    scene's own FP64 solve, and the MIXED solve of the batch (one launch per
+    step over all three) meets the 1e-4 bar against it, with a thermal band
+    as a 65th column (panels of 64 + 1)."""
+    parts = [scenes.row_crops(6000, 3), scenes.urban(9000, 4), scenes.config1(5, 700, 10)]
+    uv, dirs = scenes.hemisphere_samples(128, 8, seed=7)
+    suv, _ = scenes.hemisphere_samples(64, 8, seed=8)
+    models, rho, tau, emis, dgeo = [], [], [], [], []
+    rng = np.random.default_rng(0)
+    for i, sc in enumerate(parts):
+        m = model_for(sc.vertices, 256, 64)
+        m.buildHemisphereGraph(uv, dirs, 128, 64, 8)
+        sun = scenes.sun_direction(20.0 + 15 * i, 40.0 * i)
+        dgeo.append(scenes.direct_geometry(sc, m.hemisphereSunlit(sun, suv, 64, 8), sun))
+        r, t = scenes.band_optics(sc, 64)
+        tr, tt, te = scenes.thermal_optics(sc, rng.uniform(280, 320, sc.facet_count))
+        rho.append(np.vstack([r, tr]))
+        tau.append(np.vstack([t, tt]))
+        emis.append(np.vstack([np.zeros_like(r), te]))
+        models.append(m)
+    sky = np.append(np.full(64, 100.0), facetcu.planck_radiance(11000.0, 250.0)).astype(np.float32)
+    beam = np.append(np.full(64, 800.0), 0.0).astype(np.float32)
+    batch = facetcu.FacetrtCuda()
+    batch.initialize(16, 16, 8)
+    offsets, diag = batch.sceneBatch(models)
+    assert list(np.diff(offsets)) == [2 * sc.facet_count for sc in parts]
+    cat = lambda xs: np.ascontiguousarray(np.concatenate(xs, axis=-1))
+    args = (cat(rho), cat(tau), sky, beam, cat(dgeo)[None, :])
+    truth, _ = batch.solveBatched(*args, emission=cat(emis), precision=facetcu.PRECISION_FP64,
+                                  tolerance=1e-12, maximum_iterations=4000)
+    for i, m in enumerate(models):
+        alone, _ = m.solveBatched(rho[i], tau[i], sky, beam, dgeo[i][None, :], emission=emis[i],
+                                  precision=facetcu.PRECISION_FP64, tolerance=1e-12,
+                                  maximum_iterations=4000)
+        assert rel_err(truth[:, offsets[i]:offsets[i + 1]], alone) < 1e-9
+    out, res = batch.solveBatched(*args, emission=cat(emis), precision=facetcu.PRECISION_MIXED,
+                                  tolerance=1e-6)
+    assert res["converged"] and rel_err(out, truth) < 1e-4
+    for m in models + [batch]:
+        m.close()

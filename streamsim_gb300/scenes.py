@@ -320,13 +320,14 @@ def thermal_optics(scene, temperature, wavelength_nm=11000.0, leaf_eps=0.97, gro
     """One thermal band: rho = 1 - eps, tau = 0, emission eps * Planck(T) per
     side (W m-2 sr-1 um-1), leaf emissivity for leaf and trunk facets, the
     ground one for soil and walls; temperature per facet (K)."""
-    from . import facetcu
     F = scene.facet_count
     eps_f = np.full(F, ground_eps)
     if not scene.walls:
         eps_f[:scene.leaf_count] = leaf_eps
-    planck = np.array([facetcu.planck_radiance(wavelength_nm, float(t))
-                       for t in np.asarray(temperature, np.float32)])
+    # Planck's law in W m-2 sr-1 um-1 (c1 = 2 h c^2, c2 = h c / k in um K)
+    um = wavelength_nm / 1000.0
+    t = np.maximum(1.0, np.asarray(temperature, np.float64))
+    planck = 1.1910439340652e8 / (um ** 5 * np.expm1(14388.291040407 / (t * um)))
     eps = np.repeat(eps_f, 2)
     rho = (1.0 - eps).astype(np.float32)
     return rho, np.zeros_like(rho), (eps * np.repeat(planck, 2)).astype(np.float32)

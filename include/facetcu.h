@@ -217,7 +217,8 @@ typedef struct {
     uint32_t precision;         /* FACETCU_PRECISION_* */
     uint32_t warm_start;        /* FACETCU_WARM_* */
     uint32_t maximum_iterations;
-    float tolerance;            /* relative change per column */
+    float tolerance;            /* stop when every side's relative change
+                                   |dB_s| / max(|B_s|, 1e-6 max|B|) <= tolerance */
     uint32_t panel_width;       /* RHS columns per resident panel (power of two, <= 128;
                                    <= 32 in FP64); 0 = the widest that fits */
     uint32_t flags;             /* FACETCU_BATCH_TIME_SWEEPS: time every sweep kernel */

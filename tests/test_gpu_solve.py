@@ -215,7 +215,8 @@ def test_scene_batch_matches_scenes_solved_alone():
         alone, _ = m.solveBatched(rho[i], tau[i], sky, beam, dgeo[i][None, :], emission=emis[i],
                                   precision=facetcu.PRECISION_FP64, tolerance=1e-12,
                                   maximum_iterations=4000)
-        assert rel_err(truth[:, offsets[i]:offsets[i + 1]], alone) < 1e-9
+        # both FP64 to 1e-12, written as float32: equal to the last bits
+        assert rel_err(truth[:, offsets[i]:offsets[i + 1]], alone) < 1e-6
     out, res = batch.solveBatched(*args, emission=cat(emis), precision=facetcu.PRECISION_MIXED,
                                   tolerance=1e-6)
     assert res["converged"] and rel_err(out, truth) < 1e-4

@@ -869,20 +869,37 @@ static float ray_triangle(vec3 o, vec3 d, vec3 a, vec3 e1, vec3 e2)
 
 static vec3 vpos(const orc_vertex *v) { return v3(v->position[0], v->position[1], v->position[2]); }
 
-static int closest_hit(const orc_vertex *V, uint32_t F, uint32_t skip, vec3 o, vec3 d, float *tbest)
+/* Nearest hit over the scene and its periodic copies (the raster mode's
+ * tiles): copy t is met by shifting the origin back by its offset; the hit
+ * names the original facet; the origin facet is skipped in tile 0 only;
+ * the smallest (t, facet) wins. */
+static int closest_hit_tiles(const orc_vertex *V, uint32_t F, uint32_t skip, vec3 o, vec3 d,
+                             uint32_t periodic_count, float size_x, float size_z, float *tbest)
 {
     int best = -1;
     float bt = FLT_MAX;
-    for (uint32_t g = 0; g < F; ++g) {
-        if (g == skip) continue;
-        const vec3 a = vpos(&V[g * 3U]);
-        const vec3 e1 = vsub(vpos(&V[g * 3U + 1U]), a);
-        const vec3 e2 = vsub(vpos(&V[g * 3U + 2U]), a);
-        const float t = ray_triangle(o, d, a, e1, e2);
-        if (t > 0.0f && t < bt) { bt = t; best = (int)g; }
+    const uint32_t tiles = (periodic_count < 20U ? periodic_count : 20U) + 1U;
+    for (uint32_t tile = 0; tile < tiles; ++tile) {
+        int tx, tz;
+        periodic_tile(tile, &tx, &tz);
+        const float ox = (float)tx * size_x, oz = (float)tz * size_z;
+        const vec3 ot = v3(o.v[0] - ox, o.v[1], o.v[2] - oz);
+        for (uint32_t g = 0; g < F; ++g) {
+            if (tile == 0U && g == skip) continue;
+            const vec3 a = vpos(&V[g * 3U]);
+            const vec3 e1 = vsub(vpos(&V[g * 3U + 1U]), a);
+            const vec3 e2 = vsub(vpos(&V[g * 3U + 2U]), a);
+            const float t = ray_triangle(ot, d, a, e1, e2);
+            if (t > 0.0f && (t < bt || (t == bt && (int)g < best))) { bt = t; best = (int)g; }
+        }
     }
     *tbest = bt;
     return best;
+}
+
+static int closest_hit(const orc_vertex *V, uint32_t F, uint32_t skip, vec3 o, vec3 d, float *tbest)
+{
+    return closest_hit_tiles(V, F, skip, o, d, 0U, 1.0f, 1.0f, tbest);
 }
 
 static vec3 sample_origin(const orc_vertex *V, uint32_t f, float u, float v)
@@ -916,6 +933,15 @@ int orc_hemisphere_graph(const orc_vertex *V, uint32_t F, const float *uv,
                          const float *dirs, uint32_t rays, uint32_t sets, uint32_t top_k,
                          orc_graph *g, uint64_t *dropped_out)
 {
+    return orc_hemisphere_graph_periodic(V, F, uv, dirs, rays, sets, top_k, 0U, 1.0f, 1.0f, g,
+                                         dropped_out);
+}
+
+int orc_hemisphere_graph_periodic(const orc_vertex *V, uint32_t F, const float *uv,
+                                  const float *dirs, uint32_t rays, uint32_t sets,
+                                  uint32_t top_k, uint32_t periodic_count, float size_x,
+                                  float size_z, orc_graph *g, uint64_t *dropped_out)
+{
     memset(g, 0, sizeof(*g));
     const uint32_t S = 2U * F;
     g->surface_count = S;
@@ -944,7 +970,7 @@ int orc_hemisphere_graph(const orc_vertex *V, uint32_t F, const float *uv,
                               T.v[1] * dx + Bt.v[1] * dy + N.v[1] * dz,
                               T.v[2] * dx + Bt.v[2] * dy + N.v[2] * dz);
             float t;
-            const int hit = closest_hit(V, F, f, o, d, &t);
+            const int hit = closest_hit_tiles(V, F, f, o, d, periodic_count, size_x, size_z, &t);
             if (hit < 0) { ++sky; continue; }
             const vec3 ng = v3(V[hit * 3U].normal[0], V[hit * 3U].normal[1], V[hit * 3U].normal[2]);
             hits[nh++] = 2U * (uint32_t)hit + (vdot(ng, d) < 0.0f ? 0U : 1U);
@@ -985,6 +1011,14 @@ int orc_hemisphere_graph(const orc_vertex *V, uint32_t F, const float *uv,
 int orc_hemisphere_sunlit(const orc_vertex *V, uint32_t F, const float *uv,
                           uint32_t samples, uint32_t sets, orc_direction sun, float *fraction)
 {
+    return orc_hemisphere_sunlit_periodic(V, F, uv, samples, sets, sun, 0U, 1.0f, 1.0f, fraction);
+}
+
+int orc_hemisphere_sunlit_periodic(const orc_vertex *V, uint32_t F, const float *uv,
+                                   uint32_t samples, uint32_t sets, orc_direction sun,
+                                   uint32_t periodic_count, float size_x, float size_z,
+                                   float *fraction)
+{
     const vec3 d = v3(sun.x, sun.y, sun.z);
     for (uint32_t s = 0; s < 2U * F; ++s) {
         const uint32_t f = s >> 1U;
@@ -997,7 +1031,7 @@ int orc_hemisphere_sunlit(const orc_vertex *V, uint32_t F, const float *uv,
             const size_t k = (size_t)set * samples + j;
             const vec3 o = sample_origin(V, f, uv[2 * k], uv[2 * k + 1]);
             float t;
-            if (closest_hit(V, F, f, o, d, &t) < 0) ++lit;
+            if (closest_hit_tiles(V, F, f, o, d, periodic_count, size_x, size_z, &t) < 0) ++lit;
         }
         fraction[s] = (float)lit / (float)samples;
     }

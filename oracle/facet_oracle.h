@@ -117,6 +117,19 @@ int orc_hemisphere_graph(const orc_vertex *vertices, uint32_t facet_count,
 int orc_hemisphere_sunlit(const orc_vertex *vertices, uint32_t facet_count,
                           const float *sample_uv, uint32_t samples, uint32_t sets,
                           orc_direction sun, float *fraction);
+/* The same with the scene's periodic copies (the raster mode's tiles,
+ * facetrtcore.cpp:226-237): nearest hit over the scene and up to 20 copies
+ * offset by (tx * size_x, tz * size_z); the origin facet is skipped in the
+ * scene's own tile only. */
+int orc_hemisphere_graph_periodic(const orc_vertex *vertices, uint32_t facet_count,
+                                  const float *sample_uv, const float *sample_dir,
+                                  uint32_t rays_per_side, uint32_t sets, uint32_t top_k,
+                                  uint32_t periodic_count, float size_x, float size_z,
+                                  orc_graph *out, uint64_t *dropped);
+int orc_hemisphere_sunlit_periodic(const orc_vertex *vertices, uint32_t facet_count,
+                                   const float *sample_uv, uint32_t samples, uint32_t sets,
+                                   orc_direction sun, uint32_t periodic_count, float size_x,
+                                   float size_z, float *fraction);
 
 void orc_free(void *p);
 

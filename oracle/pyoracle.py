@@ -158,6 +158,12 @@ class Oracle:
                                            C.POINTER(OrcGraph), C.POINTER(C.c_uint64)]
         L.orc_hemisphere_sunlit.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
                                             C.c_uint32, OrcDirection, C.c_void_p]
+        L.orc_hemisphere_graph_periodic.argtypes = [
+            C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+            C.c_uint32, C.c_float, C.c_float, C.c_void_p, C.c_void_p]
+        L.orc_hemisphere_sunlit_periodic.argtypes = [
+            C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, OrcDirection, C.c_uint32,
+            C.c_float, C.c_float, C.c_void_p]
         L.orc_free.argtypes = [C.c_void_p]
 
     # -- geometry helpers -------------------------------------------------
@@ -275,24 +281,27 @@ class Oracle:
         return out
 
     # -- hemisphere mode -----------------------------------------------
-    def hemisphere_graph(self, vertices, sample_uv, sample_dir, rays, sets, top_k):
+    def hemisphere_graph(self, vertices, sample_uv, sample_dir, rays, sets, top_k,
+                         periodic=(0, 1.0, 1.0)):
         vertices = np.ascontiguousarray(vertices, np.float32)
         sample_uv = np.ascontiguousarray(sample_uv, np.float32)
         sample_dir = np.ascontiguousarray(sample_dir, np.float32)
         g = OrcGraph()
         dropped = C.c_uint64()
-        self.lib.orc_hemisphere_graph(vertices.ctypes.data, len(vertices) // 3,
-                                      sample_uv.ctypes.data, sample_dir.ctypes.data, rays, sets,
-                                      top_k, C.byref(g), C.byref(dropped))
+        self.lib.orc_hemisphere_graph_periodic(
+            vertices.ctypes.data, len(vertices) // 3, sample_uv.ctypes.data,
+            sample_dir.ctypes.data, rays, sets, top_k, int(periodic[0]), C.c_float(periodic[1]),
+            C.c_float(periodic[2]), C.byref(g), C.byref(dropped))
         return self._take_graph(g), dropped.value
 
-    def hemisphere_sunlit(self, vertices, sample_uv, samples, sets, sun):
+    def hemisphere_sunlit(self, vertices, sample_uv, samples, sets, sun, periodic=(0, 1.0, 1.0)):
         vertices = np.ascontiguousarray(vertices, np.float32)
         sample_uv = np.ascontiguousarray(sample_uv, np.float32)
         out = np.zeros(2 * (len(vertices) // 3), np.float32)
         d = OrcDirection(*[float(x) for x in sun])
-        self.lib.orc_hemisphere_sunlit(vertices.ctypes.data, len(vertices) // 3,
-                                       sample_uv.ctypes.data, samples, sets, d, out.ctypes.data)
+        self.lib.orc_hemisphere_sunlit_periodic(
+            vertices.ctypes.data, len(vertices) // 3, sample_uv.ctypes.data, samples, sets, d,
+            int(periodic[0]), C.c_float(periodic[1]), C.c_float(periodic[2]), out.ctypes.data)
         return out
 
 

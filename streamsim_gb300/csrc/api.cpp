@@ -113,6 +113,17 @@ const int kTileOffsets[20][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}, {-1, -1}, {-1
                                  {1, 1},  {-2, 0}, {2, 0}, {0, -2}, {0, 2}, {-2, -1}, {-2, 1},
                                  {2, -1}, {2, 1},  {-1, -2}, {1, -2}, {-1, 2}, {1, 2}};
 
+PeriodicTiles make_tiles(const facetcu_context* ctx)
+{
+    PeriodicTiles p;
+    p.count = std::min(ctx->config.periodic_neighbor_count, 20u);
+    for (uint32_t t = 1; t <= p.count; ++t) {
+        p.dx[t] = float(kTileOffsets[t - 1][0]) * ctx->config.periodic_size_x;
+        p.dz[t] = float(kTileOffsets[t - 1][1]) * ctx->config.periodic_size_z;
+    }
+    return p;
+}
+
 RasterFrame make_frame(const facetcu_context* ctx)
 {
     RasterFrame f{};
@@ -611,8 +622,8 @@ int facetcu_build_hemisphere_graph(facetcu_context* ctx, const facetcu_hemispher
         unsigned long long drop = 0;
         hemisphere_graph(ctx->vertices.as<facetcu_vertex>(), ctx->facets, ctx->bvh,
                          ctx->samples_uv.as<float>(), ctx->samples_dir.as<float>(),
-                         config->rays_per_side, config->sample_sets, config->top_k, g, &drop,
-                         ctx->ws, s);
+                         config->rays_per_side, config->sample_sets, config->top_k,
+                         make_tiles(ctx), g, &drop, ctx->ws, s);
         float closure = 0.0f;
         uint32_t sampled = 0;
         graph_closure(g, &closure, &sampled, ctx->ws, s);
@@ -649,7 +660,7 @@ int facetcu_hemisphere_sunlit(facetcu_context* ctx, const facetcu_direction* sun
         float* d = static_cast<float*>(ctx->fraction.reserve(size_t(S) * 4));
         hemisphere_sunlit(ctx->vertices.as<facetcu_vertex>(), ctx->facets, ctx->bvh,
                           ctx->samples_uv.as<float>(), samples, sample_sets,
-                          make_float3(sun->x, sun->y, sun->z), d, s);
+                          make_float3(sun->x, sun->y, sun->z), make_tiles(ctx), d, s);
         FCU_CHECK(cudaMemcpyAsync(fraction, d, size_t(S) * 4, cudaMemcpyDeviceToHost, s));
         FCU_CHECK(cudaStreamSynchronize(s));
         return FACETCU_OK;

@@ -8,8 +8,10 @@
 // seen: 2g if the ray meets g's normal side, 2g + 1 otherwise.  The warp
 // sorts the 32 x (rays/32) hit ids in shared memory, counts runs, keeps the
 // top_k most-hit sides (ties: lower side index) and writes the row sorted
-// by neighbour with denominator = kept + sky rays.  Exactly the rules of the
-// C oracle (orc_hemisphere_graph), so counts are comparable bit for bit.
+// by neighbour with denominator = kept + sky rays.  With periodic tiles the
+// nearest hit is taken over the scene and its copies (see Tiles).  Exactly
+// the rules of the C oracle (orc_hemisphere_graph_periodic), so counts are
+// comparable bit for bit.
 // This file is compiled with -fmad=false: the origin, direction and
 // Moller-Trumbore arithmetic round like the oracle's.
 #include <cfloat>
@@ -77,14 +79,14 @@ struct Hit {
     uint32_t facet;
 };
 
-// Nearest hit (any_hit = false) or occlusion (any_hit = true) over the LBVH.
-// Returns false when the traversal stack overflowed.
+// Nearest hit (any_hit = false) or occlusion (any_hit = true) over the LBVH,
+// improving on `best` (callers start it at {FLT_MAX, kSky}; periodic tiles
+// carry it from tile to tile).  Returns false when the traversal stack
+// overflowed.
 template <bool kAny>
 __device__ bool trace(const float4* __restrict__ nodes, const float4* __restrict__ tri,
                       uint32_t leaves, Vec o, Vec d, uint32_t skip, Hit& best)
 {
-    best.t = FLT_MAX;
-    best.facet = kSky;
     const Vec inv = {safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
     auto test_leaf = [&](uint32_t k) {
         const float4 A = __ldg(tri + 3 * size_t(k));
@@ -142,6 +144,31 @@ __device__ bool trace(const float4* __restrict__ nodes, const float4* __restrict
 struct Frame {
     Vec N, T, B;
 };
+
+// Periodic tiles (the raster mode's: the scene plus up to 20 copies offset by
+// periodicTileOffset(t) x (periodicSizeX, periodicSizeZ)).  A copy is met by
+// shifting the ray origin back by the tile's offset; the hit names the
+// original facet; the origin facet is skipped in the scene's own tile only.
+struct Tiles {
+    float x[21], z[21];
+    uint32_t n;
+};
+
+template <bool kAny>
+__device__ bool trace_tiles(const float4* __restrict__ nodes, const float4* __restrict__ tri,
+                            uint32_t leaves, const Tiles& tiles, Vec o, Vec d, uint32_t skip,
+                            Hit& best)
+{
+    best.t = FLT_MAX;
+    best.facet = kSky;
+    bool ok = true;
+    for (uint32_t t = 0; t < tiles.n; ++t) {
+        const Vec ot = {o.x - tiles.x[t], o.y, o.z - tiles.z[t]};
+        ok &= trace<kAny>(nodes, tri, leaves, ot, d, t == 0 ? skip : kSky, best);
+        if (kAny && best.facet != kSky) break;
+    }
+    return ok;
+}
 
 // The oracle's side_frame: helper = |N.y| < 0.9 ? +Y : +X.
 __device__ __forceinline__ Frame side_frame(const facetcu_vertex* V, uint32_t s)
@@ -205,7 +232,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_hemi_rows(
     const facetcu_vertex* __restrict__ V, const float4* __restrict__ nodes,
     const float4* __restrict__ tri, uint32_t leaves, uint32_t surfaces, const float* __restrict__ uv,
     const float* __restrict__ dirs, uint32_t rays, uint32_t sets, uint32_t npow, uint32_t top_k,
-    uint32_t* tmp_edges, uint32_t* nnz, uint32_t* denom, uint32_t* skyc,
+    Tiles tiles, uint32_t* tmp_edges, uint32_t* nnz, uint32_t* denom, uint32_t* skyc,
     unsigned long long* dropped, uint32_t* error)
 {
     extern __shared__ uint32_t smem[];
@@ -228,7 +255,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_hemi_rows(
                                fr.T.y * dx + fr.B.y * dy + fr.N.y * dz,
                                fr.T.z * dx + fr.B.z * dy + fr.N.z * dz};
                 Hit h;
-                if (!trace<false>(nodes, tri, leaves, o, d, f, h)) atomicExch(error, 1u);
+                if (!trace_tiles<false>(nodes, tri, leaves, tiles, o, d, f, h))
+                    atomicExch(error, 1u);
                 if (h.facet != kSky) {
                     const Vec ng = {V[3 * h.facet].normal[0], V[3 * h.facet].normal[1],
                                     V[3 * h.facet].normal[2]};
@@ -343,7 +371,7 @@ __global__ void __launch_bounds__(256) k_hemi_sunlit(const facetcu_vertex* __res
                                                      const float4* __restrict__ tri, uint32_t leaves,
                                                      uint32_t surfaces, const float* __restrict__ uv,
                                                      uint32_t samples, uint32_t sets, Vec sun,
-                                                     float* fraction, uint32_t* error)
+                                                     Tiles tiles, float* fraction, uint32_t* error)
 {
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -360,19 +388,30 @@ __global__ void __launch_bounds__(256) k_hemi_sunlit(const facetcu_vertex* __res
         const size_t k = size_t(set) * samples + j;
         const Vec o = sample_origin(V, f, uv[2 * k], uv[2 * k + 1]);
         Hit h;
-        if (!trace<true>(nodes, tri, leaves, o, sun, f, h)) atomicExch(error, 1u);
+        if (!trace_tiles<true>(nodes, tri, leaves, tiles, o, sun, f, h)) atomicExch(error, 1u);
         if (h.facet == kSky) ++lit;
     }
     for (int o = 16; o > 0; o >>= 1) lit += __shfl_xor_sync(0xffffffffu, lit, o);
     if (lane == 0) fraction[s] = float(lit) / float(samples);
 }
 
+Tiles make_tiles(const PeriodicTiles& p)
+{
+    Tiles t{};
+    t.n = std::min<uint32_t>(p.count, 20u) + 1u;
+    for (uint32_t i = 0; i < t.n; ++i) {
+        t.x[i] = p.dx[i];
+        t.z[i] = p.dz[i];
+    }
+    return t;
+}
+
 }  // namespace
 
 void hemisphere_graph(const facetcu_vertex* d_vertices, uint32_t facets, const Lbvh& bvh,
                       const float* d_uv, const float* d_dir, uint32_t rays, uint32_t sets,
-                      uint32_t top_k, DeviceGraph& g, unsigned long long* dropped, Workspace& ws,
-                      cudaStream_t s)
+                      uint32_t top_k, const PeriodicTiles& periodic, DeviceGraph& g,
+                      unsigned long long* dropped, Workspace& ws, cudaStream_t s)
 {
     const uint32_t S = 2u * facets;
     top_k = std::min(top_k, rays);
@@ -400,7 +439,7 @@ void hemisphere_graph(const facetcu_vertex* d_vertices, uint32_t facets, const L
     const unsigned grid_blocks = unsigned(std::max(1, sms * std::max(per_sm, 1)));
     k_hemi_rows<<<grid_blocks, kWarps * 32, smem, s>>>(
         d_vertices, bvh.nodes.as<float4>(), bvh.tri.as<float4>(), bvh.leaves, S, d_uv, d_dir, rays,
-        sets, npow, top_k, tmp_edges, rows, den, sky, d_dropped, d_error);
+        sets, npow, top_k, make_tiles(periodic), tmp_edges, rows, den, sky, d_dropped, d_error);
     FCU_LAUNCH("k_hemi_rows");
     // rows currently holds per-side nnz; scan in place into offsets
     exclusive_scan_u32(rows, rows, S, d_total, ws, s);
@@ -422,7 +461,7 @@ void hemisphere_graph(const facetcu_vertex* d_vertices, uint32_t facets, const L
 
 void hemisphere_sunlit(const facetcu_vertex* d_vertices, uint32_t facets, const Lbvh& bvh,
                        const float* d_uv, uint32_t samples, uint32_t sets, float3 sun,
-                       float* d_fraction, cudaStream_t s)
+                       const PeriodicTiles& periodic, float* d_fraction, cudaStream_t s)
 {
     const uint32_t S = 2u * facets;
     DeviceBuffer err;
@@ -431,7 +470,7 @@ void hemisphere_sunlit(const facetcu_vertex* d_vertices, uint32_t facets, const 
     k_hemi_sunlit<<<(S * 32 + 255) / 256, 256, 0, s>>>(d_vertices, bvh.nodes.as<float4>(),
                                                        bvh.tri.as<float4>(), bvh.leaves, S, d_uv,
                                                        samples, sets, {sun.x, sun.y, sun.z},
-                                                       d_fraction, d_error);
+                                                       make_tiles(periodic), d_fraction, d_error);
     FCU_LAUNCH("k_hemi_sunlit");
     uint32_t e = 0;
     FCU_CHECK(cudaMemcpyAsync(&e, d_error, 4, cudaMemcpyDeviceToHost, s));

@@ -217,13 +217,18 @@ void lbvh_build(const facetcu_vertex* d_vertices, uint32_t facets, Lbvh& bvh, Wo
 // Facet ids sorted by the 30-bit Morton code of their centroids in [lo, hi].
 void morton_order(const facetcu_vertex* d_vertices, uint32_t facets, const float lo[3],
                   const float hi[3], uint32_t* d_order, Workspace& ws, cudaStream_t s);
+// Periodic tile offsets (tile 0 = the scene itself), as in RasterFrame.
+struct PeriodicTiles {
+    uint32_t count = 0;  // neighbour tiles (<= 20)
+    float dx[21] = {}, dz[21] = {};
+};
 void hemisphere_graph(const facetcu_vertex* d_vertices, uint32_t facets, const Lbvh& bvh,
                       const float* d_uv, const float* d_dir, uint32_t rays, uint32_t sets,
-                      uint32_t top_k, DeviceGraph& g, unsigned long long* dropped,
-                      Workspace& ws, cudaStream_t s);
+                      uint32_t top_k, const PeriodicTiles& periodic, DeviceGraph& g,
+                      unsigned long long* dropped, Workspace& ws, cudaStream_t s);
 void hemisphere_sunlit(const facetcu_vertex* d_vertices, uint32_t facets, const Lbvh& bvh,
                        const float* d_uv, uint32_t samples, uint32_t sets, float3 sun,
-                       float* d_fraction, cudaStream_t s);
+                       const PeriodicTiles& periodic, float* d_fraction, cudaStream_t s);
 
 // ---- warm-start MLP (mlp.cu) -----------------------------------------------
 namespace mlp {

@@ -141,3 +141,30 @@ def test_hemisphere_argument_validation():
     with pytest.raises(ValueError, match="rays_per_side"):
         m.buildHemisphereGraph(big_uv, big_dirs, 1024, 16, 1)
     m.close()
+
+
+@pytest.mark.parametrize("neighbours", [4, 8, 20])
+def test_hemisphere_periodic_tiles_bit_exact(oracle, neighbours):
+    """Periodic tiling in the hemisphere mode: rays see the scene and its
+    copies in the raster mode's neighbour tiles (offsets of the tile size,
+    here the 10 m field), against the oracle's brute-force caster over the
+    same tiles.  Low grazing rays from the soil now hit leaves of the copies
+    instead of the sky."""
+    sc = scenes.config1(seed=4, leaves=250, grid=6)
+    rays = 64
+    uv, dirs = scenes.hemisphere_samples(rays, 8, seed=6)
+    m = facetcu.FacetrtCuda()
+    m.initialize(64, 64, 64, 0, neighbours, 10.0, 10.0)
+    m.setGeometry(sc.vertices)
+    m.buildHemisphereGraph(uv, dirs, rays, 32, 8)
+    g, _ = oracle.hemisphere_graph(sc.vertices, uv, dirs, rays, 8, 32,
+                                   periodic=(neighbours, 10.0, 10.0))
+    assert graphs_equal(m.graph(), g) is None
+    flat, _ = oracle.hemisphere_graph(sc.vertices, uv, dirs, rays, 8, 32)
+    assert g.sky_counts.sum() < flat.sky_counts.sum()  # the copies block sky
+    suv, _ = scenes.hemisphere_samples(32, 8, seed=7)
+    sun = scenes.sun_direction(70.0, 30.0)
+    lit = m.hemisphereSunlit(sun, suv, 32, 8)
+    assert np.array_equal(lit, oracle.hemisphere_sunlit(sc.vertices, suv, 32, 8, sun,
+                                                        periodic=(neighbours, 10.0, 10.0)))
+    m.close()

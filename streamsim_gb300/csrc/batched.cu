@@ -52,6 +52,7 @@ struct PanelParams {
     const float* direct;
     const float* skyL;    // [P]
     const float* colmax;  // [P] max|B| of the previous sweep (floor of the per-side test)
+    const float* omega;   // [P] Chebyshev weight of the int8 step being formed (or null)
 };
 
 // The per-side stop test: |dB_s| / max(|B_s|, kSideFloor * max|B|) <= tol
@@ -441,6 +442,16 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_sweep_wide(GraphVie
 // BF16 defect, while each gathered neighbour row is half as wide and no
 // periodic FP32 correction sweep is needed.  |R_out| < max|R_in| because
 // c < 1, so Q_out fits in [-127, 127] (clamped all the same).
+//
+// Chebyshev acceleration (Golub and Varga's semi-iterative method on
+// [-c, c]): the step formed is delta' = omega R + (omega - 1) delta instead
+// of R, with the weights omega_1 = 1, omega_2 = 1 / (1 - c^2 / 2),
+// omega_{k+1} = 1 / (1 - c^2 omega_k / 4).  K is non-negative, so every
+// eigenvalue lies in |lambda| <= c, its Perron root; c is estimated per
+// column from the residual ratio after kChebWarm plain steps and Chebyshev
+// is used only for c <= kChebMax, where the convergence ellipse of [-c, c]
+// holds that whole disk.  R is updated by exactly the applied step, so the
+// weights change the path, never the fixed point.
 
 __device__ __forceinline__ void edge_word_i(const uint32_t* __restrict__ packed,
                                             const facetcu_csr_edge* __restrict__ edges,
@@ -620,14 +631,17 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_step_i8(
     constexpr int L = P / 16, G = 32 / L, NC = P / 32;
     const int lane = threadIdx.x & 31;
     const int col0 = (lane % L) * 16 + i8_offset<G>(lane / L);
-    float si[NC], inv_so[NC], md[NC], mb[NC];
+    float si[NC], inv_so[NC], md[NC], mb[NC], mr[NC], om[NC], fl[NC];
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
         si[k] = sig_in[col0 + k];
         const float so = sig_out[col0 + k];
         inv_so[k] = so > 0.0f ? 1.0f / so : 0.0f;
+        om[k] = pp.omega ? pp.omega[col0 + k] : 1.0f;
+        fl[k] = kSideFloor * pp.colmax[col0 + k];
         md[k] = 0.0f;
         mb[k] = 0.0f;
+        mr[k] = 0.0f;
     }
     for_each_facet(g.facets, counter, lane, [&](uint32_t f) {
         {
@@ -667,10 +681,17 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_step_i8(
                 x1[k] += dl1;
                 e0[k] = e0[k] - dl0 + kd0;
                 e1[k] = e1[k] - dl1 + kd1;
-                q0[k] = max(-127, min(127, __float2int_rn(e0[k] * inv_so[k])));
-                q1[k] = max(-127, min(127, __float2int_rn(e1[k] * inv_so[k])));
+                // next step: omega R + (omega - 1) delta (omega = 1: the residual)
+                const float n0 = om[k] * e0[k] + (om[k] - 1.0f) * dl0;
+                const float n1 = om[k] * e1[k] + (om[k] - 1.0f) * dl1;
+                q0[k] = max(-127, min(127, __float2int_rn(n0 * inv_so[k])));
+                q1[k] = max(-127, min(127, __float2int_rn(n1 * inv_so[k])));
                 md[k] = fmaxf(md[k], fmaxf(fabsf(e0[k]), fabsf(e1[k])));
                 mb[k] = fmaxf(mb[k], fmaxf(fabsf(x0[k]), fabsf(x1[k])));
+                // per-side test on the exact residual: R is the change the
+                // next Jacobi sweep would make
+                mr[k] = fmaxf(mr[k], fmaxf(__fdividef(fabsf(e0[k]), fmaxf(fabsf(x0[k]), fl[k])),
+                                           __fdividef(fabsf(e1[k]), fmaxf(fabsf(x1[k]), fl[k]))));
             }
             VecN<NC>::st(X + i0, x0);
             VecN<NC>::st(X + i1, x1);
@@ -680,9 +701,6 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_step_i8(
             VecN<NC>::stq(Qout + i1, q1);
         }
     });
-    float mr[NC];
-#pragma unroll
-    for (int k = 0; k < NC; ++k) mr[k] = 0.0f;  // the steps stop on the absolute test
     publish_cols<NC>(md, mb, mr, col0, true, P, stats);
 }
 
@@ -801,9 +819,46 @@ __global__ void k_defect_init(const float* Bold, const float* Bnew, __nv_bfloat1
 // in colmax (the next sweep's floor) and clears the stats.  With scale_a /
 // scale_b, also stores max|dB| / 127 per column there (the int8 step
 // scales).
+constexpr float kChebWarm = 4.0f;  // plain int8 steps before c is estimated
+constexpr float kChebMax = 0.7f;   // largest c for which the weights are used
+
+// Chebyshev state per column (cheb[0..4 kMaxP)): previous max|R|, c (-1 =
+// off), the weight of the step being formed, steps done.  mode 1: reset
+// after an FP32 sweep (max|R_0| = md); mode 2: after an int8 step, advance
+// the schedule and size the next scale for omega R + (omega - 1) delta.
+__device__ __forceinline__ float cheb_advance(float* cheb, int c, int mode, float md)
+{
+    float* prev = cheb;
+    float* cc = cheb + kMaxP;
+    float* om = cheb + 2 * kMaxP;
+    float* nn = cheb + 3 * kMaxP;
+    if (mode == 1) {
+        prev[c] = md;
+        cc[c] = 0.0f;
+        om[c] = 1.0f;
+        nn[c] = 0.0f;
+        return 1.0f;
+    }
+    const float n = nn[c] + 1.0f;
+    nn[c] = n;
+    float w = 1.0f;
+    if (n < kChebWarm) {
+        prev[c] = md;
+    } else if (n == kChebWarm) {
+        const float est = prev[c] > 0.0f ? md / prev[c] : 0.0f;
+        cc[c] = est > 0.0f && est <= kChebMax ? est : -1.0f;
+    } else if (cc[c] > 0.0f) {
+        const float c2 = cc[c] * cc[c];
+        w = n == kChebWarm + 1.0f ? 1.0f / (1.0f - 0.5f * c2) : 1.0f / (1.0f - 0.25f * c2 * om[c]);
+    }
+    om[c] = w;
+    return w;
+}
+
 __global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint32_t it,
                         uint32_t* counter, float* scale_a, float* scale_b, uint32_t* it_dev,
-                        bool per_side, float* colmax)
+                        bool per_side, float* colmax, float* cheb = nullptr, int cheb_mode = 0,
+                        const float* scale_prev = nullptr)
 {
     __shared__ int all_ok, abs_ok;
     __shared__ float worst;
@@ -825,8 +880,13 @@ __global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint3
         if (!a_ok) atomicExch(&abs_ok, 0);
         if (!(per_side ? s_ok : a_ok)) atomicExch(&all_ok, 0);
         atomicMax(reinterpret_cast<int*>(&worst), __float_as_int(per_side ? mr : rel));
-        // int8 step scales: sigma = max|R| / 127 for the column
-        if (scale_a && !already) scale_a[threadIdx.x] = md / 127.0f;
+        // int8 step scales: sigma = max|R| / 127 for the column, or with
+        // Chebyshev weights a bound on omega R + (omega - 1) delta
+        float w = 1.0f;
+        if (cheb && !already) w = cheb_advance(cheb, int(threadIdx.x), cheb_mode, md);
+        float sigma = md / 127.0f;
+        if (w != 1.0f && scale_prev) sigma = (w * md + (w - 1.0f) * 127.0f * scale_prev[threadIdx.x]) / 127.0f;
+        if (scale_a && !already) scale_a[threadIdx.x] = sigma;
         if (scale_b && !already) scale_b[threadIdx.x] = md / 127.0f;
         if (colmax && !already) colmax[threadIdx.x] = mb;
     }
@@ -1088,9 +1148,10 @@ void record_steps(const StepGraphKey& k, cudaStream_t s)
     for (uint32_t j = 0; j < kStepBatch; ++j) {
         launch_step_i8(k.P, k.g, k.pp, qb[j & 1u], qb[(j + 1) & 1u], k.X, k.R, slot[j & 1u],
                        slot[(j + 1) & 1u], k.stats, counter, k.flag + 3, s);
+        float* colmax = reinterpret_cast<float*>(k.flag + 16);
         k_check<<<1, kMaxP, 0, s>>>(k.stats, k.flag + 3, k.P, k.tol, 0u, counter, slot[j & 1u],
-                                    nullptr, k.flag + 12, false,
-                                    reinterpret_cast<float*>(k.flag + 16));
+                                    nullptr, k.flag + 12, true, colmax, colmax + 3 * kMaxP, 2,
+                                    slot[(j + 1) & 1u]);
         FCU_LAUNCH("k_check");
     }
 }
@@ -1209,12 +1270,13 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
     char* x1 = static_cast<char*>(st.x1.reserve(cells_max * elem));
     float* prm = static_cast<float*>(st.q.reserve(cells_max * 4 * 4 + kMaxP * 4));
     // [3 kMaxP stats: max|dB|, max|B|, max per-side change][16 flags]
-    // [kMaxP colmax][2 kMaxP int8 step scales]
-    uint32_t* stats = static_cast<uint32_t*>(st.colstats.reserve((6 * kMaxP + 16) * 4));
+    // [kMaxP colmax][2 kMaxP int8 step scales][4 kMaxP Chebyshev state]
+    uint32_t* stats = static_cast<uint32_t*>(st.colstats.reserve((10 * kMaxP + 16) * 4));
     uint32_t* flag = stats + 3 * kMaxP;
     uint32_t* counter = flag + 8;
     float* colmax = reinterpret_cast<float*>(flag + 16);
     float* sig = colmax + kMaxP;  // two slots of kMaxP int8 step scales
+    float* cheb = sig + 2 * kMaxP;
     // MIXED: wide panels run int8 steps (two int8 panels + the FP32
     // residual), narrow ones BF16 defect cycles (two BF16 panels).
     const bool wide_mixed = mixed && Pmax >= 32;
@@ -1256,7 +1318,8 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
         float* pemis = prm + 2 * cells;
         float* pdir = prm + 3 * cells;
         float* psky = prm + 4 * cells;
-        PanelParams pp{prho, ptau, pemis, pdir, psky, colmax};
+        PanelParams pp{prho, ptau, pemis, pdir, psky, colmax,
+                       mixed && P >= 32 ? cheb + 2 * kMaxP : nullptr};
         __nv_bfloat16* d0 = dbuf;
         __nv_bfloat16* d1 = dbuf ? dbuf + cells : nullptr;
         // Per-cell bytes: full sweep = state in + out + rho, tau, emission,
@@ -1334,17 +1397,17 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
             }
             cur = int(host_flag[1] & 1u);
         } else if (P >= 32) {
-            // FP32 sweep; then residual-tracked int8 steps until max|R| <=
-            // tol/8 max|X|; then the FP32 sweep again verifies max|dB| <=
-            // tol max|B| (and restarts the steps in the rare case it does
-            // not hold).  The int8 steps resolve a side only to about
-            // sigma/2 = max|R|/254 in absolute terms, where a Jacobi
-            // iterate's residual shrinks with the side's radiosity; dim
-            // sides get their accuracy back from brighter neighbours in the
-            // final FP32 sweep, and the steps run a factor 8 (about three
-            // steps) below the tolerance so that the per-side error stays
-            // well inside the 1e-4 bar on every workload measured.
-            const float step_tol = tol * 0.125f;
+            // FP32 sweep; then residual-tracked int8 steps until the
+            // per-side test holds on their exact residual R (R_s is the
+            // change the next Jacobi sweep would make to side s); then an
+            // FP32 sweep verifies the per-side test.  If it fails there and
+            // even the absolute test fails, the steps restart from the fresh
+            // residual; if only sides far below the column's maximum are
+            // still moving, plain FP32 sweeps finish them.  (The int8 steps
+            // resolve a side only to about sigma/2 = max|R|/254 absolute;
+            // every step shrinks sigma, so dim sides converge as the steps
+            // go on.)
+            const float step_tol = tol;
             float* X = reinterpret_cast<float*>(x0);
             float* Y = reinterpret_cast<float*>(x1);
             int8_t* qb[2] = {qbuf, qbuf + cells};
@@ -1354,7 +1417,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                     launch_sweep<float>(P, g, pp, X, Y, stats, counter, flag, s);
                 });
                 k_check<<<1, kMaxP, 0, s>>>(stats, flag, P, tol, it, counter, slot[0], slot[1],
-                                            nullptr, true, colmax);
+                                            nullptr, true, colmax, cheb, 1);
                 FCU_LAUNCH("k_check");
                 launches += 1;
                 ++it;
@@ -1416,7 +1479,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                         // max|R_new| / 127 for the step after next
                         k_check<<<1, kMaxP, 0, s>>>(stats, flag + 3, P, step_tol, it + k,
                                                     counter, slot[j & 1u], nullptr, nullptr,
-                                                    false, colmax);
+                                                    true, colmax, cheb, 2, slot[(j + 1) & 1u]);
                         FCU_LAUNCH("k_check");
                         ++launches;
                     }

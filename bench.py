@@ -509,12 +509,9 @@ def run_c3(args, rank, world, local):
 
     step_s, res, clocks = timed(fc.PRECISION_MIXED, args.steps, args.warmup)
     err = error()
+    # the same solve in plain FP32 to the same per-side rule (it meets the bar too)
     fp32_s, res32, _ = timed(fc.PRECISION_FP32, 1, 0)
     err32 = error()
-    # FP32 run to the MIXED steps' own target (an eighth of the tolerance),
-    # capped at 60 sweeps: the FP32 solve that meets the 1e-4 bar
-    fp32t_s, res32t, _ = timed(fc.PRECISION_FP32, 1, 0, tol=args.tolerance * 0.125, maxit=60)
-    err32t = error()
     rt = solve(fc.PRECISION_MIXED, fc.BATCH_TIME_SWEEPS)
     peaks = {}
     try:
@@ -541,12 +538,7 @@ def run_c3(args, rank, world, local):
         "iterations": res["iterations"], "residual_corrections": res["residual_corrections"],
         "batched_fp32": {"value": units / fp32_s, "ms_per_step": fp32_s * 1e3,
                          "iterations": res32["iterations"], "max_rel_err_vs_fp64": err32},
-        "batched_fp32_step_tol": {"value": units / fp32t_s, "ms_per_step": fp32t_s * 1e3,
-                                     "iterations": res32t["iterations"],
-                                     "converged": bool(res32t["converged"]),
-                                     "max_rel_err_vs_fp64": err32t},
         "speedup_vs_batched_fp32": fp32_s / step_s,
-        "speedup_vs_batched_fp32_meeting_the_bar": fp32t_s / step_s,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "kernel": "k_step_i8<128>",
                      "launches_timed": rt["timed_sweeps"],

@@ -161,6 +161,7 @@ __device__ bool trace_tiles(const float4* __restrict__ nodes, const float4* __re
 {
     best.t = FLT_MAX;
     best.facet = kSky;
+    if (tiles.n <= 1) return trace<kAny>(nodes, tri, leaves, o, d, skip, best);  // no copies
     bool ok = true;
     for (uint32_t t = 0; t < tiles.n; ++t) {
         const Vec ot = {o.x - tiles.x[t], o.y, o.z - tiles.z[t]};

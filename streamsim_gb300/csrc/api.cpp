@@ -879,6 +879,22 @@ void validate_batch(const facetcu_batch_config* cfg)
         throw Error(FACETCU_OVERFLOW_ERROR, "band_count x sun_count exceeds 2^31");
 }
 
+// The reference's optics checks (facetrt_vulkan.cpp solve), run on the
+// device over every band and side.
+void check_batch_inputs(facetcu_context* ctx, const float* rho, const float* tau,
+                        const float* emis, size_t n, const float* sky, const float* beam,
+                        uint32_t bands)
+{
+    const uint32_t bad = validate_inputs(rho, tau, emis, n, sky, beam, bands, ctx->scratch,
+                                         ctx->stream);
+    if (bad & 1u)
+        throw Error(FACETCU_INVALID_ARGUMENT,
+                    "Optical values must be finite, non-negative, and reflectance+transmittance<=1");
+    if (bad & 2u) throw Error(FACETCU_INVALID_ARGUMENT, "skyRadiosity must be finite and non-negative");
+    if (bad & 4u)
+        throw Error(FACETCU_INVALID_ARGUMENT, "beam irradiance must be finite and non-negative");
+}
+
 int run_batched(facetcu_context* ctx, const facetcu_batch_config* cfg, const float* rho,
                 const float* tau, const float* emis, const float* sky, const float* beam,
                 const float* dgeo, const float* initial, float* out, facetcu_batch_result* result)
@@ -968,6 +984,9 @@ int facetcu_solve_batched_device(facetcu_context* ctx, const facetcu_batch_confi
             throw Error(FACETCU_INVALID_ARGUMENT, "warm_start = GIVEN needs an initial radiosity");
         if (cfg->warm_start == FACETCU_WARM_MLP && !ctx->net.ready)
             throw Error(FACETCU_LOGIC_ERROR, "the MLP warm start needs trained parameters");
+        check_batch_inputs(ctx, reflectance, transmittance, emission,
+                           size_t(cfg->band_count) * ctx->graph.surfaces, sky, beam,
+                           cfg->band_count);
         return run_batched(ctx, cfg, reflectance, transmittance, emission, sky, beam,
                            direct_geometry, initial, radiosity, result);
     });
@@ -990,19 +1009,6 @@ int facetcu_solve_batched(facetcu_context* ctx, const facetcu_batch_config* cfg,
             throw Error(FACETCU_LOGIC_ERROR, "the MLP warm start needs trained parameters");
         const size_t S = ctx->graph.surfaces, B = cfg->band_count, K = cfg->sun_count;
         const size_t R = B * K;
-        for (size_t i = 0; i < B * S; ++i) {
-            const float r = reflectance[i], t = transmittance[i];
-            const float e = emission ? emission[i] : 0.0f;
-            if (!std::isfinite(r) || !std::isfinite(t) || !std::isfinite(e) || r < 0.0f ||
-                t < 0.0f || e < 0.0f || r + t > 1.0001f)
-                throw Error(FACETCU_INVALID_ARGUMENT,
-                            "Optical values must be finite, non-negative, and reflectance+transmittance<=1");
-        }
-        for (size_t b = 0; b < B; ++b) {
-            validate_sky(sky[b]);
-            if (!std::isfinite(beam[b]) || beam[b] < 0.0f)
-                throw Error(FACETCU_INVALID_ARGUMENT, "beam irradiance must be finite and non-negative");
-        }
         // one device block for all inputs: rho, tau, emis, dgeo, sky, beam, initial, out
         const size_t n_bs = B * S, n_ks = direct_geometry ? K * S : 0, n_rs = R * S;
         const size_t init_n = cfg->warm_start == FACETCU_WARM_GIVEN ? n_rs : 0;
@@ -1024,6 +1030,8 @@ int facetcu_solve_batched(facetcu_context* ctx, const facetcu_batch_config* cfg,
         FCU_CHECK(cudaMemcpyAsync(d_sky, sky, B * 4, cudaMemcpyHostToDevice, s));
         FCU_CHECK(cudaMemcpyAsync(d_beam, beam, B * 4, cudaMemcpyHostToDevice, s));
         if (init_n) FCU_CHECK(cudaMemcpyAsync(d_init, initial, init_n * 4, cudaMemcpyHostToDevice, s));
+        check_batch_inputs(ctx, d_rho, d_tau, emission ? d_emis : nullptr, n_bs, d_sky, d_beam,
+                           uint32_t(B));
         const int rc = run_batched(ctx, cfg, d_rho, d_tau, emission ? d_emis : nullptr, d_sky, d_beam,
                                    n_ks ? d_dgeo : nullptr, init_n ? d_init : nullptr, d_out, result);
         FCU_CHECK(cudaMemcpyAsync(radiosity, d_out, n_rs * 4, cudaMemcpyDeviceToHost, s));

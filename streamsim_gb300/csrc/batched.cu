@@ -1235,6 +1235,54 @@ void ensure_permuted(DeviceGraph& gr, const BatchProblem& p, Workspace& ws, cuda
 }  // namespace
 
 // Host driver.  Returns FACETCU_OK or FACETCU_NOT_CONVERGED.
+namespace {
+// Input checks of the batched solve on the device (the host loop over
+// bands x sides would cost more than the solve): bit 1 = an optical value
+// that is not finite, negative, or with reflectance + transmittance > 1;
+// bit 2 = a sky value not finite or negative; bit 4 = the same for beam.
+__global__ void k_validate_inputs(const float* __restrict__ rho, const float* __restrict__ tau,
+                                  const float* __restrict__ emis, size_t n,
+                                  const float* __restrict__ sky, const float* __restrict__ beam,
+                                  uint32_t bands, uint32_t* flags)
+{
+    uint32_t f = 0;
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    const size_t first = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (size_t i = first; i < n; i += stride) {
+        const float r = rho[i], t = tau[i], e = emis ? emis[i] : 0.0f;
+        if (!isfinite(r) || !isfinite(t) || !isfinite(e) || r < 0.0f || t < 0.0f || e < 0.0f ||
+            r + t > 1.0001f)
+            f |= 1u;
+    }
+    if (first < bands) {
+        const float k = sky[first], b = beam[first];
+        if (!isfinite(k) || k < 0.0f) f |= 2u;
+        if (!isfinite(b) || b < 0.0f) f |= 4u;
+    }
+    f = __reduce_or_sync(0xffffffffu, f);
+    if ((threadIdx.x & 31) == 0 && f) atomicOr(flags, f);
+}
+}  // namespace
+
+uint32_t validate_inputs(const float* rho, const float* tau, const float* emis, size_t n,
+                         const float* sky, const float* beam, uint32_t bands, DeviceBuffer& scratch,
+                         cudaStream_t s)
+{
+    uint32_t* d = static_cast<uint32_t*>(scratch.reserve(64));
+    FCU_CHECK(cudaMemsetAsync(d, 0, 4, s));
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t need = std::max<size_t>((n + 255) / 256, (bands + 255) / 256);
+    const unsigned grid = unsigned(std::max<size_t>(1, std::min<size_t>(need, size_t(sms) * 8)));
+    k_validate_inputs<<<grid, 256, 0, s>>>(rho, tau, emis, n, sky, beam, bands, d);
+    FCU_LAUNCH("k_validate_inputs");
+    uint32_t h = 0;
+    FCU_CHECK(cudaMemcpyAsync(&h, d, 4, cudaMemcpyDeviceToHost, s));
+    FCU_CHECK(cudaStreamSynchronize(s));
+    return h;
+}
+
 void release_graphs(BatchState& st)
 {
     if (st.step_graph) cudaGraphExecDestroy(st.step_graph);

@@ -199,6 +199,11 @@ struct BatchState {
     alignas(8) unsigned char step_graph_key[256] = {};
 };
 void release_graphs(BatchState& st);
+// Device-side checks of the batched solve's inputs; returns the error bits
+// (1 optics, 2 sky, 4 beam).
+uint32_t validate_inputs(const float* rho, const float* tau, const float* emis, size_t n,
+                         const float* sky, const float* beam, uint32_t bands, DeviceBuffer& scratch,
+                         cudaStream_t s);
 int batched_solve(const DeviceGraph& g, const BatchProblem& p, const facetcu_batch_config& cfg,
                   const float* d_initial, float* d_out, BatchState& st, Workspace& ws,
                   cudaStream_t s, facetcu_batch_result* result);

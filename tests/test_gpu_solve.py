@@ -222,3 +222,38 @@ def test_scene_batch_matches_scenes_solved_alone():
     assert res["converged"] and rel_err(out, truth) < 1e-4
     for m in models + [batch]:
         m.close()
+
+
+def test_batched_input_checks_on_host_and_device_paths(c1):
+    """The optics, sky and beam checks of the batched solve (the reference's
+    solve-time validation) run on the device for both entry points: a NaN,
+    a negative value or rho + tau > 1 anywhere in bands x sides, a negative
+    sky or beam, each raise the reference's message; valid inputs still
+    solve afterwards."""
+    torch = pytest.importorskip("torch")
+    sc = c1["scene"]
+    m = c1["model"]
+    rho, tau, dgeo, sky, beam = _bands(sc, c1["lit"], c1["sun"], 8)
+    cases = []
+    r = rho.copy(); r[5, 123] = np.nan; cases.append((r, tau, sky, beam, "Optical values"))
+    t = tau.copy(); t[7, -1] = -0.1; cases.append((rho, t, sky, beam, "Optical values"))
+    r = rho.copy(); r[2, 77] = 0.9; t = tau.copy(); t[2, 77] = 0.2
+    cases.append((r, t, sky, beam, "Optical values"))
+    k = sky.copy(); k[3] = -1.0; cases.append((rho, tau, k, beam, "skyRadiosity"))
+    b = beam.copy(); b[6] = np.inf; cases.append((rho, tau, sky, b, "beam irradiance"))
+    dev = torch.device("cuda")
+    S = sc.surface_count
+    out = torch.empty((8, S), dtype=torch.float32, device=dev)
+    for r, t, k, b, msg in cases:
+        with pytest.raises(ValueError, match=msg):
+            m.solveBatched(r, t, k, b, dgeo)
+        d = {n: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+             for n, v in (("r", r), ("t", t), ("k", k), ("b", b), ("g", dgeo))}
+        torch.cuda.synchronize()
+        cfg = facetcu.BatchConfig(8, 1, facetcu.PRECISION_MIXED, facetcu.WARM_NONE, 200, 1e-5, 0, 0)
+        with pytest.raises(ValueError, match=msg):
+            m.solveBatchedDevice(cfg, d["r"].data_ptr(), d["t"].data_ptr(), None,
+                                 d["k"].data_ptr(), d["b"].data_ptr(), d["g"].data_ptr(), None,
+                                 out.data_ptr())
+    ok, res = m.solveBatched(rho, tau, sky, beam, dgeo, tolerance=1e-5)
+    assert res["converged"] and np.all(np.isfinite(ok))

@@ -9,6 +9,9 @@
 #include <algorithm>
 #include <array>
 #include <chrono>
+#include <fstream>
+#include <map>
+#include <sstream>
 #include <cmath>
 #include <cstdio>
 #include <limits>
@@ -54,6 +57,8 @@ struct facetcu_context {
     DeviceBuffer samples_uv, samples_dir, fraction;
     spectral::Tables spec;
     DeviceBuffer spec_io;
+    std::map<std::string, uint32_t> tuned;  // autotuned panel widths by problem key
+    std::string gpu_name;                   // for the autotuner's key
 };
 
 namespace {
@@ -895,10 +900,30 @@ void check_batch_inputs(facetcu_context* ctx, const float* rho, const float* tau
         throw Error(FACETCU_INVALID_ARGUMENT, "beam irradiance must be finite and non-negative");
 }
 
-int run_batched(facetcu_context* ctx, const facetcu_batch_config* cfg, const float* rho,
+// The autotuner's key: GPU, graph size, columns, precision.
+std::string tune_key(facetcu_context* ctx, const facetcu_batch_config* cfg)
+{
+    if (ctx->gpu_name.empty()) {
+        cudaDeviceProp prop{};
+        FCU_CHECK(cudaGetDeviceProperties(&prop, ctx->device));
+        ctx->gpu_name = prop.name;
+    }
+    std::ostringstream k;
+    k << ctx->gpu_name << "|S=" << ctx->graph.surfaces << "|nnz=" << ctx->graph.nnz
+      << "|R=" << uint64_t(cfg->band_count) * cfg->sun_count << "|precision=" << cfg->precision;
+    return k.str();
+}
+
+int run_batched(facetcu_context* ctx, const facetcu_batch_config* cfg_in, const float* rho,
                 const float* tau, const float* emis, const float* sky, const float* beam,
                 const float* dgeo, const float* initial, float* out, facetcu_batch_result* result)
 {
+    facetcu_batch_config tuned_cfg = *cfg_in;
+    if (tuned_cfg.panel_width == 0 && !ctx->tuned.empty()) {
+        const auto it = ctx->tuned.find(tune_key(ctx, cfg_in));
+        if (it != ctx->tuned.end()) tuned_cfg.panel_width = it->second;
+    }
+    const facetcu_batch_config* cfg = &tuned_cfg;
     BatchProblem p{};
     p.vertices = ctx->vertices.as<facetcu_vertex>();
     for (int a = 0; a < 3; ++a) {
@@ -1471,6 +1496,94 @@ int facetcu_scene_batch(facetcu_context* ctx, facetcu_context* const* scenes,
             diagnostics->directed_edge_count = uint32_t(nnz);
             diagnostics->max_closure_error = closure;
         }
+        return FACETCU_OK;
+    });
+}
+
+// ---- autotuning ------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+// JSON-lines cache: {"key": "...", "panel_width": N} per line.
+void read_tune_cache(const char* path, std::map<std::string, uint32_t>& out)
+{
+    std::ifstream in(path);
+    std::string line;
+    while (std::getline(in, line)) {
+        const size_t k0 = line.find("\"key\": \"");
+        const size_t p0 = line.find("\"panel_width\": ");
+        if (k0 == std::string::npos || p0 == std::string::npos) continue;
+        const size_t ks = k0 + 8, ke = line.find('"', ks);
+        if (ke == std::string::npos) continue;
+        out[line.substr(ks, ke - ks)] = uint32_t(std::strtoul(line.c_str() + p0 + 15, nullptr, 10));
+    }
+}
+
+void write_tune_cache(const char* path, const std::map<std::string, uint32_t>& m)
+{
+    const std::string tmp = std::string(path) + ".tmp";
+    {
+        std::ofstream out(tmp);
+        if (!out) throw Error(FACETCU_RUNTIME_ERROR, std::string("cannot write ") + tmp);
+        for (const auto& kv : m)
+            out << "{\"key\": \"" << kv.first << "\", \"panel_width\": " << kv.second << "}\n";
+    }
+    if (std::rename(tmp.c_str(), path) != 0)
+        throw Error(FACETCU_RUNTIME_ERROR, std::string("cannot replace ") + path);
+}
+
+}  // namespace
+
+extern "C" {
+
+int facetcu_autotune_batched(facetcu_context* ctx, const facetcu_batch_config* config,
+                             const float* reflectance, const float* transmittance,
+                             const float* emission, const float* sky, const float* beam,
+                             const float* direct_geometry, float* radiosity,
+                             const char* cache_path, uint32_t* panel_width)
+{
+    return guarded(ctx, [&] {
+        require_graph(ctx, "autotuneBatched()");
+        validate_batch(config);
+        if (!reflectance || !transmittance || !sky || !beam || !radiosity || !panel_width)
+            throw Error(FACETCU_INVALID_ARGUMENT,
+                        "reflectance, transmittance, sky, beam, output and panel_width are required");
+        const std::string key = tune_key(ctx, config);
+        if (cache_path) read_tune_cache(cache_path, ctx->tuned);
+        auto hit = ctx->tuned.find(key);
+        if (hit != ctx->tuned.end()) {
+            *panel_width = hit->second;
+            return FACETCU_OK;
+        }
+        check_batch_inputs(ctx, reflectance, transmittance, emission,
+                           size_t(config->band_count) * ctx->graph.surfaces, sky, beam,
+                           config->band_count);
+        const uint64_t R = uint64_t(config->band_count) * config->sun_count;
+        const uint32_t cap = config->precision == FACETCU_PRECISION_FP64 ? 32u : 128u;
+        uint32_t best = 0;
+        double best_t = 0.0;
+        for (uint32_t P = 32; P <= cap; P *= 2) {
+            if (P > R && P != 32) break;  // wider than the columns: only padding
+            facetcu_batch_config c = *config;
+            c.panel_width = P;
+            c.warm_start = FACETCU_WARM_NONE;
+            c.maximum_iterations = 6;  // a few sweeps of every panel
+            c.tolerance = 0.0f;
+            c.flags = 0;
+            facetcu_batch_result r{};
+            run_batched(ctx, &c, reflectance, transmittance, emission, sky, beam,
+                        direct_geometry, nullptr, radiosity, &r);  // warms the graph copies
+            run_batched(ctx, &c, reflectance, transmittance, emission, sky, beam,
+                        direct_geometry, nullptr, radiosity, &r);
+            if (best == 0 || r.seconds < best_t) {
+                best = P;
+                best_t = r.seconds;
+            }
+        }
+        ctx->tuned[key] = best;
+        if (cache_path) write_tune_cache(cache_path, ctx->tuned);
+        *panel_width = best;
         return FACETCU_OK;
     });
 }

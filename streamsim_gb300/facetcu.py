@@ -200,6 +200,8 @@ SIGNATURES.update({
     "facetcu_solve_bands": (C.c_int, [_ctx, C.POINTER(SpectralParameters), _vp,
                                       C.POINTER(Direction), _vp, _vp, C.POINTER(BandResult)]),
 })
+SIGNATURES["facetcu_autotune_batched"] = (C.c_int, [_ctx, C.POINTER(BatchConfig)] + [_vp] * 7 +
+                                          [C.c_char_p, C.POINTER(_u32)])
 SIGNATURES["facetcu_scene_batch"] = (C.c_int, [_ctx, _vp, _u32, _vp, C.POINTER(GraphDiagnostics)])
 OPTIONAL_SIGNATURES = {}
 MLP_INPUTS = 12
@@ -670,6 +672,16 @@ class FacetrtCuda:
         self._check(self.lib.facetcu_mlp_samples_device(
             self.h, C.byref(cfg), rho_ptr, tau_ptr, emis_ptr, sky_ptr, beam_ptr, dgeo_ptr,
             converged_ptr, features_ptr, targets_ptr))
+
+    def autotuneBatched(self, cfg, rho_ptr, tau_ptr, emis_ptr, sky_ptr, beam_ptr, dgeo_ptr,
+                        out_ptr, cache_path=None):
+        """Time the panel widths on short solves of these device inputs and keep
+        the fastest for later solves with panel_width = 0; returns it."""
+        p = C.c_uint32()
+        self._check(self.lib.facetcu_autotune_batched(
+            self.h, C.byref(cfg), rho_ptr, tau_ptr, emis_ptr, sky_ptr, beam_ptr, dgeo_ptr, out_ptr,
+            os.fsencode(cache_path) if cache_path else None, C.byref(p)))
+        return p.value
 
     def solveBatchedDevice(self, cfg, rho_ptr, tau_ptr, emis_ptr, sky_ptr, beam_ptr, dgeo_ptr,
                            init_ptr, out_ptr):

@@ -257,3 +257,44 @@ def test_batched_input_checks_on_host_and_device_paths(c1):
                                  out.data_ptr())
     ok, res = m.solveBatched(rho, tau, sky, beam, dgeo, tolerance=1e-5)
     assert res["converged"] and np.all(np.isfinite(ok))
+
+
+def test_autotune_panel_width_and_cache(c1, tmp_path):
+    """facetcu_autotune_batched times the panel widths on short solves, keeps
+    the fastest (one of 32/64/128 not wider than the columns), writes it to
+    the JSON-lines cache, and later solves with panel_width = 0 use it: the
+    same bits as a solve with that width given explicitly, also in a fresh
+    context that only reads the cache."""
+    torch = pytest.importorskip("torch")
+    sc = c1["scene"]
+    m = c1["model"]
+    rho, tau, _, sky, beam = _bands(sc, c1["lit"], c1["sun"], 32)
+    dgeo = np.stack([scenes.direct_geometry(sc, c1["lit"], scenes.sun_direction(z, 135))
+                     for z in (20, 40, 60)])
+    dev = torch.device("cuda")
+    d = {n: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+         for n, v in (("r", rho), ("t", tau), ("k", sky), ("b", beam), ("g", dgeo))}
+    out = torch.empty((96, sc.surface_count), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    ptrs = (d["r"].data_ptr(), d["t"].data_ptr(), None, d["k"].data_ptr(), d["b"].data_ptr(),
+            d["g"].data_ptr())
+    cache = tmp_path / "tune.jsonl"
+    cfg = facetcu.BatchConfig(32, 3, facetcu.PRECISION_MIXED, facetcu.WARM_NONE, 500, 1e-5, 0, 0)
+    best = m.autotuneBatched(cfg, *ptrs, out.data_ptr(), str(cache))
+    assert best in (32, 64)  # 96 columns: 128 would only pad
+    text = cache.read_text()
+    assert f'"panel_width": {best}' in text and "|R=96|precision=1" in text
+
+    def solve(model, width):
+        c = facetcu.BatchConfig(32, 3, facetcu.PRECISION_MIXED, facetcu.WARM_NONE, 500, 1e-5,
+                                width, 0)
+        model.solveBatchedDevice(c, *ptrs, out.data_ptr())
+        return out.cpu().numpy()
+
+    tuned = solve(m, 0)
+    assert np.array_equal(tuned, solve(m, best))
+    fresh = model_for(sc.vertices, 512, 64)
+    fresh.setGraph(*m.graph())
+    assert fresh.autotuneBatched(cfg, *ptrs, out.data_ptr(), str(cache)) == best  # from the cache
+    assert np.array_equal(solve(fresh, 0), tuned)
+    fresh.close()

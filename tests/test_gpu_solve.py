@@ -288,7 +288,7 @@ def test_autotune_panel_width_and_cache(c1, tmp_path):
     def solve(model, width):
         c = facetcu.BatchConfig(32, 3, facetcu.PRECISION_MIXED, facetcu.WARM_NONE, 500, 1e-5,
                                 width, 0)
-        model.solveBatchedDevice(c, *ptrs, out.data_ptr())
+        model.solveBatchedDevice(c, *ptrs, None, out.data_ptr())
         return out.cpu().numpy()
 
     tuned = solve(m, 0)

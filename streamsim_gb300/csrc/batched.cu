@@ -468,15 +468,39 @@ __device__ __forceinline__ void edge_word_i(const uint32_t* __restrict__ packed,
     }
 }
 
-// Sign-extended byte k of w (PTX prmt with the sign-replicate selector bit).
-template <int k>
-__device__ __forceinline__ int sbyte(uint32_t w)
+// sum over 4 of signed byte a_i x unsigned byte b_i, plus c (PTX dp4a).
+__device__ __forceinline__ int dp4a_su(uint32_t a, uint32_t b, int c)
 {
-    constexpr uint32_t sel = uint32_t(k) | ((uint32_t(k) | 8u) << 4) | ((uint32_t(k) | 8u) << 8) |
-                             ((uint32_t(k) | 8u) << 12);
+    int d;
+    asm("dp4a.s32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)
+{
     uint32_t d;
-    asm("prmt.b32 %0, %1, 0, %2;" : "=r"(d) : "r"(w), "n"(sel));
-    return int(d);
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(sel));
+    return d;
+}
+
+// Bytes (shift .. shift+7) of four counts as one word, edge i in byte i.
+__device__ __forceinline__ uint32_t pack_bytes(int c0, int c1, int c2, int c3, int shift)
+{
+    return (uint32_t(c0 >> shift) & 255u) | ((uint32_t(c1 >> shift) & 255u) << 8) |
+           ((uint32_t(c2 >> shift) & 255u) << 16) | ((uint32_t(c3 >> shift) & 255u) << 24);
+}
+
+// 4 x 4 byte transpose: a, b, c, d are four edges' words (byte k = column
+// k); t[k] gets column k of the four edges (byte i = edge i).
+__device__ __forceinline__ void transpose4(uint32_t a, uint32_t b, uint32_t c, uint32_t d,
+                                           uint32_t* t)
+{
+    const uint32_t ab_lo = prmt(a, b, 0x5140u), ab_hi = prmt(a, b, 0x7362u);
+    const uint32_t cd_lo = prmt(c, d, 0x5140u), cd_hi = prmt(c, d, 0x7362u);
+    t[0] = prmt(ab_lo, cd_lo, 0x5410u);
+    t[1] = prmt(ab_lo, cd_lo, 0x7632u);
+    t[2] = prmt(ab_hi, cd_hi, 0x5410u);
+    t[3] = prmt(ab_hi, cd_hi, 0x7632u);
 }
 
 // acc[0..16) += sum over edges of side s of count * Q[n][sub * 16 + k]; the
@@ -495,6 +519,7 @@ __device__ __forceinline__ void gather_i8(const uint32_t* __restrict__ rows,
     constexpr int W = G >= 4 ? G / 4 : 1;  // packed words per lane per round
     constexpr int E = 32 * W;              // edges per round
     constexpr int U = E / G;               // loads per lane per round
+    static_assert(U % 4 == 0, "edges are accumulated four at a time");
     const int grp = lane / L, sub = lane % L;
     const uint4* __restrict__ Q16 = reinterpret_cast<const uint4*>(Q);
     const uint32_t start = __ldg(rows + s), end = __ldg(rows + s + 1);
@@ -533,15 +558,36 @@ __device__ __forceinline__ void gather_i8(const uint32_t* __restrict__ rows,
                 c[u] = 0;
             }
         }
+        // Four edges at a time: transpose their 4 x 4 byte blocks so that
+        // one register holds one column's four values, then one dp4a adds
+        // value x count for all four (counts packed as unsigned bytes).  A
+        // packed word's count is below 2^(32 - nb_bits) <= 2^10; the rare
+        // counts above 255 (and any 32-bit count of an unpacked graph) add
+        // their higher bytes in further warp-uniform passes, which keeps the
+        // sums equal to the 32-bit products.
+        uint32_t cor = 0u;
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const uint32_t wd[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
+        for (int u = 0; u < U; ++u) cor |= uint32_t(c[u]);
+        const uint32_t call = __reduce_or_sync(0xffffffffu, cor);
+#pragma unroll
+        for (int h = 0; h < U; h += 4) {
+            const uint32_t lo = pack_bytes(c[h], c[h + 1], c[h + 2], c[h + 3], 0);
+            const uint32_t e0[4] = {q[h].x, q[h].y, q[h].z, q[h].w};
+            const uint32_t e1[4] = {q[h + 1].x, q[h + 1].y, q[h + 1].z, q[h + 1].w};
+            const uint32_t e2[4] = {q[h + 2].x, q[h + 2].y, q[h + 2].z, q[h + 2].w};
+            const uint32_t e3[4] = {q[h + 3].x, q[h + 3].y, q[h + 3].z, q[h + 3].w};
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                acc[4 * i + 0] += c[u] * sbyte<0>(wd[i]);
-                acc[4 * i + 1] += c[u] * sbyte<1>(wd[i]);
-                acc[4 * i + 2] += c[u] * sbyte<2>(wd[i]);
-                acc[4 * i + 3] += c[u] * sbyte<3>(wd[i]);
+                uint32_t t[4];
+                transpose4(e0[i], e1[i], e2[i], e3[i], t);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) acc[4 * i + k] = dp4a_su(t[k], lo, acc[4 * i + k]);
+                for (int sh = 8; sh < 32 && (call >> sh) != 0u; sh += 8) {
+                    const uint32_t cb = pack_bytes(c[h], c[h + 1], c[h + 2], c[h + 3], sh);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        acc[4 * i + k] += int(uint32_t(dp4a_su(t[k], cb, 0)) << sh);
+                }
             }
         }
     }

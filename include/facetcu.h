@@ -455,6 +455,142 @@ int facetcu_solve_bands(facetcu_context *ctx, const facetcu_spectral_parameters 
                         const float *sunlit, const facetcu_direction *sun, float *band_radiosity,
                         float *light_enhancement, facetcu_band_result *result);
 
+/* ---- FacetEB: the coupled radiation / energy-balance node ---------------- */
+/* The shortwave spectrum of a FacetEB run (ShortwaveSpectrum and
+ * loadShortwaveSpectrum, facetrtcore.cpp:2458-2541): direct and diffuse
+ * samples per 1 nm from 400 nm, per micrometre.  Fewer than 2 samples (or
+ * a non-positive integral) select the reference's flat fallback of 2001
+ * samples, 0.5 * direct_fraction and 0.5 * (1 - direct_fraction); otherwise
+ * both are scaled so that their summed trapezoid integral is one. */
+typedef struct {
+    const float *direct;
+    const float *diffuse;
+    uint32_t sample_count;   /* min of the two lengths */
+    float direct_fraction;   /* directScatteringRatio, clamped to [0, 1] */
+    uint32_t window_width;   /* spectralAccelerationWidth, samples per window (1..1000) */
+} facetcu_shortwave_spectrum;
+/* One spectral-acceleration window (runFacetEBCore :3499-3536): solved with
+ * the optics of sample `energy_band` (the window centre). */
+typedef struct {
+    float direct_normal; /* W m^-2 of the window's direct beam, normal to the sun */
+    float diffuse;       /* W m^-2 of the window's sky radiosity */
+    uint32_t energy_band;
+} facetcu_shortwave_window;
+/* The windows of one node (total_shortwave W m^-2 on the horizontal,
+ * cos_zenith = max(0, sun.y)), skipping windows with no energy as the
+ * reference does, and for each of band_count wavelengths the spectral
+ * direct and diffuse irradiance total_shortwave * spectrum(lambda) * 0.001
+ * (band_direct / band_diffuse may be NULL).  Host only; *window_count is
+ * set even when capacity is too small (then FACETCU_OVERFLOW_ERROR). */
+int facetcu_shortwave_windows(const facetcu_shortwave_spectrum *spectrum, float total_shortwave,
+                              float cos_zenith, const float *wavelengths, uint32_t band_count,
+                              facetcu_shortwave_window *windows, uint32_t capacity,
+                              uint32_t *window_count, float *band_direct, float *band_diffuse);
+
+/* The energy-balance fields of SurfaceParameters (facetrtcore.cpp:113-138);
+ * facetcu_energy_surface_defaults() fills the reference's defaults. */
+typedef struct {
+    facetcu_surface_parameters optics;     /* band values, TIR reflectance/transmittance */
+    const float *energy_reflectance;       /* per shortwave sample; empty: the Planck(5778 K)- */
+    uint32_t energy_reflectance_count;     /*   weighted mean of optics.reflectance */
+    const float *energy_transmittance;
+    uint32_t energy_transmittance_count;
+    float surface_resistance;      /* s m^-1 */
+    float specific_heat;           /* J kg^-1 K^-1 */
+    float density;                 /* kg m^-3 */
+    float thermal_conductivity;    /* W m^-1 K^-1 */
+    float soil_moisture;           /* below 0.03: dry soil, no latent heat */
+    float heat_capacity_per_area;  /* J m^-2 K^-1 of object facets */
+    int32_t soil_temperature_method; /* 0: storage = 0.35 Rn; 1: force-restore; 2: 1.5 x force-restore */
+    uint32_t photovoltaic;
+    uint32_t vegetation;
+    float pv_eta25, pv_gamma, pv_bifaciality;
+    float convective_scale;
+} facetcu_energy_surface;
+void facetcu_energy_surface_defaults(facetcu_energy_surface *surface);
+
+/* runFacetEBCore's settings (facetrtcore.cpp:3196-3233) and scene fields.
+ * Facets without a material take the reference's fixed fallbacks
+ * (surfaceForFacet :607-620): SurfaceParameters{} for objects, reflectance
+ * 0.20 / transmittance 0 / TIR 0.05 for the ground. */
+typedef struct {
+    const facetcu_energy_surface *materials; /* Scene::materials */
+    uint32_t material_count;
+    const uint32_t *material_indices; /* per facet, or NULL */
+    const float *texture_factors;     /* per facet reflectance factor, or NULL (1) */
+    uint32_t leaf_facet_count;
+    float background_angular_strength;
+    const float *wavelengths;         /* sensor bands of the node output, may be 0 */
+    uint32_t band_count;
+    float sky_temperature;            /* K, clamped by the caller to [150, 350] */
+    float time_step;                  /* dTime, s (>= 1) */
+    uint32_t coupling_iterations;     /* 1..100 */
+    float temperature_tolerance;      /* K */
+    float temperature_relaxation;     /* 0.05..1 */
+    int32_t vegetation_temperature_method; /* 0 Ball-Berry, 1 Farquhar */
+    uint32_t solver_iterations;       /* Jacobi sweeps per solve: 64 = kIterations */
+    float solver_tolerance;           /* 0: every solve runs solver_iterations sweeps from
+                                         zero, as the reference; > 0: stop on the per-side
+                                         rule and start each longwave solve from the last */
+    uint32_t precision;               /* FACETCU_PRECISION_FP32 or _MIXED (needs solver_tolerance > 0) */
+} facetcu_energy_parameters;
+/* One meteorological row (MeteoStep :3172-3181). */
+typedef struct {
+    float air_temperature;   /* deg C */
+    float vapor_pressure;    /* hPa */
+    float pressure;          /* hPa */
+    float wind_speed;        /* m s^-1 */
+    float shortwave;         /* W m^-2 */
+    float longwave;          /* W m^-2; <= 0: sigma T_sky^4 */
+} facetcu_meteo;
+/* Per-side fields of a node (host arrays of 2F floats; NULL = not wanted,
+ * except temperature). */
+typedef struct {
+    float *temperature;        /* in: the state at the node start; out: the solved state */
+    float *radiosity;          /* shortwave + final longwave (combineRadiativeSolutions) */
+    float *shortwave_radiosity;
+    float *diffuse_radiosity;  /* shortwave without direct light */
+    float *longwave_radiosity;
+    float *absorbed_shortwave;
+    float *incident_shortwave;
+    float *net_radiation;
+    float *sensible_heat;
+    float *latent_heat;
+    float *storage_heat;
+    float *photovoltaic_power;
+    float *band_output;        /* [band_count][2F]: apparent reflectance (optical), radiance */
+} facetcu_energy_fields;
+typedef struct {
+    uint32_t coupling_iterations;
+    uint32_t converged;
+    float max_temperature_delta;           /* K */
+    float max_energy_residual;             /* W m^-2 */
+    float max_energy_residual_equivalent;  /* K */
+    uint32_t shortwave_sweeps;             /* of the window solve */
+    uint32_t longwave_sweeps;              /* summed over the coupling solves */
+    uint32_t band_sweeps;
+    uint32_t solves;                       /* radiosity solves the reference would run */
+    double seconds;
+} facetcu_energy_result;
+/* One FacetEB time node (runFacetEBCore :3462-3908) on the context's graph:
+ * every shortwave window solved with and without its direct beam as one
+ * batched solve, incident and absorbed shortwave accumulated in window order,
+ * then up to coupling_iterations rounds of longwave optics from the
+ * temperatures, a longwave solve, incident longwave, the per-facet energy
+ * fluxes (net radiation, sensible, latent, storage, PV), the residual and
+ * the relaxed Newton temperature update, all on the device; a final
+ * longwave solve and flux evaluation; and the sensor bands (spectral optics
+ * of the solved state, one batched solve, apparent reflectance).  sunlit is
+ * the node's sun raster (2F floats), sun its direction.  Returns
+ * FACETCU_RUNTIME_ERROR "FacetEB energy residual is not finite" as the
+ * reference throws. */
+int facetcu_faceteb_node(facetcu_context *ctx, const facetcu_energy_parameters *parameters,
+                         const facetcu_meteo *meteo, const facetcu_direction *sun,
+                         const float *sunlit, const facetcu_shortwave_window *windows,
+                         uint32_t window_count, const float *band_direct,
+                         const float *band_diffuse, facetcu_energy_fields *fields,
+                         facetcu_energy_result *result);
+
 #ifdef __cplusplus
 }
 #endif

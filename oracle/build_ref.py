@@ -15,7 +15,9 @@ appends the extern "C" wrappers of oracle/ref_shim.inc:
                                  GraphDiagnostics, SolveResult
     facetrtcore.cpp    39-53     Clock/Vec3 aliases
     facetrtcore.cpp    74-630    constants, Scene, geometry, optics helpers
-    facetrtcore.cpp    703-1620  CpuRasterizer .. runCpu
+    facetrtcore.cpp    703-1620  CpuRasterizer .. runCpu (with the FacetEB
+                                 helpers: latent heat, storage, energy optics)
+    facetrtcore.cpp    2458-2497 ShortwaveSpectrum (FacetEB's window integrals)
 
 Everything generated goes to oracle/_ref/ (git-ignored).  The generated
 source travels with the repository snapshot, so on a machine without the
@@ -39,7 +41,8 @@ RANGES = [
     ("facetrt_vulkan.h", 15, 62, "namespace facetvk {", "}"),
     ("facetrtcore.cpp", 39, 53, "namespace {", None),
     ("facetrtcore.cpp", 74, 630, None, None),
-    ("facetrtcore.cpp", 703, 1620, None, "}  // namespace"),
+    ("facetrtcore.cpp", 703, 1620, None, None),
+    ("facetrtcore.cpp", 2458, 2497, None, "}  // namespace"),
 ]
 # (file, line, text the line must start with) — guards against a different
 # revision of the reference.
@@ -55,6 +58,8 @@ ANCHORS = [
     ("facetrtcore.cpp", 1585, "RunResult runCpu("),
     ("facetrtcore.cpp", 1621, "RunResult runGpu("),
     ("facetrtcore.cpp", 631, "std::shared_ptr<const ReflectanceVarianceTexture> loadReflectanceVarianceTexture("),
+    ("facetrtcore.cpp", 2458, "struct ShortwaveSpectrum {"),
+    ("facetrtcore.cpp", 2497, "};"),
 ]
 PRELUDE = """// GENERATED by oracle/build_ref.py from the reference tree. Not product
 // code and not committed: test infrastructure for parity checks only.

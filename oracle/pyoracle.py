@@ -343,8 +343,111 @@ class Reference:
                                                 C.c_uint32, C.c_float, C.c_float, C.c_void_p,
                                                 C.c_float, C.c_float, C.c_uint32, C.c_void_p])
 
+        L.ref_shortwave_windows.restype = C.c_uint32
+        L.ref_shortwave_windows.argtypes = ([C.c_void_p, C.c_void_p, C.c_uint32, C.c_float,
+                                             C.c_uint32, C.c_float, C.c_float, C.c_void_p,
+                                             C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                                             C.c_void_p])
+        L.ref_faceteb_node.restype = C.c_int
+        L.ref_faceteb_node.argtypes = ([C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_uint32, C.c_float, C.c_float,
+                                        C.c_float] + [C.c_void_p] * 5 +
+                                       [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_uint32] + [C.c_void_p] * 4)
+
     def error(self):
         return self.lib.ref_last_error().decode()
+
+    def shortwave_windows(self, total, cosz, direct=None, diffuse=None, direct_fraction=0.8,
+                          width=100, wavelengths=()):
+        """The windows of runFacetEBCore (facetrtcore.cpp:3485-3536) and the
+        per-band spectral irradiances, through the reference's
+        ShortwaveSpectrum: (windows (n, 3), band_direct, band_diffuse)."""
+        d = None if direct is None else np.ascontiguousarray(direct, np.float32)
+        f = None if diffuse is None else np.ascontiguousarray(diffuse, np.float32)
+        n = 0 if d is None or f is None else min(d.size, f.size)
+        wl = np.ascontiguousarray(wavelengths, np.float32)
+        cap = 4096
+        win = np.zeros((cap, 3), np.float32)
+        bd = np.zeros(max(wl.size, 1), np.float32)
+        bf = np.zeros(max(wl.size, 1), np.float32)
+        k = self.lib.ref_shortwave_windows(
+            None if d is None else d.ctypes.data, None if f is None else f.ctypes.data, n,
+            direct_fraction, width, total, cosz, wl.ctypes.data if wl.size else None, wl.size,
+            win.ctypes.data, cap, bd.ctypes.data, bf.ctypes.data)
+        return win[:k].astype(np.float64), bd[:wl.size], bf[:wl.size]
+
+    @staticmethod
+    def _pack_energy_surface(m):
+        head = [len(m.reflectance), len(m.transmittance), len(m.energy_reflectance),
+                len(m.energy_transmittance), m.tir_reflectance, m.tir_transmittance,
+                m.sunlit_temperature, m.shaded_temperature, m.surface_resistance,
+                m.specific_heat, m.density, m.thermal_conductivity, m.soil_moisture,
+                m.heat_capacity_per_area, m.soil_temperature_method, float(bool(m.photovoltaic)),
+                float(bool(m.vegetation)), m.pv_eta25, m.pv_gamma, m.pv_bifaciality,
+                m.convective_scale]
+        return np.concatenate([np.asarray(head, np.float32),
+                               np.asarray(m.reflectance, np.float32).ravel(),
+                               np.asarray(m.transmittance, np.float32).ravel(),
+                               np.asarray(m.energy_reflectance, np.float32).ravel(),
+                               np.asarray(m.energy_transmittance, np.float32).ravel()])
+
+    ENERGY_FIELDS = ("radiosity", "shortwave_radiosity", "diffuse_radiosity",
+                     "longwave_radiosity", "absorbed_shortwave", "incident_shortwave",
+                     "net_radiation", "sensible_heat", "latent_heat", "storage_heat",
+                     "photovoltaic_power")
+
+    def faceteb_node(self, vertices, leaf_count, graph, sunlit, zenith, azimuth, meteo,
+                     temperature, materials=(), material_indices=None, texture_factors=None,
+                     strength=0.0, spectrum=None, direct_fraction=0.8, width=100, time_step=1800.0,
+                     coupling_iterations=20, tolerance=0.05, relaxation=0.5, vegetation_method=0,
+                     sky_temperature=250.0, wavelengths=()):
+        """One FacetEB node (runFacetEBCore, facetrtcore.cpp:3462-3908) on the
+        reference's CPU functions.  graph = (rows, edges (nnz, 2), denom,
+        sky); meteo = (air C, vapour, pressure, wind, shortwave, longwave);
+        spectrum = (direct, diffuse) or None.  Returns (fields dict incl.
+        temperature and band_output, summary dict)."""
+        vertices = np.ascontiguousarray(vertices, np.float32)
+        F = len(vertices) // 3
+        S = 2 * F
+        rows, edges, denom, sky = [np.ascontiguousarray(a, np.uint32) for a in graph]
+        lit = np.ascontiguousarray(sunlit, np.float32)
+        packed = (np.concatenate([self._pack_energy_surface(m) for m in materials])
+                  if materials else np.zeros(1, np.float32))
+        mi = None if material_indices is None else np.ascontiguousarray(material_indices, np.uint32)
+        tex = None if texture_factors is None else np.ascontiguousarray(texture_factors, np.float32)
+        sd = sf = None
+        n = 0
+        if spectrum is not None:
+            sd = np.ascontiguousarray(spectrum[0], np.float32)
+            sf = np.ascontiguousarray(spectrum[1], np.float32)
+            n = min(sd.size, sf.size)
+        met = np.asarray(meteo, np.float32)
+        settings = np.asarray([time_step, coupling_iterations, tolerance, relaxation,
+                               vegetation_method, sky_temperature, width, direct_fraction],
+                              np.float32)
+        wl = np.ascontiguousarray(wavelengths, np.float32)
+        T = np.ascontiguousarray(temperature, np.float32).copy()
+        fields = np.zeros((11, S), np.float32)
+        bands = np.zeros((max(wl.size, 1), S), np.float32)
+        summary = np.zeros(5, np.float32)
+        rc = self.lib.ref_faceteb_node(
+            vertices.ctypes.data, F, leaf_count, None if mi is None else mi.ctypes.data,
+            None if tex is None else tex.ctypes.data, packed.ctypes.data, len(materials),
+            strength, zenith, azimuth, rows.ctypes.data, edges.ctypes.data, denom.ctypes.data,
+            sky.ctypes.data, lit.ctypes.data, None if sd is None else sd.ctypes.data,
+            None if sf is None else sf.ctypes.data, n, met.ctypes.data, settings.ctypes.data,
+            wl.ctypes.data if wl.size else None, wl.size, T.ctypes.data, fields.ctypes.data,
+            bands.ctypes.data, summary.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(self.error())
+        out = {k: fields[i] for i, k in enumerate(self.ENERGY_FIELDS)}
+        out["temperature"] = T
+        out["band_output"] = bands[:wl.size]
+        return out, {"coupling_iterations": int(summary[0]), "converged": int(summary[1]),
+                     "max_temperature_delta": float(summary[2]),
+                     "max_energy_residual": float(summary[3]),
+                     "max_energy_residual_equivalent": float(summary[4])}
 
     def planck(self, wavelength, temperature):
         return float(self.lib.ref_planck(wavelength, temperature))

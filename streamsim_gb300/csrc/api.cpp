@@ -14,6 +14,7 @@
 #include <sstream>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <limits>
 #include <memory>
 #include <string>
@@ -57,6 +58,7 @@ struct facetcu_context {
     DeviceBuffer samples_uv, samples_dir, fraction;
     spectral::Tables spec;
     DeviceBuffer spec_io;
+    DeviceBuffer eb_io, eb_tab;  // FacetEB node fields and per-material tables
     std::map<std::string, uint32_t> tuned;  // autotuned panel widths by problem key
     std::string gpu_name;                   // for the autotuner's key
 };
@@ -363,7 +365,7 @@ int facetcu_destroy(facetcu_context* ctx)
                             &ctx->sun_total, &ctx->sun_visible, &ctx->batch.x0, &ctx->batch.x1,
                             &ctx->batch.half, &ctx->batch.colstats, &ctx->batch.q,
                             &ctx->batch.corr, &ctx->batch.i8, &ctx->batch_inputs, &ctx->spec_io,
-                            &ctx->spec.dev})
+                            &ctx->spec.dev, &ctx->eb_io, &ctx->eb_tab})
         b->release();
     release_graphs(ctx->batch);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1584,6 +1586,411 @@ int facetcu_autotune_batched(facetcu_context* ctx, const facetcu_batch_config* c
         ctx->tuned[key] = best;
         if (cache_path) write_tune_cache(cache_path, ctx->tuned);
         *panel_width = best;
+        return FACETCU_OK;
+    });
+}
+
+}  // extern "C"
+
+// ---- FacetEB node -----------------------------------------------------------
+namespace {
+
+const float kGroundReflectance[1] = {0.20f};
+const float kGroundTransmittance[1] = {0.0f};
+
+// surfaceForFacet's fixed fallbacks (facetrtcore.cpp:607-620).
+facetcu_energy_surface fallback_surface(bool ground)
+{
+    facetcu_energy_surface m;
+    facetcu_energy_surface_defaults(&m);
+    if (ground) {
+        m.optics.reflectance = kGroundReflectance;
+        m.optics.transmittance = kGroundTransmittance;
+        m.optics.tir_reflectance = 0.05f;
+        m.optics.sunlit_temperature = 305.0f;
+        m.optics.shaded_temperature = 295.0f;
+    }
+    return m;
+}
+
+float value_at(const float* v, uint32_t n, uint32_t i, float fallback)
+{
+    if (!v || n == 0) return fallback;
+    return v[i < n ? i : n - 1];
+}
+
+void validate_energy(const facetcu_context* ctx, const facetcu_energy_parameters* p,
+                     const facetcu_meteo* meteo, const facetcu_direction* sun, const float* sunlit,
+                     const facetcu_shortwave_window* windows, uint32_t window_count,
+                     const float* band_direct, const float* band_diffuse,
+                     const facetcu_energy_fields* fields)
+{
+    if (!p || !meteo || !sun || !sunlit || !fields || !fields->temperature)
+        throw Error(FACETCU_INVALID_ARGUMENT,
+                    "parameters, meteo, sun, sunlit and fields.temperature are required");
+    if (window_count && !windows) throw Error(FACETCU_INVALID_ARGUMENT, "windows are required");
+    if (p->band_count && (!p->wavelengths || !band_direct || !band_diffuse))
+        throw Error(FACETCU_INVALID_ARGUMENT,
+                    "sensor bands need wavelengths, band_direct and band_diffuse");
+    if (p->band_count && !fields->band_output)
+        throw Error(FACETCU_INVALID_ARGUMENT, "sensor bands need fields.band_output");
+    for (uint32_t b = 0; b < p->band_count; ++b)
+        if (!std::isfinite(p->wavelengths[b]) || p->wavelengths[b] <= 0.0f)
+            throw Error(FACETCU_INVALID_ARGUMENT, "wavelengths must be finite and positive");
+    if (p->material_count && !p->materials)
+        throw Error(FACETCU_INVALID_ARGUMENT, "material_count > 0 needs materials");
+    for (uint32_t m = 0; m < p->material_count; ++m) {
+        validate_surface(p->materials[m].optics);
+        if ((p->materials[m].energy_reflectance_count && !p->materials[m].energy_reflectance) ||
+            (p->materials[m].energy_transmittance_count && !p->materials[m].energy_transmittance))
+            throw Error(FACETCU_INVALID_ARGUMENT, "a surface's energy band values are missing");
+    }
+    if (p->leaf_facet_count > ctx->facets)
+        throw Error(FACETCU_INVALID_ARGUMENT, "leaf_facet_count exceeds the facet count");
+    if (p->coupling_iterations < 1 || p->coupling_iterations > 100)
+        throw Error(FACETCU_INVALID_ARGUMENT, "coupling_iterations must be in [1, 100]");
+    if (!(p->temperature_relaxation > 0.0f && p->temperature_relaxation <= 1.0f))
+        throw Error(FACETCU_INVALID_ARGUMENT, "temperature_relaxation must be in (0, 1]");
+    if (!(p->time_step >= 1.0f) || !std::isfinite(p->time_step))
+        throw Error(FACETCU_INVALID_ARGUMENT, "time_step must be finite and >= 1");
+    if (!(p->temperature_tolerance >= 0.0f) || !(p->solver_tolerance >= 0.0f))
+        throw Error(FACETCU_INVALID_ARGUMENT, "tolerances must be non-negative");
+    if (p->solver_iterations < 1)
+        throw Error(FACETCU_INVALID_ARGUMENT, "solver_iterations must be at least 1");
+    if (p->precision != FACETCU_PRECISION_FP32 && p->precision != FACETCU_PRECISION_MIXED)
+        throw Error(FACETCU_INVALID_ARGUMENT, "precision must be FP32 or MIXED");
+    if (p->precision == FACETCU_PRECISION_MIXED && p->solver_tolerance <= 0.0f)
+        throw Error(FACETCU_INVALID_ARGUMENT, "MIXED precision needs a solver_tolerance");
+    if (!std::isfinite(sun->x) || !std::isfinite(sun->y) || !std::isfinite(sun->z))
+        throw Error(FACETCU_INVALID_ARGUMENT, "sun direction must be finite");
+    for (uint32_t w = 0; w < window_count; ++w)
+        if (!std::isfinite(windows[w].direct_normal) || !std::isfinite(windows[w].diffuse) ||
+            windows[w].direct_normal < 0.0f || windows[w].diffuse < 0.0f)
+            throw Error(FACETCU_INVALID_ARGUMENT, "window irradiances must be finite and >= 0");
+}
+
+}  // namespace
+
+extern "C" {
+
+int facetcu_faceteb_node(facetcu_context* ctx, const facetcu_energy_parameters* parameters,
+                         const facetcu_meteo* meteo, const facetcu_direction* sun,
+                         const float* sunlit, const facetcu_shortwave_window* windows,
+                         uint32_t window_count, const float* band_direct,
+                         const float* band_diffuse, facetcu_energy_fields* fields,
+                         facetcu_energy_result* result)
+{
+    return guarded(ctx, [&] {
+        require_graph(ctx, "facetebNode()");
+        validate_energy(ctx, parameters, meteo, sun, sunlit, windows, window_count, band_direct,
+                        band_diffuse, fields);
+        const auto t0 = std::chrono::steady_clock::now();
+        const facetcu_energy_parameters& p = *parameters;
+        const uint32_t F = ctx->facets, M = p.material_count, W = window_count, nb = p.band_count;
+        const size_t S = ctx->graph.surfaces;
+        if (S != 2 * size_t(F))
+            throw Error(FACETCU_LOGIC_ERROR, "the graph does not belong to the current geometry");
+        cudaStream_t st = ctx->stream;
+        const facetcu_vertex* V = ctx->vertices.as<facetcu_vertex>();
+
+        // per-slot tables: materials, then the object and ground fallbacks
+        const facetcu_energy_surface object_fb = fallback_surface(false);
+        const facetcu_energy_surface ground_fb = fallback_surface(true);
+        auto surface = [&](uint32_t slot) -> const facetcu_energy_surface& {
+            return slot < M ? p.materials[slot] : (slot == M ? object_fb : ground_fb);
+        };
+        std::vector<energy::Material> mats(M + 2);
+        std::vector<float2> sw_table(size_t(M + 2) * 2 * W);
+        std::vector<facetcu_surface_parameters> optics(M);
+        for (uint32_t slot = 0; slot < M + 2; ++slot) {
+            const facetcu_energy_surface& m = surface(slot);
+            if (slot < M) optics[slot] = m.optics;
+            energy::Material& d = mats[slot];
+            d.tir_r = m.optics.tir_reflectance;
+            d.tir_t = m.optics.tir_transmittance;
+            d.surface_resistance = m.surface_resistance;
+            d.heat_capacity = m.heat_capacity_per_area;
+            d.soil_moisture = m.soil_moisture;
+            d.storage_coefficient = energy::storage_coefficient(m, p.time_step);
+            d.pv_eta25 = m.pv_eta25;
+            d.pv_gamma = m.pv_gamma;
+            d.pv_bifaciality = m.pv_bifaciality;
+            d.convective_scale = m.convective_scale;
+            d.soil_method = m.soil_temperature_method;
+            d.photovoltaic = m.photovoltaic ? 1u : 0u;
+            d.vegetation = m.vegetation ? 1u : 0u;
+            for (uint32_t obj = 0; obj < 2; ++obj) {
+                // the broadband value when no per-sample energy spectrum is given
+                const float r_fb = obj ? 0.10f : 0.20f, t_fb = obj ? 0.05f : 0.0f;
+                const float r_mean =
+                    m.energy_reflectance_count
+                        ? 0.0f
+                        : energy::shortwave_weighted_value(m.optics.reflectance,
+                                                           m.optics.reflectance_count, r_fb);
+                const float t_mean =
+                    m.energy_transmittance_count
+                        ? 0.0f
+                        : energy::shortwave_weighted_value(m.optics.transmittance,
+                                                           m.optics.transmittance_count, t_fb);
+                for (uint32_t w = 0; w < W; ++w) {
+                    const uint32_t band = windows[w].energy_band;
+                    sw_table[(size_t(slot) * 2 + obj) * W + w] = make_float2(
+                        m.energy_reflectance_count
+                            ? value_at(m.energy_reflectance, m.energy_reflectance_count, band, r_fb)
+                            : r_mean,
+                        m.energy_transmittance_count
+                            ? value_at(m.energy_transmittance, m.energy_transmittance_count, band,
+                                       t_fb)
+                            : t_mean);
+                }
+            }
+        }
+        // band values of the sensor bands (bandValue of the same surfaces)
+        facetcu_spectral_parameters sp{};
+        const float one_band = 550.0f;
+        sp.wavelengths = nb ? p.wavelengths : &one_band;
+        sp.band_count = nb ? nb : 1;
+        sp.object = object_fb.optics;
+        sp.ground = ground_fb.optics;
+        sp.materials = M ? optics.data() : nullptr;
+        sp.material_count = M;
+        sp.leaf_facet_count = p.leaf_facet_count;
+        sp.background_angular_strength = p.background_angular_strength;
+        sp.sky_temperature = p.sky_temperature;
+        if (nb) ctx->spec.build(sp, st);
+
+        // the node's air (runFacetEBCore :3556-3571)
+        const float sky_longwave = meteo->longwave > 0.0f
+                                       ? meteo->longwave
+                                       : 5.670374419e-8f * std::pow(p.sky_temperature, 4.0f);
+        energy::Air air{};
+        air.air = std::clamp(meteo->air_temperature + 273.15f, 220.0f, 340.0f);
+        air.conductance = 5.8f + 4.1f * std::sqrt(std::max(0.1f, meteo->wind_speed));
+        air.pressure = std::max(100.0f, meteo->pressure);
+        air.density = air.pressure * 100.0f / (287.05f * air.air);
+        air.resistance = air.density * 1005.0f / std::max(0.1f, air.conductance);
+        air.vapor = meteo->vapor_pressure;
+        air.time_step = p.time_step;
+        air.relaxation = p.temperature_relaxation;
+        air.vegetation_method = p.vegetation_temperature_method == 1 ? 1 : 0;
+        std::vector<float> small(2 * size_t(W) + 3 * size_t(nb) + 2);
+        for (uint32_t w = 0; w < W; ++w) {
+            small[w] = windows[w].direct_normal;
+            small[W + w] = windows[w].diffuse;
+        }
+        const float cosz = std::max(0.0f, sun->y);
+        for (uint32_t b = 0; b < nb; ++b) {
+            const bool opt = ctx->spec.optical[b] != 0;
+            small[2 * W + b] = opt ? band_diffuse[b] * 0.5f
+                                   : facetcu_planck_radiance(p.wavelengths[b], p.sky_temperature);
+            small[2 * W + nb + b] = opt ? band_direct[b] : 0.0f;
+            small[2 * W + 2 * nb + b] = opt ? band_direct[b] * cosz + band_diffuse[b] * 0.5f : 0.0f;
+        }
+        small[2 * W + 3 * nb] = sky_longwave;
+        small[2 * W + 3 * nb + 1] = 0.0f;
+
+        // device layout
+        auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+        const size_t tab_bytes = al(mats.size() * sizeof(energy::Material)) +
+                                 al(sw_table.size() * 8 + 8) + al(small.size() * 4) +
+                                 al(size_t(nb) * 4 + 4) + al(F * 4) * 2 + al(64);
+        char* tb = static_cast<char*>(ctx->eb_tab.reserve(tab_bytes));
+        auto take_t = [&](size_t b) {
+            char* r = tb;
+            tb += al(b);
+            return r;
+        };
+        auto* d_mats = reinterpret_cast<energy::Material*>(take_t(mats.size() * sizeof(energy::Material)));
+        auto* d_sw_table = reinterpret_cast<float2*>(take_t(sw_table.size() * 8 + 8));
+        float* d_small = reinterpret_cast<float*>(take_t(small.size() * 4));
+        float* d_wl = reinterpret_cast<float*>(take_t(size_t(nb) * 4 + 4));
+        uint32_t* d_material = p.material_indices ? reinterpret_cast<uint32_t*>(take_t(F * 4)) : nullptr;
+        float* d_texture = p.texture_factors ? reinterpret_cast<float*>(take_t(F * 4)) : nullptr;
+        uint32_t* d_stats = reinterpret_cast<uint32_t*>(take_t(64));
+        const float* d_dni = d_small;
+        const float* d_diff = d_small + W;
+        const float* d_bsky = d_small + 2 * W;
+        const float* d_bbeam = d_small + 2 * W + nb;
+        const float* d_bref = d_small + 2 * W + 2 * nb;
+        const float* d_lwsky = d_small + 2 * W + 3 * nb;
+        const float* d_zero = d_lwsky + 1;
+
+        const size_t per_side = 26;  // single-column fields (below)
+        const size_t io_bytes = al(S * 4) * per_side + al(size_t(W) * S * 4) * 5 +
+                                al(size_t(nb) * S * 4) * 4;
+        char* c = static_cast<char*>(ctx->eb_io.reserve(io_bytes));
+        auto take = [&](size_t n) {
+            float* r = reinterpret_cast<float*>(c);
+            c += al(n * 4);
+            return r;
+        };
+        float* d_sunlit = take(S);
+        float* d_dgeo = take(2 * S);  // [direct geometry][zeros]: the window solve's two suns
+        float* d_T = take(S);
+        float* d_Tprev = take(S);
+        float* d_abs = take(S);
+        float* d_inc = take(S);
+        float* d_swb = take(S);
+        float* d_db = take(S);
+        float* d_lrho = take(S);
+        float* d_ltau = take(S);
+        float* d_lemis = take(S);
+        float* d_lB[2] = {take(S), take(S)};
+        float* d_lH = take(S);
+        energy::Fluxes fx{};
+        fx.net = take(S);
+        fx.sensible = take(S);
+        fx.latent = take(S);
+        fx.latent_slope = take(S);
+        fx.storage = take(S);
+        fx.storage_slope = take(S);
+        fx.pv = take(S);
+        fx.pv_slope = take(S);
+        float* d_swrho = take(size_t(W) * S);
+        float* d_swtau = take(size_t(W) * S);
+        float* d_swB = take(2 * size_t(W) * S);
+        float* d_swH = take(size_t(W) * S);
+        float* d_brho = take(size_t(nb) * S);
+        float* d_btau = take(size_t(nb) * S);
+        float* d_bemis = take(size_t(nb) * S);
+        float* d_bout = take(size_t(nb) * S);
+
+        FCU_CHECK(cudaMemcpyAsync(d_mats, mats.data(), mats.size() * sizeof(energy::Material),
+                                  cudaMemcpyHostToDevice, st));
+        if (!sw_table.empty())
+            FCU_CHECK(cudaMemcpyAsync(d_sw_table, sw_table.data(), sw_table.size() * 8,
+                                      cudaMemcpyHostToDevice, st));
+        FCU_CHECK(cudaMemcpyAsync(d_small, small.data(), small.size() * 4, cudaMemcpyHostToDevice, st));
+        if (nb) FCU_CHECK(cudaMemcpyAsync(d_wl, p.wavelengths, size_t(nb) * 4, cudaMemcpyHostToDevice, st));
+        if (d_material)
+            FCU_CHECK(cudaMemcpyAsync(d_material, p.material_indices, size_t(F) * 4,
+                                      cudaMemcpyHostToDevice, st));
+        if (d_texture)
+            FCU_CHECK(cudaMemcpyAsync(d_texture, p.texture_factors, size_t(F) * 4,
+                                      cudaMemcpyHostToDevice, st));
+        FCU_CHECK(cudaMemcpyAsync(d_sunlit, sunlit, S * 4, cudaMemcpyHostToDevice, st));
+        FCU_CHECK(cudaMemcpyAsync(d_T, fields->temperature, S * 4, cudaMemcpyHostToDevice, st));
+        FCU_CHECK(cudaMemcpyAsync(d_Tprev, d_T, S * 4, cudaMemcpyDeviceToDevice, st));
+        FCU_CHECK(cudaMemsetAsync(d_dgeo + S, 0, S * 4, st));
+        energy::direct_geometry(F, V, *sun, d_sunlit, d_dgeo, st);
+
+        facetcu_energy_result r{};
+        const bool accel = p.solver_tolerance > 0.0f;
+        auto solve = [&](uint32_t bands, uint32_t suns, uint32_t precision, const float* rho,
+                         const float* tau, const float* emis, const float* sky, const float* beam,
+                         const float* dgeo, const float* init, float* out) {
+            facetcu_batch_config cfg{};
+            cfg.band_count = bands;
+            cfg.sun_count = suns;
+            cfg.precision = precision;
+            cfg.warm_start = init ? FACETCU_WARM_GIVEN : FACETCU_WARM_NONE;
+            cfg.maximum_iterations = p.solver_iterations;
+            cfg.tolerance = p.solver_tolerance;
+            facetcu_batch_result br{};
+            const int rc = run_batched(ctx, &cfg, rho, tau, emis, sky, beam, dgeo, init, out, &br);
+            if (rc != FACETCU_OK && rc != FACETCU_NOT_CONVERGED) nested(ctx, rc);
+            return br.iterations;
+        };
+
+        // shortwave windows: each with and without its direct beam, one solve
+        if (W) {
+            energy::shortwave_optics(F, W, V, d_material, M, d_texture, p.leaf_facet_count,
+                                     d_sw_table, p.background_angular_strength, *sun, d_swrho,
+                                     d_swtau, st);
+            r.shortwave_sweeps = solve(W, 2, p.precision, d_swrho, d_swtau, nullptr, d_diff, d_dni,
+                                       d_dgeo, nullptr, d_swB);
+            energy::window_incident(ctx->graph, W, d_swB, d_diff, d_dni, d_dgeo, d_swH, st);
+            energy::shortwave_sum(uint32_t(S), W, d_swrho, d_swtau, d_swH, d_swB, d_abs, d_inc,
+                                  d_swb, d_db, st);
+        } else {
+            for (float* z : {d_abs, d_inc, d_swb, d_db}) FCU_CHECK(cudaMemsetAsync(z, 0, S * 4, st));
+        }
+
+        // coupling rounds
+        uint32_t stats[4] = {0, 0, 0, 0};
+        auto read_stats = [&] {
+            FCU_CHECK(cudaMemcpyAsync(stats, d_stats, sizeof(stats), cudaMemcpyDeviceToHost, st));
+            FCU_CHECK(cudaStreamSynchronize(st));
+            if (stats[3]) throw Error(FACETCU_RUNTIME_ERROR, "FacetEB energy residual is not finite");
+        };
+        auto as_float = [](uint32_t u) {
+            float f;
+            std::memcpy(&f, &u, 4);
+            return f;
+        };
+        int cur = -1;  // d_lB[cur] holds the latest longwave radiosity
+        auto longwave = [&] {
+            energy::longwave_optics(F, V, d_material, M, p.leaf_facet_count, d_mats,
+                                    p.background_angular_strength, d_T, d_lrho, d_ltau, d_lemis, st);
+            const int next = cur < 0 ? 0 : cur ^ 1;
+            r.longwave_sweeps += solve(1, 1, p.precision, d_lrho, d_ltau, d_lemis, d_lwsky, d_zero,
+                                       nullptr, (accel && cur >= 0) ? d_lB[cur] : nullptr,
+                                       d_lB[next]);
+            cur = next;
+            energy::window_incident(ctx->graph, 1, d_lB[cur], d_lwsky, nullptr, nullptr, d_lH, st);
+        };
+        float max_dt = 0.0f;
+        for (uint32_t round = 0; round < p.coupling_iterations; ++round) {
+            longwave();
+            energy::balance(F, p.leaf_facet_count, d_material, M, d_mats, air, d_lrho, d_ltau,
+                            d_lemis, d_lH, d_abs, d_inc, d_T, d_Tprev, fx, d_stats, true, st);
+            read_stats();
+            max_dt = as_float(stats[0]);
+            r.coupling_iterations = round + 1;
+            if (max_dt <= p.temperature_tolerance && as_float(stats[2]) <= p.temperature_tolerance)
+                break;
+        }
+        longwave();
+        energy::balance(F, p.leaf_facet_count, d_material, M, d_mats, air, d_lrho, d_ltau, d_lemis,
+                        d_lH, d_abs, d_inc, d_T, d_Tprev, fx, d_stats, false, st);
+        read_stats();
+        r.max_temperature_delta = max_dt;
+        r.max_energy_residual = as_float(stats[1]);
+        r.max_energy_residual_equivalent = as_float(stats[2]);
+        r.converged = (max_dt <= p.temperature_tolerance &&
+                       r.max_energy_residual_equivalent <= p.temperature_tolerance)
+                          ? 1u
+                          : 0u;
+
+        // sensor bands of the solved state
+        if (nb) {
+            energy::state_optics(F, nb, V, d_material, M, d_texture, p.leaf_facet_count,
+                                 ctx->spec.table, d_mats, ctx->spec.optical_dev, d_wl,
+                                 p.background_angular_strength, *sun, d_T, d_brho, d_btau, d_bemis,
+                                 st);
+            r.band_sweeps = solve(nb, 1, p.precision, d_brho, d_btau, d_bemis, d_bsky, d_bbeam,
+                                  d_dgeo, nullptr, d_bout);
+            energy::state_output(d_bout, S, nb, ctx->spec.optical_dev, d_bref, st);
+        }
+        r.solves = 2 * W + r.coupling_iterations + 1 + nb;
+
+        auto get = [&](float* host, const float* dev, size_t n) {
+            if (host) FCU_CHECK(cudaMemcpyAsync(host, dev, n * 4, cudaMemcpyDeviceToHost, st));
+        };
+        get(fields->temperature, d_T, S);
+        get(fields->shortwave_radiosity, d_swb, S);
+        get(fields->diffuse_radiosity, d_db, S);
+        get(fields->longwave_radiosity, d_lB[cur], S);
+        get(fields->absorbed_shortwave, d_abs, S);
+        get(fields->incident_shortwave, d_inc, S);
+        get(fields->net_radiation, fx.net, S);
+        get(fields->sensible_heat, fx.sensible, S);
+        get(fields->latent_heat, fx.latent, S);
+        get(fields->storage_heat, fx.storage, S);
+        get(fields->photovoltaic_power, fx.pv, S);
+        get(fields->band_output, d_bout, size_t(nb) * S);
+        std::vector<float> sw, lw;
+        if (fields->radiosity) {
+            sw.resize(S);
+            lw.resize(S);
+            get(sw.data(), d_swb, S);
+            get(lw.data(), d_lB[cur], S);
+        }
+        FCU_CHECK(cudaStreamSynchronize(st));
+        if (fields->radiosity)
+            for (size_t s = 0; s < S; ++s) fields->radiosity[s] = lw[s] + sw[s];
+        r.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (result) *result = r;
         return FACETCU_OK;
     });
 }

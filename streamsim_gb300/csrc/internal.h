@@ -269,6 +269,63 @@ void targets(const float* B, const float* B1, uint32_t S, uint32_t bands, uint32
              const float* sky, const float* beam, float* T, cudaStream_t s);
 }  // namespace mlp
 
+// ---- FacetEB node kernels (energy.cu) --------------------------------------
+namespace energy {
+// Per material slot (materials, then the object and ground fallbacks).
+struct Material {
+    float tir_r, tir_t;
+    float surface_resistance, heat_capacity, soil_moisture;
+    float storage_coefficient;  // soilStorageCoefficient(surface, dTime)
+    float pv_eta25, pv_gamma, pv_bifaciality, convective_scale;
+    int32_t soil_method;
+    uint32_t photovoltaic, vegetation;
+};
+// Per-node air scalars (runFacetEBCore :3560-3571).
+struct Air {
+    float air;          // K, clamp(T_air + 273.15, 220, 340)
+    float conductance;  // 5.8 + 4.1 sqrt(max(0.1, wind))
+    float pressure;     // max(100, p) hPa
+    float density;      // p 100 / (287.05 T)
+    float resistance;   // density 1005 / max(0.1, conductance)
+    float vapor;        // hPa
+    float time_step;
+    float relaxation;
+    int32_t vegetation_method;
+};
+struct Fluxes {
+    float *net, *sensible, *latent, *latent_slope, *storage, *storage_slope, *pv, *pv_slope;
+};
+void shortwave_optics(uint32_t F, uint32_t W, const facetcu_vertex* V, const uint32_t* material,
+                      uint32_t M, const float* texture, uint32_t leaf, const float2* table,
+                      float strength, facetcu_direction sun, float* rho, float* tau,
+                      cudaStream_t s);
+void direct_geometry(uint32_t F, const facetcu_vertex* V, facetcu_direction sun,
+                     const float* sunlit, float* dgeo, cudaStream_t s);
+void window_incident(const DeviceGraph& g, uint32_t W, const float* B, const float* sky,
+                     const float* dni, const float* dgeo, float* H, cudaStream_t s);
+void shortwave_sum(uint32_t S, uint32_t W, const float* rho, const float* tau, const float* H,
+                   const float* B, float* absorbed, float* incident, float* radiosity,
+                   float* diffuse, cudaStream_t s);
+void longwave_optics(uint32_t F, const facetcu_vertex* V, const uint32_t* material, uint32_t M,
+                     uint32_t leaf, const Material* mats, float strength, const float* T,
+                     float* rho, float* tau, float* emis, cudaStream_t s);
+void balance(uint32_t F, uint32_t leaf, const uint32_t* material, uint32_t M,
+             const Material* mats, const Air& a, const float* lw_rho, const float* lw_tau,
+             const float* lw_emis, const float* lw_in, const float* absorbed,
+             const float* incident, float* T, const float* T_prev, const Fluxes& out,
+             uint32_t* stats, bool update, cudaStream_t s);
+void state_optics(uint32_t F, uint32_t nb, const facetcu_vertex* V, const uint32_t* material,
+                  uint32_t M, const float* texture, uint32_t leaf, const float4* table,
+                  const Material* mats, const uint8_t* optical, const float* wavelengths,
+                  float strength, facetcu_direction sun, const float* T, float* rho, float* tau,
+                  float* emis, cudaStream_t s);
+void state_output(float* B, size_t S, uint32_t nb, const uint8_t* optical, const float* reference,
+                  cudaStream_t s);
+// Host arithmetic of the reference (faceteb.cpp).
+float shortwave_weighted_value(const float* values, uint32_t n, float fallback);
+float storage_coefficient(const facetcu_energy_surface& m, float time_step);
+}  // namespace energy
+
 // ---- spectral optics (spectral.cu) ----------------------------------------
 namespace spectral {
 bool optical_wavelength(float wavelength);

@@ -35,6 +35,13 @@ namespace {
 
 thread_local std::string g_host_error;
 
+}  // namespace
+
+// The message facetcu_host_last_error() reports for host-only entry points.
+void facetcu_set_host_error(const std::string& message) { g_host_error = message; }
+
+namespace {
+
 using V3 = std::array<float, 3>;
 
 V3 sub(const V3& a, const V3& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2]}; }

@@ -139,6 +139,66 @@ class BandResult(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ShortwaveSpectrum(C.Structure):
+    _fields_ = [("direct", C.c_void_p), ("diffuse", C.c_void_p), ("sample_count", C.c_uint32),
+                ("direct_fraction", C.c_float), ("window_width", C.c_uint32)]
+
+
+class ShortwaveWindow(C.Structure):
+    _fields_ = [("direct_normal", C.c_float), ("diffuse", C.c_float), ("energy_band", C.c_uint32)]
+
+
+class EnergySurfaceParameters(C.Structure):
+    _fields_ = [("optics", SurfaceParameters),
+                ("energy_reflectance", C.c_void_p), ("energy_reflectance_count", C.c_uint32),
+                ("energy_transmittance", C.c_void_p), ("energy_transmittance_count", C.c_uint32),
+                ("surface_resistance", C.c_float), ("specific_heat", C.c_float),
+                ("density", C.c_float), ("thermal_conductivity", C.c_float),
+                ("soil_moisture", C.c_float), ("heat_capacity_per_area", C.c_float),
+                ("soil_temperature_method", C.c_int32), ("photovoltaic", C.c_uint32),
+                ("vegetation", C.c_uint32), ("pv_eta25", C.c_float), ("pv_gamma", C.c_float),
+                ("pv_bifaciality", C.c_float), ("convective_scale", C.c_float)]
+
+
+class EnergyParameters(C.Structure):
+    _fields_ = [("materials", C.c_void_p), ("material_count", C.c_uint32),
+                ("material_indices", C.c_void_p), ("texture_factors", C.c_void_p),
+                ("leaf_facet_count", C.c_uint32), ("background_angular_strength", C.c_float),
+                ("wavelengths", C.c_void_p), ("band_count", C.c_uint32),
+                ("sky_temperature", C.c_float), ("time_step", C.c_float),
+                ("coupling_iterations", C.c_uint32), ("temperature_tolerance", C.c_float),
+                ("temperature_relaxation", C.c_float),
+                ("vegetation_temperature_method", C.c_int32), ("solver_iterations", C.c_uint32),
+                ("solver_tolerance", C.c_float), ("precision", C.c_uint32)]
+
+
+class Meteo(C.Structure):
+    _fields_ = [("air_temperature", C.c_float), ("vapor_pressure", C.c_float),
+                ("pressure", C.c_float), ("wind_speed", C.c_float), ("shortwave", C.c_float),
+                ("longwave", C.c_float)]
+
+
+ENERGY_FIELDS = ("temperature", "radiosity", "shortwave_radiosity", "diffuse_radiosity",
+                 "longwave_radiosity", "absorbed_shortwave", "incident_shortwave",
+                 "net_radiation", "sensible_heat", "latent_heat", "storage_heat",
+                 "photovoltaic_power", "band_output")
+
+
+class EnergyFields(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ENERGY_FIELDS]
+
+
+class EnergyResult(C.Structure):
+    _fields_ = [("coupling_iterations", C.c_uint32), ("converged", C.c_uint32),
+                ("max_temperature_delta", C.c_float), ("max_energy_residual", C.c_float),
+                ("max_energy_residual_equivalent", C.c_float), ("shortwave_sweeps", C.c_uint32),
+                ("longwave_sweeps", C.c_uint32), ("band_sweeps", C.c_uint32),
+                ("solves", C.c_uint32), ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _vp = C.c_void_p
 _u32 = C.c_uint32
 _ctx = C.c_void_p
@@ -203,6 +263,14 @@ SIGNATURES.update({
 SIGNATURES["facetcu_autotune_batched"] = (C.c_int, [_ctx, C.POINTER(BatchConfig)] + [_vp] * 7 +
                                           [C.c_char_p, C.POINTER(_u32)])
 SIGNATURES["facetcu_scene_batch"] = (C.c_int, [_ctx, _vp, _u32, _vp, C.POINTER(GraphDiagnostics)])
+SIGNATURES.update({
+    "facetcu_shortwave_windows": (C.c_int, [C.POINTER(ShortwaveSpectrum), C.c_float, C.c_float, _vp,
+                                            _u32, _vp, _u32, C.POINTER(_u32), _vp, _vp]),
+    "facetcu_energy_surface_defaults": (None, [C.POINTER(EnergySurfaceParameters)]),
+    "facetcu_faceteb_node": (C.c_int, [_ctx, C.POINTER(EnergyParameters), C.POINTER(Meteo),
+                                       C.POINTER(Direction), _vp, _vp, _u32, _vp, _vp,
+                                       C.POINTER(EnergyFields), C.POINTER(EnergyResult)]),
+})
 OPTIONAL_SIGNATURES = {}
 MLP_INPUTS = 12
 MLP_OUTPUTS = 64
@@ -352,6 +420,106 @@ def spectral_parameters(wavelengths, leaf_facet_count, object_surface=None, grou
                            _ptr(keep["tex"]) if "tex" in keep else None, leaf_facet_count,
                            background_angular_strength, sky_temperature, 1 if accelerated else 0)
     return p, keep
+
+
+class EnergySurface(Surface):
+    """SurfaceParameters with the energy-balance fields
+    (facetrtcore.cpp:113-138); the defaults are the reference's."""
+
+    def __init__(self, reflectance=(0.10,), transmittance=(0.05,), tir_reflectance=0.03,
+                 tir_transmittance=0.0, sunlit_temperature=300.0, shaded_temperature=296.0,
+                 energy_reflectance=(), energy_transmittance=(), surface_resistance=120.0,
+                 specific_heat=1180.0, density=1800.0, thermal_conductivity=1.55,
+                 soil_moisture=0.25, heat_capacity_per_area=60000.0, soil_temperature_method=1,
+                 photovoltaic=False, vegetation=True, pv_eta25=0.22, pv_gamma=-0.0035,
+                 pv_bifaciality=0.0, convective_scale=1.0):
+        super().__init__(reflectance, transmittance, tir_reflectance, tir_transmittance,
+                         sunlit_temperature, shaded_temperature)
+        self.energy_reflectance = np.asarray(energy_reflectance, np.float32).ravel()
+        self.energy_transmittance = np.asarray(energy_transmittance, np.float32).ravel()
+        self.surface_resistance = surface_resistance
+        self.specific_heat = specific_heat
+        self.density = density
+        self.thermal_conductivity = thermal_conductivity
+        self.soil_moisture = soil_moisture
+        self.heat_capacity_per_area = heat_capacity_per_area
+        self.soil_temperature_method = soil_temperature_method
+        self.photovoltaic = photovoltaic
+        self.vegetation = vegetation
+        self.pv_eta25 = pv_eta25
+        self.pv_gamma = pv_gamma
+        self.pv_bifaciality = pv_bifaciality
+        self.convective_scale = convective_scale
+
+    def energy_struct(self):
+        er, et = self.energy_reflectance, self.energy_transmittance
+        return EnergySurfaceParameters(
+            self.struct(), _ptr(er) if er.size else None, er.size, _ptr(et) if et.size else None,
+            et.size, self.surface_resistance, self.specific_heat, self.density,
+            self.thermal_conductivity, self.soil_moisture, self.heat_capacity_per_area,
+            self.soil_temperature_method, 1 if self.photovoltaic else 0,
+            1 if self.vegetation else 0, self.pv_eta25, self.pv_gamma, self.pv_bifaciality,
+            self.convective_scale)
+
+
+def energy_parameters(leaf_facet_count, materials=(), material_indices=None,
+                      texture_factors=None, background_angular_strength=0.0, wavelengths=(),
+                      sky_temperature=250.0, time_step=1800.0, coupling_iterations=20,
+                      temperature_tolerance=0.05, temperature_relaxation=0.5,
+                      vegetation_temperature_method=0, solver_iterations=64, solver_tolerance=0.0,
+                      precision=PRECISION_FP32):
+    """runFacetEBCore's settings (defaults as the reference's XML defaults,
+    facetrtcore.cpp:3196-3233): an EnergyParameters struct plus the arrays it
+    points to (keep both)."""
+    mats = list(materials)
+    keep = {"surfaces": mats, "wl": _f32(wavelengths)}
+    arr = None
+    if mats:
+        arr = (EnergySurfaceParameters * len(mats))(*[m.energy_struct() for m in mats])
+        keep["mats"] = arr
+    if material_indices is not None:
+        keep["mi"] = np.ascontiguousarray(material_indices, np.uint32)
+    if texture_factors is not None:
+        keep["tex"] = _f32(texture_factors)
+    p = EnergyParameters(C.cast(arr, C.c_void_p) if arr is not None else None, len(mats),
+                         _ptr(keep["mi"]) if "mi" in keep else None,
+                         _ptr(keep["tex"]) if "tex" in keep else None, leaf_facet_count,
+                         background_angular_strength,
+                         _ptr(keep["wl"]) if keep["wl"].size else None, keep["wl"].size,
+                         sky_temperature, time_step, coupling_iterations, temperature_tolerance,
+                         temperature_relaxation, vegetation_temperature_method, solver_iterations,
+                         solver_tolerance, precision)
+    return p, keep
+
+
+def shortwave_windows(total_shortwave, cos_zenith, direct=None, diffuse=None,
+                      direct_fraction=0.8, window_width=100, wavelengths=()):
+    """The node's spectral-acceleration windows and per-band spectral
+    irradiance: (windows (n, 3) [direct normal, diffuse, centre sample],
+    ShortwaveWindow array, band_direct, band_diffuse)."""
+    lib = load()
+    d = None if direct is None else _f32(direct)
+    f = None if diffuse is None else _f32(diffuse)
+    n = 0 if d is None or f is None else min(d.size, f.size)
+    spec = ShortwaveSpectrum(_ptr(d) if d is not None else None,
+                             _ptr(f) if f is not None else None, n, direct_fraction, window_width)
+    wl = _f32(wavelengths)
+    bd = np.zeros(wl.size, np.float32)
+    bf = np.zeros(wl.size, np.float32)
+    count = _u32(0)
+    lib.facetcu_shortwave_windows(C.byref(spec), total_shortwave, cos_zenith,
+                                  _ptr(wl) if wl.size else None, wl.size, None, 0,
+                                  C.byref(count), None, None)  # counts the windows
+    cap = count.value
+    arr = (ShortwaveWindow * max(cap, 1))()
+    rc = lib.facetcu_shortwave_windows(C.byref(spec), total_shortwave, cos_zenith,
+                                       _ptr(wl) if wl.size else None, wl.size,
+                                       C.cast(arr, C.c_void_p), cap, C.byref(count), _ptr(bd),
+                                       _ptr(bf))
+    _host_check(rc)
+    win = np.array([[w.direct_normal, w.diffuse, w.energy_band] for w in arr[:count.value]],
+                   np.float64).reshape(-1, 3)
+    return win, arr, bd, bf
 
 
 def device_count():
@@ -622,6 +790,37 @@ class FacetrtCuda:
                                                  C.byref(d), _ptr(bands), _ptr(enh),
                                                  C.byref(res)))
         return bands, enh, res.as_dict()
+
+    # -- FacetEB node --------------------------------------------------------
+    def facetebNode(self, parameters, meteo, sun, sunlit, windows, temperature,
+                    band_direct=None, band_diffuse=None, fields=ENERGY_FIELDS):
+        """One FacetEB time node: (dict of per-side fields, result dict).
+        windows is the ShortwaveWindow array of shortwave_windows();
+        temperature the state at the node start (2F,); meteo a dict or Meteo."""
+        lit = _f32(sunlit)
+        S = lit.size
+        if isinstance(meteo, dict):
+            meteo = Meteo(**meteo)
+        out = {}
+        for k in fields:
+            n = S * parameters.band_count if k == "band_output" else S
+            if k == "band_output" and n == 0:
+                continue
+            out[k] = np.zeros(n, np.float32)
+        out["temperature"] = _f32(temperature).copy()
+        f = EnergyFields(**{k: _ptr(v) for k, v in out.items()})
+        nwin = len(windows) if windows is not None else 0
+        bd = None if band_direct is None else _f32(band_direct)
+        bf = None if band_diffuse is None else _f32(band_diffuse)
+        d = Direction(*[float(x) for x in np.ravel(sun)[:3]])
+        res = EnergyResult()
+        self._check(self.lib.facetcu_faceteb_node(
+            self.h, C.byref(parameters), C.byref(meteo), C.byref(d), _ptr(lit),
+            C.cast(windows, C.c_void_p) if nwin else None, nwin, _ptr(bd), _ptr(bf), C.byref(f),
+            C.byref(res)))
+        if "band_output" in out:
+            out["band_output"] = out["band_output"].reshape(parameters.band_count, S)
+        return out, res.as_dict()
 
     # -- learned warm start -------------------------------------------------
     def mlpReset(self, seed=1):

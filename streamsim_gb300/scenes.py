@@ -374,3 +374,32 @@ def hemisphere_samples(rays, sets=32, seed=1234):
         uv[p, :, 0] = su * (1.0 - w2)
         uv[p, :, 1] = su * w2
     return uv, dirs
+
+
+def energy_site(seed=0, leaves=1500, soil_cells=16):
+    """A small FacetEB site: a leaf crown, a building, a tilted PV array and
+    a soil plane (objects first, soil last, as loadProjectScene orders them).
+    Returns (scene, material_indices, kinds) where kinds names the material
+    slots: 0 leaf, 1 wall, 2 PV, 3-5 soils (force-restore, 0.35 Rn, dry
+    1.5 x force-restore); index 99 marks facets without a material."""
+    rng = np.random.default_rng(seed)
+    centres = rng.normal(0.0, 1.0, (leaves, 3))
+    centres *= (1.4 * rng.uniform(0, 1, leaves) ** (1 / 3) /
+                np.linalg.norm(centres, axis=1))[:, None]
+    centres += np.array([-2.0, 2.6, 0.0])
+    leaf = _triangles_to_vertices(*equilateral(centres, uniform_sphere(leaves, rng), 0.08, rng))
+    wall = _triangles_to_vertices(*box(1.0, -2.5, 2.5, 2.0, 3.0, cell=0.6))
+    tilt = np.array([0.0, 0.55, -0.85])
+    panel = _triangles_to_vertices(*quad_grid((-3.0, 0.8, 3.0), (3.0, 0.0, 0.0), tilt, 8, 2))
+    soil = _triangles_to_vertices(*soil_grid(-6, 6, -6, 6, soil_cells, soil_cells))
+    objects = len(leaf) // 3 + len(wall) // 3 + len(panel) // 3
+    vertices = np.concatenate([leaf, wall, panel, soil])
+    F = len(vertices) // 3
+    nl, nw, npv = len(leaf) // 3, len(wall) // 3, len(panel) // 3
+    mi = np.empty(F, np.uint32)
+    mi[:nl] = np.where(rng.uniform(0, 1, nl) < 0.9, 0, 99)
+    mi[nl:nl + nw] = 1
+    mi[nl + nw:objects] = 2
+    mi[objects:] = rng.choice([3, 4, 5, 99], F - objects, p=[0.4, 0.25, 0.25, 0.1])
+    return Scene(vertices, objects, f"energy_site(seed={seed})", walls=False), mi, (
+        "leaf", "wall", "pv", "soil", "soil_storage_035", "dry_soil")

@@ -64,10 +64,11 @@ def parse():
     p.add_argument("--scenes", type=int, default=32, help="c5: number of scenes")
     p.add_argument("--scene-min", type=int, default=20000, help="c5: smallest scene (facets)")
     p.add_argument("--scene-max", type=int, default=400000, help="c5: largest scene (facets)")
-    p.add_argument("--config", default="c2", choices=["c2", "c3", "c5"],
+    p.add_argument("--config", default="c2", choices=["c2", "c3", "c5", "eb"],
                    help="c2: the headline workload; c3: 150-tree forest, 256 suns x 64 bands "
                         "(16,384 right-hand sides, outputs kept on the device); c5: 32 scenes "
-                        "of uneven size, 64 bands + a thermal band, as one batch")
+                        "of uneven size, 64 bands + a thermal band, as one batch; eb: one "
+                        "FacetEB time node (shortwave windows, longwave coupling, sensor bands)")
     p.add_argument("--warm-start", default="none", choices=["auto", "mlp", "none"],
                    help="mlp: the shipped MLP weights; auto: those when present and bands == 64")
     return p.parse_args()
@@ -692,6 +693,121 @@ def run_c5(args, rank, world, local):
     batch.close()
 
 
+def run_eb(args, rank, world, local):
+    """One FacetEB time node (runFacetEBCore, facetrtcore.cpp:3462-3908) on
+    the config-2 forest: 20 shortwave windows (each solved with and without
+    its direct beam), up to 20 longwave coupling rounds with the energy
+    balance and temperature update, and 8 sensor bands.  The unit counts the
+    single-column solves the reference's node runs (2 per window, one per
+    coupling round plus the final one, one per band) times the facets, per
+    second of node time through the host-buffer C ABI.  Compared with the
+    same node at the reference's fixed 64 sweeps per solve, and with the
+    reference's solveCpu (one 64-sweep solve timed, times the node's solve
+    count: its node is that loop of solves, single-threaded)."""
+    import torch
+
+    from streamsim_gb300 import facetcu as fc
+    from streamsim_gb300 import scenes
+
+    torch.cuda.set_device(local)
+    w = build_workload(args, fc, scenes)
+    m, sc = w["model"], w["scene"]
+    F, S = sc.facet_count, sc.surface_count
+    leaves = sc.leaf_count - sc.trunk_count
+    mi = np.full(F, 2, np.uint32)
+    mi[:leaves] = 0
+    mi[leaves:sc.leaf_count] = 1
+    red_edge = np.where(np.arange(2001) < 300, 0.06, 0.46).astype(np.float32)
+    materials = [
+        fc.EnergySurface([0.05, 0.08, 0.45, 0.30, 0.22], [0.04, 0.06, 0.40], 0.02, 0.01,
+                         energy_reflectance=red_edge, energy_transmittance=0.8 * red_edge,
+                         surface_resistance=150.0, heat_capacity_per_area=1500.0),
+        fc.EnergySurface([0.25, 0.35], [0.0], 0.05, 0.0, vegetation=False,
+                         heat_capacity_per_area=90000.0),
+        fc.EnergySurface([0.15], [0.0], 0.05, 0.0, soil_moisture=0.22),
+    ]
+    nm = np.arange(2001, dtype=np.float64)
+    direct = (np.exp(-((nm - 150.0) / 600.0) ** 2)).astype(np.float32)
+    diffuse = (0.35 * np.exp(-((nm - 20.0) / 300.0) ** 2)).astype(np.float32)
+    bands = [450.0, 550.0, 650.0, 865.0, 1610.0, 2200.0, 10000.0, 11000.0]
+    meteo = dict(air_temperature=24.0, vapor_pressure=15.0, pressure=1000.0, wind_speed=2.0,
+                 shortwave=750.0, longwave=330.0)
+    sun = w["sun"]
+    win, windows, bd, bf = fc.shortwave_windows(meteo["shortwave"], max(0.0, float(sun[1])),
+                                                direct, diffuse, 0.8, 100, bands)
+    T0 = np.full(S, meteo["air_temperature"] + 273.15, np.float32)
+    lit = w["lit"]
+
+    def node(tolerance):
+        p, keep = fc.energy_parameters(sc.leaf_count, materials, mi, None, 0.0, bands,
+                                       solver_tolerance=tolerance)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out, res = m.facetebNode(p, meteo, sun, lit, windows, T0, bd, bf)
+        return out, res, time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        node(1e-6)
+    times = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            out, res, dt = node(1e-6)
+            times.append(dt)
+    node_s = float(np.mean(times))
+    fixed, fres, fixed_s = node(0.0)
+    fixed, fres, fixed_s = node(0.0)
+    units = F * res["solves"]
+    h2d = 4 * (2 * S + 2 * F) + 12 * len(win)
+    d2h = 4 * S * (12 + len(bands))
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import pyoracle
+        from oracle.pyoracle import Graph
+        try:
+            ref = pyoracle.Reference(pyoracle.build_reference())
+            kind = "reference"
+        except Exception:
+            ref, kind = pyoracle.Oracle(), "port"
+        g = Graph(*m.graph())
+        o = np.zeros((S, 4), np.float32)
+        o[:, 0] = 0.3
+        o[:, 1] = 0.2
+        o[:, 3] = w["dgeo"][0] * 500.0
+        t0 = time.perf_counter()
+        ref.solve(g, o, 40.0, 64)
+        one = time.perf_counter() - t0
+        cpu = {"value": F / one, "unit": UNIT, "cores": 1, "kind": kind,
+               "sample": f"one 64-sweep solveCpu ({one:.2f} s) x the node's "
+                         f"{res['solves']} solves = {one * res['solves']:.0f} s per node "
+                         "(the reference's node is that loop of single-threaded solves)",
+               "node_seconds_estimate": one * res["solves"]}
+    line = {
+        "metric": METRIC, "value": units / node_s, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": node_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene generator, no dataset)",
+        "config": {"workload": f"FacetEB node on the config2 forest: {F:,} facets, "
+                               f"{len(win)} shortwave windows, 20 coupling rounds at most, "
+                               f"{len(bands)} sensor bands",
+                   "facets": F, "windows": len(win), "bands": len(bands),
+                   "solver_tolerance": 1e-6, "view_factors": w["vf"],
+                   "l2": "inputs far larger than L2 (no flush needed)"},
+        "node": {k: res[k] for k in ("coupling_iterations", "converged", "max_temperature_delta",
+                                     "max_energy_residual_equivalent", "shortwave_sweeps",
+                                     "longwave_sweeps", "band_sweeps", "solves")},
+        "fixed_sweeps": {"value": units / fixed_s, "ms_per_step": fixed_s * 1e3,
+                         "coupling_iterations": fres["coupling_iterations"],
+                         "max_abs_temperature_difference_K": float(
+                             np.max(np.abs(fixed["temperature"] - out["temperature"])))},
+        "e2e": {"value": units / node_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(res["kernel_launches"]), "clocks": clocks.summary(),
+        "roofline": None, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    m.close()
+
+
 def run_reference(args, rank, world, local):
     if rank != 0:
         return
@@ -724,6 +840,8 @@ def main():
         run_c3(args, rank, world, local)
     elif args.config == "c5":
         run_c5(args, rank, world, local)
+    elif args.config == "eb":
+        run_eb(args, rank, world, local)
     else:
         run_gpu(args, rank, world, local)
     if world > 1:

@@ -570,6 +570,7 @@ typedef struct {
     uint32_t longwave_sweeps;              /* summed over the coupling solves */
     uint32_t band_sweeps;
     uint32_t solves;                       /* radiosity solves the reference would run */
+    uint32_t kernel_launches;              /* kernels the node launched */
     double seconds;
 } facetcu_energy_result;
 /* One FacetEB time node (runFacetEBCore :3462-3908) on the context's graph:

@@ -1816,7 +1816,7 @@ int facetcu_faceteb_node(facetcu_context* ctx, const facetcu_energy_parameters* 
         const float* d_zero = d_lwsky + 1;
 
         const size_t per_side = 26;  // single-column fields (below)
-        const size_t io_bytes = al(S * 4) * per_side + al(size_t(W) * S * 4) * 5 +
+        const size_t io_bytes = al(S * 4) * per_side + al(size_t(W) * S * 4) * 6 +
                                 al(size_t(nb) * S * 4) * 4;
         char* c = static_cast<char*>(ctx->eb_io.reserve(io_bytes));
         auto take = [&](size_t n) {
@@ -1850,6 +1850,7 @@ int facetcu_faceteb_node(facetcu_context* ctx, const facetcu_energy_parameters* 
         float* d_swtau = take(size_t(W) * S);
         float* d_swB = take(2 * size_t(W) * S);
         float* d_swH = take(size_t(W) * S);
+        float* d_swBT = take(size_t(W) * S);
         float* d_brho = take(size_t(nb) * S);
         float* d_btau = take(size_t(nb) * S);
         float* d_bemis = take(size_t(nb) * S);
@@ -1875,6 +1876,7 @@ int facetcu_faceteb_node(facetcu_context* ctx, const facetcu_energy_parameters* 
         energy::direct_geometry(F, V, *sun, d_sunlit, d_dgeo, st);
 
         facetcu_energy_result r{};
+        r.kernel_launches = 1;
         const bool accel = p.solver_tolerance > 0.0f;
         auto solve = [&](uint32_t bands, uint32_t suns, uint32_t precision, const float* rho,
                          const float* tau, const float* emis, const float* sky, const float* beam,
@@ -1889,6 +1891,7 @@ int facetcu_faceteb_node(facetcu_context* ctx, const facetcu_energy_parameters* 
             facetcu_batch_result br{};
             const int rc = run_batched(ctx, &cfg, rho, tau, emis, sky, beam, dgeo, init, out, &br);
             if (rc != FACETCU_OK && rc != FACETCU_NOT_CONVERGED) nested(ctx, rc);
+            r.kernel_launches += br.kernel_launches;
             return br.iterations;
         };
 
@@ -1899,9 +1902,11 @@ int facetcu_faceteb_node(facetcu_context* ctx, const facetcu_energy_parameters* 
                                      d_swtau, st);
             r.shortwave_sweeps = solve(W, 2, p.precision, d_swrho, d_swtau, nullptr, d_diff, d_dni,
                                        d_dgeo, nullptr, d_swB);
-            energy::window_incident(ctx->graph, W, d_swB, d_diff, d_dni, d_dgeo, d_swH, st);
+            energy::window_incident(ctx->graph, W, d_swB, d_diff, d_dni, d_dgeo, d_swBT, d_swH,
+                                    st);
             energy::shortwave_sum(uint32_t(S), W, d_swrho, d_swtau, d_swH, d_swB, d_abs, d_inc,
                                   d_swb, d_db, st);
+            r.kernel_launches += 4;
         } else {
             for (float* z : {d_abs, d_inc, d_swb, d_db}) FCU_CHECK(cudaMemsetAsync(z, 0, S * 4, st));
         }
@@ -1927,7 +1932,9 @@ int facetcu_faceteb_node(facetcu_context* ctx, const facetcu_energy_parameters* 
                                        nullptr, (accel && cur >= 0) ? d_lB[cur] : nullptr,
                                        d_lB[next]);
             cur = next;
-            energy::window_incident(ctx->graph, 1, d_lB[cur], d_lwsky, nullptr, nullptr, d_lH, st);
+            energy::window_incident(ctx->graph, 1, d_lB[cur], d_lwsky, nullptr, nullptr, nullptr,
+                                    d_lH, st);
+            r.kernel_launches += 3;  // optics, incident and the balance after it
         };
         float max_dt = 0.0f;
         for (uint32_t round = 0; round < p.coupling_iterations; ++round) {
@@ -1961,6 +1968,7 @@ int facetcu_faceteb_node(facetcu_context* ctx, const facetcu_energy_parameters* 
             r.band_sweeps = solve(nb, 1, p.precision, d_brho, d_btau, d_bemis, d_bsky, d_bbeam,
                                   d_dgeo, nullptr, d_bout);
             energy::state_output(d_bout, S, nb, ctx->spec.optical_dev, d_bref, st);
+            r.kernel_launches += 2;
         }
         r.solves = 2 * W + r.coupling_iterations + 1 + nb;
 

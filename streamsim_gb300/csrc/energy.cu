@@ -14,7 +14,10 @@
 //                        :952-1003), window-major planes for the batched solver
 //   k_direct_geometry    clamp(sunlit) max(0, n . sun), times a beam per column
 //   k_window_incident    H[w][s] for every window column (incidentIrradianceCpu
-//                        :1531-1559, FP64 gather in edge order)
+//                        :1531-1559: an FP64 gather there, a compensated FP32 one
+//                        here), a warp per side over a side-major copy of the
+//                        windows (k_transpose)
+//   k_incident_one       the same for the single longwave column
 //   k_shortwave_sum      the window accumulation in window order (:3536-3552)
 //   k_longwave_optics    makeEnergyLongwaveOptics (:1005-1036)
 //   k_balance            evaluateEnergyFluxes + measureEnergyResidual + the
@@ -152,31 +155,120 @@ __global__ void k_direct_geometry(uint32_t F, const facetcu_vertex* __restrict__
     dgeo[s] = sclamp(sunlit[s], 0.0f, 1.0f) * smax(0.0f, dotf(side_normal(V, s), sun));
 }
 
-__global__ void k_window_incident(uint32_t S, uint32_t W, const uint32_t* __restrict__ rows,
-                                  const facetcu_csr_edge* __restrict__ edges,
-                                  const uint32_t* __restrict__ denom,
-                                  const uint32_t* __restrict__ skyc, const float* __restrict__ B,
-                                  const float* __restrict__ sky, const float* __restrict__ dni,
-                                  const float* __restrict__ dgeo, float* __restrict__ H)
+// Side-major copy of the first W columns of a column-major [R][S] block.
+__global__ void k_transpose(uint32_t S, uint32_t W, const float* __restrict__ B,
+                            float* __restrict__ BT)
 {
     const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= size_t(S) * W) return;
-    const uint32_t w = uint32_t(i / S), s = uint32_t(i % S);
-    const float* __restrict__ Bw = B + size_t(w) * S;
-    const float L = sky[w];
-    double diffuse = L;
-    const uint32_t d = denom[s];
-    if (d != 0u) {
-        diffuse = double(skyc[s]) * double(L);
-        const uint32_t end = rows[s + 1];
-        for (uint32_t e = rows[s]; e < end; ++e) {
-            const facetcu_csr_edge ed = edges[e];
-            diffuse += double(ed.count) * double(Bw[ed.neighbor]);
+    const uint32_t s = uint32_t(i / W), w = uint32_t(i % W);
+    BT[i] = B[size_t(w) * S + s];
+}
+
+// Compensated FP32 sum of count x B terms: each product split exactly into
+// p + e (TwoProduct with an explicit fmaf) and each addition into s + err
+// (Neumaier's TwoSum); the errors accumulate in c.  sum + c then carries
+// about twice the float precision, as close to the reference's FP64 sum as
+// its conversion back to float can tell, at FP32 throughput (GB300's FP64
+// rate is a small fraction of it).
+struct Csum {
+    float s, c;
+};
+__device__ __forceinline__ void csum_add(Csum& a, float t, float e)
+{
+    const float s = a.s + t;
+    const float err = fabsf(a.s) >= fabsf(t) ? (a.s - s) + t : (t - s) + a.s;
+    a.s = s;
+    a.c += err + e;
+}
+__device__ __forceinline__ void csum_term(Csum& a, uint32_t count, float v)
+{
+    const float n = float(count);  // exact below 2^24
+    const float p = n * v;
+    csum_add(a, p, fmaf(n, v, -p));
+}
+__device__ __forceinline__ double csum_value(const Csum& a) { return double(a.s) + double(a.c); }
+
+// H[w][s] = max(0, diffuse + D): one warp per side, lane w of each 32-wide
+// window group sums its window's gather in the reference's edge order (each
+// edge is one broadcast load, its W values one contiguous row of BT).
+__global__ void k_window_incident(uint32_t S, uint32_t W, const uint32_t* __restrict__ rows,
+                                  const facetcu_csr_edge* __restrict__ edges,
+                                  const uint32_t* __restrict__ denom,
+                                  const uint32_t* __restrict__ skyc, const float* __restrict__ BT,
+                                  const float* __restrict__ sky, const float* __restrict__ dni,
+                                  const float* __restrict__ dgeo, float* __restrict__ H)
+{
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
+    if (warp >= S) return;
+    const uint32_t s = warp;
+    const uint32_t d = denom[s], start = rows[s], end = rows[s + 1];
+    const float g = dgeo ? dgeo[s] : 0.0f;
+    for (uint32_t w0 = 0; w0 < W; w0 += 32) {
+        const uint32_t w = w0 + lane;
+        const bool on = w < W;
+        const float L = on ? sky[w] : 0.0f;
+        double diffuse = L;
+        if (d != 0u) {
+            Csum acc{0.0f, 0.0f};
+            uint32_t e = start;
+            for (; e + 4 <= end; e += 4) {
+                facetcu_csr_edge ed[4];
+                float v[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) ed[k] = edges[e + k];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) v[k] = on ? BT[size_t(ed[k].neighbor) * W + w] : 0.0f;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) csum_term(acc, ed[k].count, v[k]);
+            }
+            for (; e < end; ++e) {
+                const facetcu_csr_edge ed = edges[e];
+                csum_term(acc, ed.count, on ? BT[size_t(ed.neighbor) * W + w] : 0.0f);
+            }
+            diffuse = (double(skyc[s]) * double(L) + csum_value(acc)) / double(d);
         }
-        diffuse /= double(d);
+        if (on) {
+            const float D = dgeo ? g * dni[w] : 0.0f;
+            H[size_t(w) * S + s] = smax(0.0f, float(diffuse) + D);
+        }
     }
-    const float D = dgeo ? dgeo[s] * dni[w] : 0.0f;
-    H[i] = smax(0.0f, float(diffuse) + D);
+}
+
+// One column, no direct term: a warp per side, lanes over the edges, the
+// lanes' compensated partial sums combined by shuffles.
+__global__ void k_incident_one(uint32_t S, const uint32_t* __restrict__ rows,
+                               const facetcu_csr_edge* __restrict__ edges,
+                               const uint32_t* __restrict__ denom,
+                               const uint32_t* __restrict__ skyc, const float* __restrict__ B,
+                               const float* __restrict__ sky, float* __restrict__ H)
+{
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
+    if (warp >= S) return;
+    const uint32_t s = warp;
+    const uint32_t d = denom[s];
+    const float L = sky[0];
+    Csum acc{0.0f, 0.0f};
+    if (d != 0u) {
+        const uint32_t end = rows[s + 1];
+        for (uint32_t e = rows[s] + lane; e < end; e += 32) {
+            const facetcu_csr_edge ed = edges[e];
+            csum_term(acc, ed.count, B[ed.neighbor]);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float os = __shfl_xor_sync(0xffffffffu, acc.s, o);
+        const float oc = __shfl_xor_sync(0xffffffffu, acc.c, o);
+        csum_add(acc, os, oc);
+    }
+    if (lane == 0) {
+        double diffuse = L;
+        if (d != 0u) diffuse = (double(skyc[s]) * double(L) + csum_value(acc)) / double(d);
+        H[s] = smax(0.0f, float(diffuse));
+    }
 }
 
 // Window accumulation in window order; columns [0, W) of B are the direct
@@ -432,13 +524,24 @@ void direct_geometry(uint32_t F, const facetcu_vertex* V, facetcu_direction sun,
 }
 
 void window_incident(const DeviceGraph& g, uint32_t W, const float* B, const float* sky,
-                     const float* dni, const float* dgeo, float* H, cudaStream_t s)
+                     const float* dni, const float* dgeo, float* BT, float* H, cudaStream_t s)
 {
-    const size_t n = size_t(g.surfaces) * W;
-    if (!n) return;
-    k_window_incident<<<blocks(n, 128), 128, 0, s>>>(
-        g.surfaces, W, g.row_offsets.as<uint32_t>(), g.edges.as<facetcu_csr_edge>(),
-        g.denominators.as<uint32_t>(), g.sky.as<uint32_t>(), B, sky, dni, dgeo, H);
+    const size_t S = g.surfaces;
+    if (!S || !W) return;
+    const uint32_t* rows = g.row_offsets.as<uint32_t>();
+    const facetcu_csr_edge* edges = g.edges.as<facetcu_csr_edge>();
+    const uint32_t* den = g.denominators.as<uint32_t>();
+    const uint32_t* skyc = g.sky.as<uint32_t>();
+    if (W == 1 && !dgeo) {
+        k_incident_one<<<blocks(S * 32, 256), 256, 0, s>>>(uint32_t(S), rows, edges, den, skyc, B,
+                                                            sky, H);
+        FCU_LAUNCH("k_incident_one");
+        return;
+    }
+    k_transpose<<<blocks(S * W, 256), 256, 0, s>>>(uint32_t(S), W, B, BT);
+    FCU_LAUNCH("k_transpose");
+    k_window_incident<<<blocks(S * 32, 256), 256, 0, s>>>(uint32_t(S), W, rows, edges, den, skyc,
+                                                          BT, sky, dni, dgeo, H);
     FCU_LAUNCH("k_window_incident");
 }
 

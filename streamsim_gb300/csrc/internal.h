@@ -301,8 +301,9 @@ void shortwave_optics(uint32_t F, uint32_t W, const facetcu_vertex* V, const uin
                       cudaStream_t s);
 void direct_geometry(uint32_t F, const facetcu_vertex* V, facetcu_direction sun,
                      const float* sunlit, float* dgeo, cudaStream_t s);
+// BT: scratch of S * W floats (unused for one column without a direct term).
 void window_incident(const DeviceGraph& g, uint32_t W, const float* B, const float* sky,
-                     const float* dni, const float* dgeo, float* H, cudaStream_t s);
+                     const float* dni, const float* dgeo, float* BT, float* H, cudaStream_t s);
 void shortwave_sum(uint32_t S, uint32_t W, const float* rho, const float* tau, const float* H,
                    const float* B, float* absorbed, float* incident, float* radiosity,
                    float* diffuse, cudaStream_t s);

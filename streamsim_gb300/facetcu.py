@@ -193,7 +193,8 @@ class EnergyResult(C.Structure):
                 ("max_temperature_delta", C.c_float), ("max_energy_residual", C.c_float),
                 ("max_energy_residual_equivalent", C.c_float), ("shortwave_sweeps", C.c_uint32),
                 ("longwave_sweeps", C.c_uint32), ("band_sweeps", C.c_uint32),
-                ("solves", C.c_uint32), ("seconds", C.c_double)]
+                ("solves", C.c_uint32), ("kernel_launches", C.c_uint32),
+                ("seconds", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

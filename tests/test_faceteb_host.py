@@ -87,3 +87,28 @@ def test_energy_surface_defaults_are_the_reference_defaults():
     assert s.optics.reflectance_count == 1 and s.optics.transmittance_count == 1
     assert np.isclose(s.optics.tir_reflectance, 0.03) and s.optics.tir_transmittance == 0.0
     assert (s.surface_resistance, s.soil_temperature_method, s.vegetation) == (120.0, 1, 1)
+
+
+def test_time_tokens_and_default_meteorology():
+    from streamsim_gb300 import faceteb
+    assert faceteb.time_token(1.0) == "DOY1_00-00"
+    assert faceteb.time_token(172.5) == "DOY172_12-00"
+    assert faceteb.time_token(10.99999) == "DOY11_00-00"  # 1439.99 min round up to the next day
+    assert faceteb.time_token(3.0208333) == "DOY3_00-30"
+    rows = faceteb.default_meteorology(4, 1800.0)
+    assert [r["node"] for r in rows] == [0, 1, 2, 3]
+    assert np.float32(rows[3]["julian_time"]) == np.float32(1.0) + np.float32(3 * 1800.0 / 86400.0)
+    assert rows[0]["pressure"] == 839.0 and rows[0]["longwave"] == 320.0
+
+
+def test_read_meteorology(tmp_path):
+    from streamsim_gb300 import faceteb
+    p = tmp_path / "meteo.txt"
+    p.write_text("julian T e p u sw lw\n"
+                 "172.25 18.5 12.0 1000 1.5 120 330\n"
+                 "bad row here\n"
+                 "172.5 24 15 1001 2.0 800 350\n"
+                 "172.75 22 14\n")
+    rows = faceteb.read_meteorology(str(p))
+    assert [r["node"] for r in rows] == [0, 2]
+    assert rows[1]["shortwave"] == 800.0 and rows[1]["air_temperature"] == 24.0

@@ -211,3 +211,43 @@ def test_node_rejects_bad_arguments(site):
     p, keep = facetcu.energy_parameters(sc.leaf_count, site["materials"], wavelengths=[550.0])
     with pytest.raises(ValueError):  # bands without their spectral irradiances
         m.facetebNode(p, DAY, site["sun"], site["lit"], None, T0)
+
+
+def test_node_sequence_writes_the_reference_records(reference, site, tmp_path):
+    """Three nodes through the FacetEB caller (morning, noon, night): each
+    node starts from the previous node's temperatures, the sun is rastered
+    per node, and the step records and faceteb.json are written."""
+    from streamsim_gb300 import faceteb
+    sc, m = site["scene"], site["model"]
+    rows = [dict(DAY, node=0, julian_time=172.375, shortwave=420.0, air_temperature=20.0),
+            dict(DAY, node=1, julian_time=172.5),
+            dict(NIGHT, node=2, julian_time=172.875)]
+    suns = {0: (60.0, 95.0), 1: (25.0, 170.0), 2: (100.0, 300.0)}
+    run = faceteb.Run(m, sc.leaf_count, site["materials"], site["mi"], site["tex"],
+                      wavelengths=BANDS, spectrum=site["spectrum"], window_width=150,
+                      coupling_iterations=6, temperature_tolerance=1e-7)
+    results, last = run.run(rows, lambda r: suns[r["node"]], output_dir=str(tmp_path),
+                            vertices=sc.vertices, progress=None)
+    assert [r["token"] for r in results] == ["DOY172_09-00", "DOY172_12-00", "DOY172_21-00"]
+    # the reference's chain on the same rasters
+    T = np.full(sc.surface_count, np.float32(20.0 + 273.15), np.float32)
+    for r in rows:
+        zen, az = suns[r["node"]]
+        lit = m.computeSunlitFraction(facetcu.sun_direction(zen, az))
+        theirs, _ = reference.faceteb_node(
+            sc.vertices, sc.leaf_count, site["graph"], lit, zen, az,
+            (r["air_temperature"], r["vapor_pressure"], r["pressure"], r["wind_speed"],
+             r["shortwave"], r["longwave"]), T, site["materials"], site["mi"], site["tex"], 0.0,
+            site["spectrum"], 0.8, 150, tolerance=1e-7, wavelengths=BANDS, coupling_iterations=6)
+        T = theirs["temperature"]
+        rec = np.fromfile(tmp_path / ".facet_steps" / f"energy_T={faceteb.time_token(r['julian_time'])}.bin",
+                          "<f4").reshape(sc.surface_count, 9 + len(BANDS))
+        assert np.max(np.abs(rec[:, 0] - theirs["temperature"])) <= 5e-3
+        assert np.array_equal(rec[:, 8], lit)
+    _compare(last, theirs, t_tol=5e-3)
+    comp = np.fromfile(tmp_path / ".facet_steps" / "components.bin", np.uint8)
+    assert comp.size == sc.facet_count and np.all(comp[sc.leaf_count:] == 1)
+    import json
+    doc = json.loads((tmp_path / "faceteb.json").read_text())
+    assert doc["time"] == "DOY172_21-00" and len(doc["temperature"]) == sc.surface_count
+    assert len(doc["vertexPositions"]) == 9 * sc.facet_count

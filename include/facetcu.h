@@ -592,6 +592,43 @@ int facetcu_faceteb_node(facetcu_context *ctx, const facetcu_energy_parameters *
                          const float *band_diffuse, facetcu_energy_fields *fields,
                          facetcu_energy_result *result);
 
+/* ---- sensor images (server.mjs:1127-1600, writeRadiosityTiffForAngle) ---- */
+/* The sensor of a project: image size, parallel or perspective projection,
+ * view angles, field of view, scene extent and sensor position.  Values
+ * that the reference reads as "not a number" take its defaults: pass NaN
+ * (position) or 0 (fov: 60, scene_x/scene_y: 1, sky_temperature: 250). */
+typedef struct {
+    uint32_t width, height;     /* sensor.x, sensor.y */
+    uint32_t perspective;       /* projection perspective / central / center */
+    double view_zenith;         /* vza, degrees */
+    double view_azimuth;        /* vaa, degrees clockwise from +X (north) toward +Z (east) */
+    double fov;                 /* vertical field of view (perspective), clamped to [0.1, 120] */
+    double scene_x, scene_y;    /* scene extent along x (north) and z (east), m */
+    double position[3];         /* positionX, positionY, height (m); any NaN: centre at 3000 m */
+    double sky_temperature;     /* K (max 120) for the thermal sky of perspective views */
+    uint32_t temperature_output; /* the values are temperatures (a FacetEB temperature image) */
+} facetcu_sensor;
+typedef struct {
+    uint32_t observed_pixels;   /* pixels of the observed (oblique) raster that see a facet */
+    uint32_t output_pixels;     /* pixels of the output image that see a facet */
+    double naming_zenith;       /* the view angles the output file is named by */
+    double naming_azimuth;
+} facetcu_image_info;
+/* Renders band_count images of per-side values (values[band][2F], host)
+ * seen by the sensor, on the context's geometry: the observed side of each
+ * facet, a z-buffered raster of side indices (barycentric test at pixel
+ * centres in double precision, the nearest depth wins and the first facet
+ * among equal depths), for a parallel sensor the nadir remap of that oblique
+ * raster onto the scene's ground grid, and for a perspective sensor the
+ * analytic sky where a pixel's ray looks up (wavelengths[band] in nm or um;
+ * the atmosphere table of the reference is not applied).  image[band][H][W]
+ * (float, NaN where nothing is seen) and side_index[H][W] (int32, -1; may be
+ * NULL) are host arrays. */
+int facetcu_render_sensor_image(facetcu_context *ctx, const facetcu_sensor *sensor,
+                                const float *values, uint32_t band_count,
+                                const float *wavelengths, float *image, int32_t *side_index,
+                                facetcu_image_info *info);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,7 +1,7 @@
 """Build libfacetcu.so (CUDA, sm_103a) in-tree with nvcc.
 
 Translation units are compiled in parallel and linked into
-streamsim_gb300/libfacetcu.so.  raster.cu, hemi.cu, lbvh.cu, spectral.cu and energy.cu are compiled with
+streamsim_gb300/libfacetcu.so.  raster.cu, hemi.cu, lbvh.cu, spectral.cu, energy.cu and image.cu are compiled with
 -fmad=false because their float results must round exactly like the
 reference's CPU code (no fused multiply-add); host code is compiled with
 -ffp-contract=off for the same reason.
@@ -19,7 +19,7 @@ LIB = os.path.join(HERE, "libfacetcu.so")
 CLI_SRC = os.path.join(HERE, "cli", "facetcu_main.cpp")
 CLI = os.path.join(HERE, "facetcu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-EXACT_FP = {"raster.cu", "hemi.cu", "lbvh.cu", "spectral.cu", "energy.cu"}
+EXACT_FP = {"raster.cu", "hemi.cu", "lbvh.cu", "spectral.cu", "energy.cu", "image.cu"}
 
 
 def nvcc():

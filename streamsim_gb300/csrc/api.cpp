@@ -59,6 +59,7 @@ struct facetcu_context {
     spectral::Tables spec;
     DeviceBuffer spec_io;
     DeviceBuffer eb_io, eb_tab;  // FacetEB node fields and per-material tables
+    DeviceBuffer img_io;         // sensor image scratch and outputs
     std::map<std::string, uint32_t> tuned;  // autotuned panel widths by problem key
     std::string gpu_name;                   // for the autotuner's key
 };
@@ -365,7 +366,7 @@ int facetcu_destroy(facetcu_context* ctx)
                             &ctx->sun_total, &ctx->sun_visible, &ctx->batch.x0, &ctx->batch.x1,
                             &ctx->batch.half, &ctx->batch.colstats, &ctx->batch.q,
                             &ctx->batch.corr, &ctx->batch.i8, &ctx->batch_inputs, &ctx->spec_io,
-                            &ctx->spec.dev, &ctx->eb_io, &ctx->eb_tab})
+                            &ctx->spec.dev, &ctx->eb_io, &ctx->eb_tab, &ctx->img_io})
         b->release();
     release_graphs(ctx->batch);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1999,6 +2000,85 @@ int facetcu_faceteb_node(facetcu_context* ctx, const facetcu_energy_parameters* 
             for (size_t s = 0; s < S; ++s) fields->radiosity[s] = lw[s] + sw[s];
         r.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (result) *result = r;
+        return FACETCU_OK;
+    });
+}
+
+}  // extern "C"
+
+// ---- sensor images ----------------------------------------------------------
+extern "C" {
+
+int facetcu_render_sensor_image(facetcu_context* ctx, const facetcu_sensor* sensor,
+                                const float* values, uint32_t band_count,
+                                const float* wavelengths, float* image, int32_t* side_index,
+                                facetcu_image_info* info)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "renderSensorImage()");
+        if (!ctx->facets) throw Error(FACETCU_LOGIC_ERROR, "renderSensorImage() needs geometry");
+        if (!sensor) throw Error(FACETCU_INVALID_ARGUMENT, "sensor is required");
+        if (band_count && (!values || !wavelengths || !image))
+            throw Error(FACETCU_INVALID_ARGUMENT, "values, wavelengths and image are required");
+        if (!band_count && !side_index)
+            throw Error(FACETCU_INVALID_ARGUMENT, "nothing to render: no bands and no side_index");
+        double nz = 0.0, na = 0.0;
+        const image::Camera cam = image::camera(*sensor, &nz, &na);
+        const size_t n = size_t(cam.width) * cam.height;
+        if (n > (size_t(1) << 28) || size_t(band_count) * n > (size_t(1) << 31))
+            throw Error(FACETCU_INVALID_ARGUMENT, "image too large");
+        for (uint32_t b = 0; b < band_count; ++b)
+            if (!std::isfinite(wavelengths[b]))
+                throw Error(FACETCU_INVALID_ARGUMENT, "wavelengths must be finite");
+        const uint32_t F = ctx->facets;
+        const size_t S = 2 * size_t(F);
+        cudaStream_t st = ctx->stream;
+        auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+        const size_t bytes = al(size_t(F) * 3 * image::kProjBytes) + al(size_t(F) * 4) +
+                             al(n * 8) + al(n * 4) * 2 + al(size_t(band_count) * S * 4) +
+                             al(size_t(band_count) * 4) + al(size_t(band_count) * n * 4) + al(8);
+        char* c = static_cast<char*>(ctx->img_io.reserve(bytes));
+        auto take = [&](size_t b) {
+            char* r = c;
+            c += al(b);
+            return r;
+        };
+        image::Scratch w{};
+        w.proj = take(size_t(F) * 3 * image::kProjBytes);
+        w.side = reinterpret_cast<int32_t*>(take(size_t(F) * 4));
+        w.zbuf = reinterpret_cast<unsigned long long*>(take(n * 8));
+        w.index = reinterpret_cast<int32_t*>(take(n * 4));
+        int32_t* d_sides = reinterpret_cast<int32_t*>(take(n * 4));
+        float* d_values = reinterpret_cast<float*>(take(size_t(band_count) * S * 4));
+        float* d_wl = reinterpret_cast<float*>(take(size_t(band_count) * 4));
+        float* d_image = reinterpret_cast<float*>(take(size_t(band_count) * n * 4));
+        uint32_t* d_counts = reinterpret_cast<uint32_t*>(take(8));
+        if (band_count) {
+            FCU_CHECK(cudaMemcpyAsync(d_values, values, size_t(band_count) * S * 4,
+                                      cudaMemcpyHostToDevice, st));
+            FCU_CHECK(cudaMemcpyAsync(d_wl, wavelengths, size_t(band_count) * 4,
+                                      cudaMemcpyHostToDevice, st));
+        }
+        const double sky_t = std::max(120.0, sensor->sky_temperature != 0.0 &&
+                                                     std::isfinite(sensor->sky_temperature)
+                                                 ? sensor->sky_temperature
+                                                 : 250.0);
+        image::render(cam, F, ctx->vertices.as<facetcu_vertex>(), d_values, band_count, S, d_wl,
+                      sensor->temperature_output != 0, sky_t, w, d_image, d_sides, d_counts, st);
+        uint32_t counts[2] = {0, 0};
+        if (band_count)
+            FCU_CHECK(cudaMemcpyAsync(image, d_image, size_t(band_count) * n * 4,
+                                      cudaMemcpyDeviceToHost, st));
+        if (side_index)
+            FCU_CHECK(cudaMemcpyAsync(side_index, d_sides, n * 4, cudaMemcpyDeviceToHost, st));
+        FCU_CHECK(cudaMemcpyAsync(counts, d_counts, 8, cudaMemcpyDeviceToHost, st));
+        FCU_CHECK(cudaStreamSynchronize(st));
+        if (info) {
+            info->observed_pixels = counts[0];
+            info->output_pixels = counts[1];
+            info->naming_zenith = nz;
+            info->naming_azimuth = na;
+        }
         return FACETCU_OK;
     });
 }

@@ -327,6 +327,28 @@ float shortwave_weighted_value(const float* values, uint32_t n, float fallback);
 float storage_coefficient(const facetcu_energy_surface& m, float time_step);
 }  // namespace energy
 
+// ---- sensor images (image.cu) ----------------------------------------------
+namespace image {
+struct Camera {
+    double right[3], up[3], out[3], forward[3], cam_pos[3];
+    double tan_half, min_x, max_y, range_x, range_y;
+    double orth_min_z, orth_max_x, orth_east, orth_north, scene_w, scene_d;
+    uint32_t width, height;
+    int32_t perspective;
+};
+struct Scratch {
+    void* proj;               // 3F projected vertices
+    int32_t* side;            // F observed sides
+    unsigned long long* zbuf; // W*H depth keys
+    int32_t* index;           // W*H facet indices, then observed sides
+};
+constexpr size_t kProjBytes = 32;  // one projected vertex
+Camera camera(const facetcu_sensor& s, double* naming_zenith, double* naming_azimuth);
+void render(const Camera& c, uint32_t F, const facetcu_vertex* V, const float* values,
+            uint32_t nb, size_t S, const float* wavelengths, bool as_temperature, double sky_t,
+            Scratch& w, float* image, int32_t* sides, uint32_t* counts, cudaStream_t s);
+}  // namespace image
+
 // ---- spectral optics (spectral.cu) ----------------------------------------
 namespace spectral {
 bool optical_wavelength(float wavelength);

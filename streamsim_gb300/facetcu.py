@@ -200,6 +200,30 @@ class EnergyResult(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Sensor(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("perspective", C.c_uint32),
+                ("view_zenith", C.c_double), ("view_azimuth", C.c_double), ("fov", C.c_double),
+                ("scene_x", C.c_double), ("scene_y", C.c_double), ("position", C.c_double * 3),
+                ("sky_temperature", C.c_double), ("temperature_output", C.c_uint32)]
+
+
+class ImageInfo(C.Structure):
+    _fields_ = [("observed_pixels", C.c_uint32), ("output_pixels", C.c_uint32),
+                ("naming_zenith", C.c_double), ("naming_azimuth", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def sensor(width=512, height=512, perspective=False, vza=0.0, vaa=0.0, fov=0.0, scene_x=1.0,
+           scene_y=1.0, position=(float("nan"),) * 3, sky_temperature=0.0,
+           temperature_output=False):
+    """A Sensor struct (the project's sensor block; 0 / NaN take the reference's
+    defaults)."""
+    return Sensor(width, height, 1 if perspective else 0, vza, vaa, fov, scene_x, scene_y,
+                  (C.c_double * 3)(*position), sky_temperature, 1 if temperature_output else 0)
+
+
 _vp = C.c_void_p
 _u32 = C.c_uint32
 _ctx = C.c_void_p
@@ -264,6 +288,8 @@ SIGNATURES.update({
 SIGNATURES["facetcu_autotune_batched"] = (C.c_int, [_ctx, C.POINTER(BatchConfig)] + [_vp] * 7 +
                                           [C.c_char_p, C.POINTER(_u32)])
 SIGNATURES["facetcu_scene_batch"] = (C.c_int, [_ctx, _vp, _u32, _vp, C.POINTER(GraphDiagnostics)])
+SIGNATURES["facetcu_render_sensor_image"] = (C.c_int, [_ctx, C.POINTER(Sensor), _vp, _u32, _vp, _vp,
+                                                      _vp, C.POINTER(ImageInfo)])
 SIGNATURES.update({
     "facetcu_shortwave_windows": (C.c_int, [C.POINTER(ShortwaveSpectrum), C.c_float, C.c_float, _vp,
                                             _u32, _vp, _u32, C.POINTER(_u32), _vp, _vp]),
@@ -822,6 +848,26 @@ class FacetrtCuda:
         if "band_output" in out:
             out["band_output"] = out["band_output"].reshape(parameters.band_count, S)
         return out, res.as_dict()
+
+    # -- sensor images ---------------------------------------------------------
+    def renderSensorImage(self, sensor_struct, values, wavelengths):
+        """Images of per-side values seen by a sensor: (image (bands, H, W)
+        float32, side index (H, W) int32, info dict)."""
+        vals = _f32(values).reshape(-1, 2 * self.facet_count) if np.size(values) else \
+            np.zeros((0, 2 * self.facet_count), np.float32)
+        wl = _f32(wavelengths).ravel()
+        nb = len(vals)
+        if wl.size < nb:
+            raise ValueError("one wavelength per band is required")
+        W = sensor_struct.width or 512
+        H = sensor_struct.height or 512
+        img = np.zeros((nb, H, W), np.float32)
+        idx = np.zeros((H, W), np.int32)
+        info = ImageInfo()
+        self._check(self.lib.facetcu_render_sensor_image(
+            self.h, C.byref(sensor_struct), _ptr(vals) if nb else None, nb,
+            _ptr(wl) if nb else None, _ptr(img) if nb else None, _ptr(idx), C.byref(info)))
+        return img, idx, info.as_dict()
 
     # -- learned warm start -------------------------------------------------
     def mlpReset(self, seed=1):

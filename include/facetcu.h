@@ -397,8 +397,10 @@ const char *facetcu_host_last_error(void);
  * (:1782-1840).  Prints `PROGRESS\t<int>\t<text>` lines and
  * `RESULT\t<path>` to stdout; on failure `facetrt: <message>` to stderr and
  * returns 1 (0 on success).  output_file NULL or "" writes facetrt.json next
- * to the input.  shader_directory is accepted and unused.  project.json
- * inputs are refused (scene and material ingestion is not built). */
+ * to the input.  shader_directory is accepted and unused.  An XML project
+ * (Input.xml) runs loadProjectScene's scene and the spectral band loop of
+ * runGpu (facetcu_project_load, facetcu_solve_bands); project.json inputs
+ * are refused (their XML view is built by the reference's Node backend). */
 int facetcu_run_facetrt_core(const char *input_path, const char *shader_directory,
                              const char *output_file);
 
@@ -628,6 +630,49 @@ int facetcu_render_sensor_image(facetcu_context *ctx, const facetcu_sensor *sens
                                 const float *values, uint32_t band_count,
                                 const float *wavelengths, float *image, int32_t *side_index,
                                 facetcu_image_info *info);
+
+/* ---- XML projects (scene and material ingestion) ------------------------ */
+/* A HiStream XML project (the reference's Input.xml) read as
+ * loadProjectScene and facetRTParametersFromInput do
+ * (facetrtcore.cpp:2038-3025): objects from OBJ files (groups bound to
+ * materials by mesh name) or cubes, placed from position files (x y z
+ * [scale [rotation]]) and clipped to the scene domain, then a flat ground
+ * grid; materials from custom, file, PROSPECT and BSM spectra (the models'
+ * optipar.txt beside the sun spectrum), thermal blocks, soil sets and
+ * surface-energy blocks.  DEM files and physical textures need GDAL and are
+ * refused with the reference's messages.  Host only; errors through
+ * facetcu_host_last_error(). */
+typedef struct facetcu_project facetcu_project;
+typedef struct {
+    uint32_t facet_count;
+    uint32_t leaf_facet_count;      /* object facets come first, the ground last */
+    uint32_t material_count;        /* Scene::materials (the ground's is the last) */
+    uint32_t band_count;
+    float sun_zenith, sun_azimuth;  /* degrees */
+    uint32_t periodic_neighbor_count;
+    float periodic_size_x, periodic_size_z;
+    uint32_t raster_size, raster_layers;
+    float background_angular_strength;
+    float minimum[3], maximum[3];
+    float sky_temperature;
+    uint32_t accelerated_solver;
+} facetcu_project_info;
+int facetcu_project_load(const char *path, facetcu_project **project);
+void facetcu_project_release(facetcu_project *project);
+int facetcu_project_get_info(const facetcu_project *project, facetcu_project_info *info);
+/* vertices[3F], material_indices[F], texture_factors[F] (any may be NULL) */
+int facetcu_project_get_geometry(const facetcu_project *project, facetcu_vertex *vertices,
+                                 uint32_t *material_indices, float *texture_factors);
+/* material index < material_count, or material_count for the parameters'
+ * object surface and material_count + 1 for the ground; the pointers stay
+ * valid while the project lives.  output_component: 0 unknown, 1 soil,
+ * 2 vegetation, 3 building, 4 PV, 5 water. */
+int facetcu_project_get_material(const facetcu_project *project, uint32_t index,
+                                 facetcu_energy_surface *surface, uint32_t *output_component);
+/* The project's FacetRTParameters and scene fields as spectral parameters
+ * for facetcu_spectral_optics / facetcu_solve_bands. */
+int facetcu_project_spectral_parameters(const facetcu_project *project,
+                                        facetcu_spectral_parameters *parameters);
 
 #ifdef __cplusplus
 }

@@ -36,6 +36,9 @@ SRC = os.path.join(OUT, "facetrt_ref.cpp")
 LIB = os.path.join(OUT, "libfacetrt_ref.so")
 REFERENCE = os.environ.get("FACETRT_REFERENCE_ROOT", "/root/reference")
 FACETRT = os.path.join(REFERENCE, "models", "histream", "src", "facetrt")
+BASE = os.path.join(REFERENCE, "models", "histream", "src", "base")
+PROJECT_SRC = os.path.join(OUT, "project_ref.cpp")
+PROJECT_LIB = os.path.join(OUT, "libproject_ref.so")
 
 RANGES = [
     ("facetrt_vulkan.h", 15, 62, "namespace facetvk {", "}"),
@@ -126,9 +129,96 @@ def compile_lib():
     subprocess.run(cmd, check=True)
 
 
+# The project loader (loadProjectScene, facetrtcore.cpp:2038-3025, for the
+# reference's XML input) with the CPU span it builds on and the spectral
+# models it calls (Compo::resolveSpectrals with fluspect and bsm,
+# compo.cpp; Utils::expint, utils.cpp; their types from structs.h and
+# structs_cg.h).  GDAL (DEM and texture files) and the project.json view
+# (nlohmann::json) are not available here: oracle/ref_project_stubs.inc
+# declares stand-ins that fail loudly, so projects using them are refused.
+PROJECT_RANGES = [
+    ("base/structs.h", 122, 128, None, None),
+    ("base/structs.h", 148, 186, None, None),
+    ("base/structs.h", 195, 206, None, None),
+    ("base/structs_cg.h", 45, 48, None, None),
+    ("@", 0, 0, "declarations", None),
+    ("base/utils.cpp", 459, 471, None, None),
+    ("base/compo.cpp", 15, 90, None, None),
+    ("base/compo.cpp", 152, 341, None, None),
+    ("base/compo.cpp", 436, 479, None, None),
+    ("facetrt/facetrt_vulkan.h", 15, 62, "namespace facetvk {", "}"),
+    ("facetrt/facetrtcore.cpp", 39, 53, "namespace {", None),
+    ("facetrt/facetrtcore.cpp", 74, 630, None, None),
+    ("@", 0, 0, "texture", None),
+    ("facetrt/facetrtcore.cpp", 703, 1620, None, None),
+    ("@", 0, 0, "view", None),
+    ("facetrt/facetrtcore.cpp", 2038, 3025, None, "}  // namespace"),
+]
+PROJECT_ANCHORS = [
+    ("base/structs.h", 122, "enum class spectralType"),
+    ("base/structs.h", 148, "struct OptCoeff"),
+    ("base/structs.h", 195, "struct SpectralXml"),
+    ("base/structs_cg.h", 45, "struct  Spectral{"),
+    ("base/utils.cpp", 459, "float Utils::expint(float x)"),
+    ("base/compo.cpp", 15, "namespace {"),
+    ("base/compo.cpp", 152, "float Compo::calctav(float alfa,float nr)"),
+    ("base/compo.cpp", 275, "std::vector<Spectral> Compo::resolveSpectrals("),
+    ("base/compo.cpp", 436, "void Compo::bsm(OptCoeff bsmCoeff,BSMParam bsm,std::vector<Spectral>& spectrals){"),
+    ("facetrt/facetrtcore.cpp", 2038, "std::string readTextFile(const std::string& path)"),
+    ("facetrt/facetrtcore.cpp", 2880, "Scene loadProjectScene(const std::string& inputFile)"),
+    ("facetrt/facetrtcore.cpp", 3025, "}"),
+]
+
+
+def generate_project():
+    src = os.path.join(REFERENCE, "models", "histream", "src")
+    read = lambda name: open(os.path.join(src, name), encoding="utf-8").read().split("\n")
+    cache = {}
+    for name, line, text in PROJECT_ANCHORS:
+        lines = cache.setdefault(name, read(name))
+        if not lines[line - 1].lstrip().startswith(text):
+            raise SystemExit(f"build_ref: {name}:{line} does not start with {text!r}")
+    with open(os.path.join(HERE, "ref_project_stubs.inc"), encoding="utf-8") as f:
+        stubs = f.read()
+    sections = {}
+    current = None
+    for line in stubs.split("\n"):
+        if line.startswith("//@@ "):
+            current = line[5:].strip()
+            sections[current] = []
+        elif current:
+            sections[current].append(line)
+    parts = [PRELUDE, "#define N1 2001"]
+    for name, lo, hi, before, after in PROJECT_RANGES:
+        if name == "@":
+            parts.extend(sections[before])
+            continue
+        lines = cache.setdefault(name, read(name))
+        if before:
+            parts.append(before)
+        parts.append(f"// ---- {name}:{lo}-{hi}")
+        parts.extend(lines[lo - 1:hi])
+        if after:
+            parts.append(after)
+    with open(os.path.join(HERE, "ref_project_shim.inc"), encoding="utf-8") as f:
+        parts.append(f.read())
+    os.makedirs(OUT, exist_ok=True)
+    with open(PROJECT_SRC, "w", encoding="utf-8") as f:
+        f.write("\n".join(parts) + "\n")
+
+
+def compile_project():
+    cmd = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-fPIC", "-shared",
+           "-w", PROJECT_SRC, "-o", PROJECT_LIB]
+    subprocess.run(cmd, check=True)
+
+
 def main():
     if os.path.isdir(FACETRT):
         generate()
+        # the project loader oracle is used by CPU tests only, here
+        generate_project()
+        compile_project()
     elif not os.path.exists(SRC):
         print("build_ref: reference tree absent and no generated source; skipping",
               file=sys.stderr)

@@ -601,3 +601,87 @@ class Reference:
 
 def reference_available():
     return os.path.exists(REF_LIB)
+
+
+PROJECT_LIB = os.path.join(HERE, "_ref", "libproject_ref.so")
+
+
+class ReferenceProject:
+    """The reference's own loadProjectScene / facetRTParametersFromInput
+    (compiled by oracle/build_ref.py into oracle/_ref/libproject_ref.so;
+    built only where the reference tree is present)."""
+
+    HEAD = 24
+
+    def __init__(self, path=PROJECT_LIB):
+        self.lib = C.CDLL(path)
+        self.lib.ref_project_last_error.restype = C.c_char_p
+        self.lib.ref_load_project.argtypes = [C.c_char_p, C.c_void_p] + [C.c_void_p] * 6
+        self.lib.ref_project_free.argtypes = [C.c_void_p]
+
+    def _take(self, ptr, n, dtype):
+        ct = C.c_float if dtype == np.float32 else C.c_uint32
+        a = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ct)), (max(n, 1),))[:n].copy()
+        self.lib.ref_project_free(ptr)
+        return a
+
+    @classmethod
+    def unpack(cls, packed, count):
+        """Split packed surfaces into dicts of their fields."""
+        names = ["tir_reflectance", "tir_transmittance", "sunlit_temperature",
+                 "shaded_temperature", "surface_resistance", "specific_heat", "density",
+                 "thermal_conductivity", "soil_moisture", "heat_capacity_per_area",
+                 "soil_temperature_method", "photovoltaic", "vegetation", "pv_eta25", "pv_gamma",
+                 "pv_bifaciality", "convective_scale", "output_component", "texture_strength",
+                 "texture_repeat"]
+        out, at = [], 0
+        for _ in range(count):
+            h = packed[at:at + cls.HEAD]
+            nr, nt, ner, net = (int(x) for x in h[:4])
+            d = dict(zip(names, h[4:].tolist()))
+            v = packed[at + cls.HEAD:]
+            d["reflectance"], v = v[:nr], v[nr:]
+            d["transmittance"], v = v[:nt], v[nt:]
+            d["energy_reflectance"], v = v[:ner], v[ner:]
+            d["energy_transmittance"] = v[:net]
+            out.append(d)
+            at += cls.HEAD + nr + nt + ner + net
+        return out
+
+    def load(self, path):
+        info = np.zeros(24, np.float32)
+        ptrs = [C.c_void_p() for _ in range(6)]
+        rc = self.lib.ref_load_project(os.fsencode(path), info.ctypes.data,
+                                       *[C.byref(p) for p in ptrs])
+        if rc != 0:
+            raise RuntimeError(self.lib.ref_project_last_error().decode())
+        F = int(info[0])
+        M = int(info[16])
+        nb = int(info[17])
+        vertices = self._take(ptrs[0], 18 * F, np.float32).reshape(3 * F, 6)
+        mi = self._take(ptrs[1], F, np.uint32)
+        # sizes of the packed blocks are only known by walking them
+        raw_m = C.cast(ptrs[2], C.POINTER(C.c_float))
+        raw_p = C.cast(ptrs[3], C.POINTER(C.c_float))
+
+        def walk(raw, count):
+            at = 0
+            for _ in range(count):
+                nr, nt, ner, net = (int(raw[at + k]) for k in range(4))
+                at += self.HEAD + nr + nt + ner + net
+            return at
+        nm, npar = walk(raw_m, M), walk(raw_p, 2)
+        materials = self.unpack(self._take(ptrs[2], nm, np.float32), M)
+        params = self.unpack(self._take(ptrs[3], npar, np.float32), 2)
+        wavelengths = self._take(ptrs[4], nb, np.float32)
+        tex = self._take(ptrs[5], F if info[20] else 0, np.float32)
+        names = ["facet_count", "leaf_facet_count", "sun_zenith", "sun_azimuth",
+                 "periodic_neighbor_count", "periodic_size_x", "periodic_size_z", "raster_size",
+                 "raster_layers", "background_angular_strength"]
+        d = dict(zip(names, info[:10].tolist()))
+        d.update(minimum=info[10:13].tolist(), maximum=info[13:16].tolist(),
+                 material_count=M, band_count=nb, sky_temperature=float(info[18]),
+                 accelerated_solver=int(info[19]))
+        return dict(info=d, vertices=vertices, material_indices=mi, materials=materials,
+                    object=params[0], ground=params[1], wavelengths=wavelengths,
+                    texture_factors=tex)

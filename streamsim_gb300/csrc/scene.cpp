@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "facetcu.h"
+#include "host_scene.h"
 
 namespace {
 
@@ -40,9 +41,8 @@ thread_local std::string g_host_error;
 // The message facetcu_host_last_error() reports for host-only entry points.
 void facetcu_set_host_error(const std::string& message) { g_host_error = message; }
 
-namespace {
-
-using V3 = std::array<float, 3>;
+namespace facetcu {
+namespace host {
 
 V3 sub(const V3& a, const V3& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2]}; }
 V3 scaled(const V3& v, float s) { return {v[0] * s, v[1] * s, v[2] * s}; }
@@ -57,21 +57,6 @@ V3 unit(const V3& v)
     if (!(length > 1.0e-8f)) throw std::runtime_error("Zero-length direction or degenerate triangle");
     return scaled(v, 1.0f / length);
 }
-
-constexpr uint32_t kSoilGrid = 48;        // facetrtcore.cpp:83
-constexpr float kBeam = 700.0f;           // facetrtcore.cpp:84
-constexpr float kSky = 100.0f;            // facetrtcore.cpp:85
-constexpr uint32_t kSweeps = 64;          // facetrtcore.cpp:82
-constexpr uint32_t kRaster = 1024;        // facetrtcore.cpp:74
-constexpr uint32_t kLayers = 64;          // facetrtcore.cpp:75
-
-struct HostScene {
-    std::vector<facetcu_vertex> vertices;
-    std::vector<uint32_t> material;
-    uint32_t leaf = 0;
-    V3 lo{}, hi{};
-    uint32_t facets() const { return uint32_t(vertices.size() / 3); }
-};
 
 bool push_triangle(HostScene& sc, const V3& a, const V3& b, const V3& c, uint32_t material)
 {
@@ -98,6 +83,79 @@ int obj_position(const std::string& token, size_t count)
         throw std::runtime_error("OBJ position index is out of range");
     return int(index);
 }
+
+// ---- the run --------------------------------------------------------------
+double ms_between(Clock::time_point a, Clock::time_point b)
+{
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+void progress(int value, const std::string& stage)
+{
+    std::cout << "PROGRESS\t" << value << '\t' << stage << std::endl;
+}
+
+Context::Context()
+{
+    if (facetcu_create(&ctx) != FACETCU_OK) throw std::bad_alloc();
+}
+Context::~Context() { facetcu_release(ctx); }
+void Context::check(int status) const
+{
+    if (status != FACETCU_OK) throw std::runtime_error(facetcu_last_error(ctx));
+}
+
+void write_web_result(const std::string& file, const HostScene& sc, const RunOutput& r)
+{
+    std::ofstream out(file, std::ios::binary);
+    if (!out) throw std::runtime_error("Cannot write web result: " + file);
+    out << std::setprecision(9) << "{\n"
+        << "  \"backend\": \"" << r.backend << "\",\n"
+        << "  \"quantity\": \"" << r.quantity << "\",\n"
+        << "  \"units\": \"" << r.units << "\",\n"
+        << "  \"facetCount\": " << sc.facets() << ",\n"
+        << "  \"leafFacetCount\": " << sc.leaf << ",\n"
+        << "  \"vertexPositions\": [";
+    for (size_t i = 0; i < sc.vertices.size(); ++i) {
+        const float* p = sc.vertices[i].position;
+        out << (i ? "," : "") << p[0] << ',' << p[1] << ',' << p[2];
+    }
+    out << "],\n"
+        << "  \"graph\": {\"directedEdges\":" << r.graph.directed_edge_count
+        << ",\"closureError\":" << r.graph.max_closure_error
+        << ",\"fragmentOverflow\":" << r.graph.fragment_overflow
+        << ",\"hashOverflow\":" << r.graph.hash_overflow << "},\n"
+        << "  \"timing\": {\"totalMs\":" << r.total_ms << ",\"visibilityMs\":" << r.visibility_ms
+        << ",\"sunlightMs\":" << r.sunlight_ms << ",\"solveMs\":" << r.solve_ms << "},\n"
+        << "  \"iterations\": " << r.iterations << ",\n"
+        << "  \"maxDelta\": " << r.max_delta << ",\n";
+    auto array = [&out](const char* name, const std::vector<float>& v, bool comma) {
+        out << "  \"" << name << "\": [";
+        for (size_t i = 0; i < v.size(); ++i) out << (i ? "," : "") << v[i];
+        out << ']' << (comma ? "," : "") << '\n';
+    };
+    array("wavelengths", r.wavelengths, true);
+    array("sunlit", r.sunlit, true);
+    array("radiosity", r.radiosity, true);
+    array("lightEnhancement", r.enhancement, !r.band_radiosity.empty());
+    if (!r.band_radiosity.empty()) array("bandRadiosity", r.band_radiosity, false);
+    out << "}\n";
+    if (!out) throw std::runtime_error("Cannot write web result: " + file);
+}
+
+}  // namespace host
+}  // namespace facetcu
+
+namespace {
+
+using namespace facetcu::host;
+
+constexpr uint32_t kSoilGrid = 48;        // facetrtcore.cpp:83
+constexpr float kBeam = 700.0f;           // facetrtcore.cpp:84
+constexpr float kSky = 100.0f;            // facetrtcore.cpp:85
+constexpr uint32_t kSweeps = 64;          // facetrtcore.cpp:82
+constexpr uint32_t kRaster = 1024;        // facetrtcore.cpp:74
+constexpr uint32_t kLayers = 64;          // facetrtcore.cpp:75
 
 HostScene load_tree_with_soil(const std::string& path)
 {
@@ -193,42 +251,6 @@ void make_optics(const facetcu_vertex* v, uint32_t facets, uint32_t leaf, const 
     }
 }
 
-// ---- the run --------------------------------------------------------------
-struct RunOutput {
-    std::string backend = "CUDA GPU";
-    std::string quantity = "hemispherical radiosity";
-    std::string units = "W m-2";
-    facetcu_graph_diagnostics graph{};
-    std::vector<float> radiosity, sunlit, enhancement, wavelengths, band_radiosity;
-    uint32_t iterations = 0;
-    float max_delta = 0.0f;
-    double total_ms = 0, visibility_ms = 0, sunlight_ms = 0, solve_ms = 0;
-};
-
-using Clock = std::chrono::steady_clock;
-double ms_between(Clock::time_point a, Clock::time_point b)
-{
-    return std::chrono::duration<double, std::milli>(b - a).count();
-}
-
-void progress(int value, const std::string& stage)
-{
-    std::cout << "PROGRESS\t" << value << '\t' << stage << std::endl;
-}
-
-struct Context {
-    facetcu_context* ctx = nullptr;
-    Context()
-    {
-        if (facetcu_create(&ctx) != FACETCU_OK) throw std::bad_alloc();
-    }
-    ~Context() { facetcu_release(ctx); }
-    void check(int status) const
-    {
-        if (status != FACETCU_OK) throw std::runtime_error(facetcu_last_error(ctx));
-    }
-};
-
 RunOutput run_gpu(const HostScene& sc)
 {
     RunOutput r;
@@ -280,44 +302,6 @@ RunOutput run_gpu(const HostScene& sc)
     r.total_ms = ms_between(t_begin, t_end);
     progress(100, "CUDA GPU complete");
     return r;
-}
-
-void write_web_result(const std::string& file, const HostScene& sc, const RunOutput& r)
-{
-    std::ofstream out(file, std::ios::binary);
-    if (!out) throw std::runtime_error("Cannot write web result: " + file);
-    out << std::setprecision(9) << "{\n"
-        << "  \"backend\": \"" << r.backend << "\",\n"
-        << "  \"quantity\": \"" << r.quantity << "\",\n"
-        << "  \"units\": \"" << r.units << "\",\n"
-        << "  \"facetCount\": " << sc.facets() << ",\n"
-        << "  \"leafFacetCount\": " << sc.leaf << ",\n"
-        << "  \"vertexPositions\": [";
-    for (size_t i = 0; i < sc.vertices.size(); ++i) {
-        const float* p = sc.vertices[i].position;
-        out << (i ? "," : "") << p[0] << ',' << p[1] << ',' << p[2];
-    }
-    out << "],\n"
-        << "  \"graph\": {\"directedEdges\":" << r.graph.directed_edge_count
-        << ",\"closureError\":" << r.graph.max_closure_error
-        << ",\"fragmentOverflow\":" << r.graph.fragment_overflow
-        << ",\"hashOverflow\":" << r.graph.hash_overflow << "},\n"
-        << "  \"timing\": {\"totalMs\":" << r.total_ms << ",\"visibilityMs\":" << r.visibility_ms
-        << ",\"sunlightMs\":" << r.sunlight_ms << ",\"solveMs\":" << r.solve_ms << "},\n"
-        << "  \"iterations\": " << r.iterations << ",\n"
-        << "  \"maxDelta\": " << r.max_delta << ",\n";
-    auto array = [&out](const char* name, const std::vector<float>& v, bool comma) {
-        out << "  \"" << name << "\": [";
-        for (size_t i = 0; i < v.size(); ++i) out << (i ? "," : "") << v[i];
-        out << ']' << (comma ? "," : "") << '\n';
-    };
-    array("wavelengths", r.wavelengths, true);
-    array("sunlit", r.sunlit, true);
-    array("radiosity", r.radiosity, true);
-    array("lightEnhancement", r.enhancement, !r.band_radiosity.empty());
-    if (!r.band_radiosity.empty()) array("bandRadiosity", r.band_radiosity, false);
-    out << "}\n";
-    if (!out) throw std::runtime_error("Cannot write web result: " + file);
 }
 
 bool has_obj_extension(const std::filesystem::path& p)
@@ -394,11 +378,14 @@ int facetcu_run_facetrt_core(const char* input_path, const char* shader_director
         const std::string input = input_path ? input_path : "";
         if (input.empty()) throw std::invalid_argument("FacetRT requires project.json");
         const std::filesystem::path in(input);
-        if (!has_obj_extension(in))
-            throw std::runtime_error(
-                "project.json scenes are not read by the CUDA backend; pass the scene OBJ");
         std::string result_file = output_file ? output_file : "";
         if (result_file.empty()) result_file = (in.parent_path() / "facetrt.json").lexically_normal().string();
+        if (!has_obj_extension(in)) {
+            // an XML project (the reference's Input.xml): loadProjectScene
+            facetcu::project::run_facetrt(input, result_file);
+            std::cout << "RESULT\t" << result_file << std::endl;
+            return 0;
+        }
         const HostScene sc = load_tree_with_soil(input);
         const char* env = std::getenv("HISTREAM_FACET_BACKEND");
         if (env && std::string(env) == "cpu")

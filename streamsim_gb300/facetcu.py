@@ -224,6 +224,22 @@ def sensor(width=512, height=512, perspective=False, vza=0.0, vaa=0.0, fov=0.0, 
                   (C.c_double * 3)(*position), sky_temperature, 1 if temperature_output else 0)
 
 
+class ProjectInfo(C.Structure):
+    _fields_ = [("facet_count", C.c_uint32), ("leaf_facet_count", C.c_uint32),
+                ("material_count", C.c_uint32), ("band_count", C.c_uint32),
+                ("sun_zenith", C.c_float), ("sun_azimuth", C.c_float),
+                ("periodic_neighbor_count", C.c_uint32), ("periodic_size_x", C.c_float),
+                ("periodic_size_z", C.c_float), ("raster_size", C.c_uint32),
+                ("raster_layers", C.c_uint32), ("background_angular_strength", C.c_float),
+                ("minimum", C.c_float * 3), ("maximum", C.c_float * 3),
+                ("sky_temperature", C.c_float), ("accelerated_solver", C.c_uint32)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["minimum"], d["maximum"] = list(self.minimum), list(self.maximum)
+        return d
+
+
 _vp = C.c_void_p
 _u32 = C.c_uint32
 _ctx = C.c_void_p
@@ -288,6 +304,15 @@ SIGNATURES.update({
 SIGNATURES["facetcu_autotune_batched"] = (C.c_int, [_ctx, C.POINTER(BatchConfig)] + [_vp] * 7 +
                                           [C.c_char_p, C.POINTER(_u32)])
 SIGNATURES["facetcu_scene_batch"] = (C.c_int, [_ctx, _vp, _u32, _vp, C.POINTER(GraphDiagnostics)])
+SIGNATURES.update({
+    "facetcu_project_load": (C.c_int, [C.c_char_p, C.POINTER(_vp)]),
+    "facetcu_project_release": (None, [_vp]),
+    "facetcu_project_get_info": (C.c_int, [_vp, C.POINTER(ProjectInfo)]),
+    "facetcu_project_get_geometry": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "facetcu_project_get_material": (C.c_int, [_vp, _u32, C.POINTER(EnergySurfaceParameters),
+                                               C.POINTER(_u32)]),
+    "facetcu_project_spectral_parameters": (C.c_int, [_vp, C.POINTER(SpectralParameters)]),
+})
 SIGNATURES["facetcu_render_sensor_image"] = (C.c_int, [_ctx, C.POINTER(Sensor), _vp, _u32, _vp, _vp,
                                                       _vp, C.POINTER(ImageInfo)])
 SIGNATURES.update({
@@ -547,6 +572,75 @@ def shortwave_windows(total_shortwave, cos_zenith, direct=None, diffuse=None,
     win = np.array([[w.direct_normal, w.diffuse, w.energy_band] for w in arr[:count.value]],
                    np.float64).reshape(-1, 3)
     return win, arr, bd, bf
+
+
+def _floats(ptr, n):
+    return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_float)), (n,)).copy() if n else \
+        np.zeros(0, np.float32)
+
+
+class Project:
+    """A HiStream XML project read by the library (facetcu_project_load):
+    the scene (vertices (3F, 6), material indices, texture factors), its
+    materials and the FacetRT parameters."""
+
+    def __init__(self, path):
+        self.lib = load()
+        self.h = C.c_void_p()
+        rc = self.lib.facetcu_project_load(os.fsencode(path), C.byref(self.h))
+        _host_check(rc)
+        info = ProjectInfo()
+        self.lib.facetcu_project_get_info(self.h, C.byref(info))
+        self.info = info.as_dict()
+        F = info.facet_count
+        self.vertices = np.zeros((3 * F, 6), np.float32)
+        self.material_indices = np.zeros(F, np.uint32)
+        self.texture_factors = np.zeros(F, np.float32)
+        self.lib.facetcu_project_get_geometry(self.h, _ptr(self.vertices),
+                                              _ptr(self.material_indices),
+                                              _ptr(self.texture_factors))
+
+    def material(self, index):
+        """Material `index` (material_count: the parameters' object surface,
+        material_count + 1: their ground) as a dict of its fields."""
+        m = EnergySurfaceParameters()
+        comp = _u32(0)
+        self._check(self.lib.facetcu_project_get_material(self.h, index, C.byref(m),
+                                                          C.byref(comp)))
+        o = m.optics
+        d = {"reflectance": _floats(o.reflectance, o.reflectance_count),
+             "transmittance": _floats(o.transmittance, o.transmittance_count),
+             "energy_reflectance": _floats(m.energy_reflectance, m.energy_reflectance_count),
+             "energy_transmittance": _floats(m.energy_transmittance,
+                                             m.energy_transmittance_count),
+             "tir_reflectance": o.tir_reflectance, "tir_transmittance": o.tir_transmittance,
+             "sunlit_temperature": o.sunlit_temperature,
+             "shaded_temperature": o.shaded_temperature, "output_component": comp.value}
+        for k, _ in EnergySurfaceParameters._fields_[5:]:
+            d[k] = getattr(m, k)
+        return d
+
+    def spectral_parameters(self):
+        """SpectralParameters for spectralOptics / solveBands (valid while
+        this project lives)."""
+        p = SpectralParameters()
+        self._check(self.lib.facetcu_project_spectral_parameters(self.h, C.byref(p)))
+        return p
+
+    def _check(self, rc):
+        if rc != OK:
+            raise ValueError("invalid project request")
+
+    def close(self):
+        if self.h:
+            self.lib.facetcu_project_release(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def device_count():

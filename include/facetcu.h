@@ -399,8 +399,8 @@ const char *facetcu_host_last_error(void);
  * returns 1 (0 on success).  output_file NULL or "" writes facetrt.json next
  * to the input.  shader_directory is accepted and unused.  An XML project
  * (Input.xml) runs loadProjectScene's scene and the spectral band loop of
- * runGpu (facetcu_project_load, facetcu_solve_bands); project.json inputs
- * are refused (their XML view is built by the reference's Node backend). */
+ * runGpu (facetcu_project_load, facetcu_solve_bands); a project.json
+ * through its XML view. */
 int facetcu_run_facetrt_core(const char *input_path, const char *shader_directory,
                              const char *output_file);
 
@@ -640,7 +640,8 @@ int facetcu_render_sensor_image(facetcu_context *ctx, const facetcu_sensor *sens
  * grid; materials from custom, file, PROSPECT and BSM spectra (the models'
  * optipar.txt beside the sun spectrum), thermal blocks, soil sets and
  * surface-energy blocks.  DEM files and physical textures need GDAL and are
- * refused with the reference's messages.  Host only; errors through
+ * refused with the reference's messages.  A project.json is read through
+ * its XML view (facetcu_project_xml_view).  Host only; errors through
  * facetcu_host_last_error(). */
 typedef struct facetcu_project facetcu_project;
 typedef struct {
@@ -669,6 +670,14 @@ int facetcu_project_get_geometry(const facetcu_project *project, facetcu_vertex 
  * 2 vegetation, 3 building, 4 PV, 5 water. */
 int facetcu_project_get_material(const facetcu_project *project, uint32_t index,
                                  facetcu_energy_surface *surface, uint32_t *output_component);
+/* The XML view of a project.json (facetInputView, facetrtcore.cpp:1888-2036,
+ * over projectjson.cpp's accessors): the form facetcu_project_load reads a
+ * project.json in.  Files are resolved against the project's folder, the
+ * runtime "defined" folder (sun spectra, optipar.txt) is ./defined.
+ * *length = the view's length; buffer (capacity bytes, NUL-terminated) may
+ * be NULL to ask for the length. */
+int facetcu_project_xml_view(const char *path, char *buffer, uint64_t capacity,
+                             uint64_t *length);
 /* The project's FacetRTParameters and scene fields as spectral parameters
  * for facetcu_spectral_optics / facetcu_solve_bands. */
 int facetcu_project_spectral_parameters(const facetcu_project *project,

@@ -64,6 +64,8 @@ struct Context {
 }  // namespace host
 
 namespace project {
+// The XML view of a project.json (facetInputView, facetrtcore.cpp:1888-2036).
+std::string xml_view(const std::string& path);
 // The eFacetRT run of an XML project (runFacetRTCore with loadProjectScene
 // and facetRTParametersFromInput, facetrtcore.cpp:3116-3161); writes
 // result_file.  Throws on failure.

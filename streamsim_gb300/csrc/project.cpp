@@ -22,8 +22,8 @@
 //
 // Not supported, as GDAL is not available: DEM height fields and physical
 // reflectance textures (both fail with the reference's message).  A
-// project.json is first turned into this XML by the reference's Node
-// backend / facetInputView; only the XML form is read here.
+// project.json is read through its XML view (project_json.cpp), as the
+// reference's readTextFile does.
 #include <algorithm>
 #include <array>
 #include <cctype>
@@ -265,10 +265,7 @@ std::string read_text(const std::string& path)
     std::string ext = std::filesystem::path(path).extension().string();
     std::transform(ext.begin(), ext.end(), ext.begin(),
                    [](unsigned char ch) { return char(std::tolower(ch)); });
-    if (ext == ".json")
-        throw std::runtime_error(
-            "project.json is read through its XML view (the reference's facetInputView); "
-            "pass the project's Input.xml: " + path);
+    if (ext == ".json") return xml_view(path);
     std::ifstream in(path, std::ios::binary);
     if (!in) throw std::runtime_error("Cannot open HiStream input: " + path);
     return {std::istreambuf_iterator<char>(in), std::istreambuf_iterator<char>()};

@@ -312,6 +312,7 @@ SIGNATURES.update({
     "facetcu_project_get_material": (C.c_int, [_vp, _u32, C.POINTER(EnergySurfaceParameters),
                                                C.POINTER(_u32)]),
     "facetcu_project_spectral_parameters": (C.c_int, [_vp, C.POINTER(SpectralParameters)]),
+    "facetcu_project_xml_view": (C.c_int, [C.c_char_p, _vp, C.c_uint64, C.POINTER(C.c_uint64)]),
 })
 SIGNATURES["facetcu_render_sensor_image"] = (C.c_int, [_ctx, C.POINTER(Sensor), _vp, _u32, _vp, _vp,
                                                       _vp, C.POINTER(ImageInfo)])
@@ -577,6 +578,16 @@ def shortwave_windows(total_shortwave, cos_zenith, direct=None, diffuse=None,
 def _floats(ptr, n):
     return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_float)), (n,)).copy() if n else \
         np.zeros(0, np.float32)
+
+
+def project_xml_view(path):
+    """The XML view of a project.json (facetInputView)."""
+    lib = load()
+    n = C.c_uint64(0)
+    _host_check(lib.facetcu_project_xml_view(os.fsencode(path), None, 0, C.byref(n)))
+    buf = C.create_string_buffer(n.value + 1)
+    _host_check(lib.facetcu_project_xml_view(os.fsencode(path), buf, n.value + 1, C.byref(n)))
+    return buf.value.decode("utf-8")
 
 
 class Project:

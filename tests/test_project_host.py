@@ -262,7 +262,114 @@ def test_errors_match_reference(tmp_path, ref_project, case):
         ref_project.load(path)
     with pytest.raises(RuntimeError) as got:
         facetcu.Project(path)
-    if case == "json":  # the reference builds the XML view with nlohmann::json
-        assert "Input.xml" in str(got.value)
+    if case == "json":  # the oracle has no JSON reader; ProjectJson::load's message
+        assert str(got.value) == "project.json has no configuration object"
     else:
         assert str(got.value) == str(want.value)
+
+
+def _project_json(root, **over):
+    import json
+    cfg = {
+        "outDir": "output",
+        "scene": {"x": 8, "y": 6, "height": 5, "voxel": 0.5,
+                  "background": {"spectralName": "soil", "thermalName": "soil_temperature",
+                                 "materialName": "soilset", "heterogeneityEnabled": True,
+                                 "angularEffectStrength": 0.3}},
+        "light": {"zenith": 35, "azimuth": "120", "direct": 0.8, "skyTemperature": 255},
+        "sensor": {"bands": "550;450, 10500 550", "continuousBands": True, "bandStart": 1000,
+                   "bandEnd": 1040, "bandStep": 20},
+        "control": {"periodicBoundary": True, "periodicNeighborCount": 4, "radiationSolver": "accelerated",
+                    "soilTemperatureMethod": 0},
+        "objects": {"items": [
+            {"name": "House", "type": "Building", "fileName": "models/house.obj",
+             "positionFile": "positions/house.txt", "materialName": "wallset",
+             "meshes": [{"name": "wall", "spectralName": "concrete", "thermalName": "building_temperature",
+                         "materialName": "wallset"},
+                        {"name": "Roof", "spectralName": "panel", "materialName": "pvset"}]},
+            {"name": "Trees", "type": "Vegetation", "fileName": "models/tree.obj",
+             "positionFile": "positions/trees.txt", "spectralName": "green_leaf",
+             "materialName": "leafset"},
+            {"name": "Smoke", "type": "Fire"},
+            {"name": "Fogbank", "type": "Building", "medium": {}},
+            {"name": "Box", "type": "Water", "spectralName": "bark", "materialName": "leafset",
+             "dimensions": [1.5, 2, 0.5]}]},
+        "spectra": [
+            {"name": "soil", "model": "BSM", "refTir": 0.04,
+             "params": {"SMC": 20, "BSMBrightness": 0.4, "BSMlat": 30, "BSMlon": 50}},
+            {"name": "green_leaf", "model": "Prospect", "refTir": 0.02, "tauTir": 0.01,
+             "params": {"Cab": 45, "Cw": 0.012, "Cdm": 0.008, "Cs": 0.1, "N": 1.6}},
+            {"name": "panel", "reflectance": "0.05,0.06,0.08,0.1", "transmittance": 0, "refTir": 0.1},
+            {"name": "concrete", "reflectance": "0.25;0.3 0.35", "refTir": 0.08},
+            {"name": "bark", "model": "file", "fileName": "spectra/bark.txt", "refTir": 0.06}],
+        "thermals": [{"name": "building_temperature", "sunlitTemperature": 310,
+                      "shadedTemperature": 298}],
+        "materials": [
+            {"name": "soilset", "type": "Soil", "params": {"method": 2, "rss": 1500, "cs": 1100,
+                                                           "rhos": 1700, "lambdas": 1.2, "SMC": 30}},
+            {"name": "pvset", "type": "Building", "energyModel": "photovoltaic",
+             "params": {"eta25": 0.2, "gamma": -0.004, "bifaciality": 0.1}},
+            {"name": "leafset", "type": "Vegetation", "params": {"heatCapacityPerArea": 1500}},
+            {"name": "wallset", "type": "Building", "params": {"heatCapacityPerArea": 90000,
+                                                               "convectiveScale": 1.3}}],
+        "meteo": {"start": 0, "end": 2, "dTime": 1800},
+    }
+    cfg.update(over)
+    doc = {"schemaVersion": 2, "format": "streamsim-project", "name": "t", "configuration": cfg}
+    path = os.path.join(str(root), "project.json")
+    with open(path, "w") as f:
+        json.dump(doc, f)
+    return path
+
+
+@pytest.mark.slow
+def test_project_json_through_its_xml_view(tmp_path, ref_project, monkeypatch):
+    if not os.path.exists(OPTIPAR):
+        pytest.skip("optipar.txt not in the reference tree")
+    _write_project(tmp_path)  # models, positions, spectra, defined/optipar.txt
+    monkeypatch.chdir(tmp_path)  # the runtime "defined" folder is ./defined
+    path = _project_json(tmp_path)
+    view = facetcu.project_xml_view(path)
+    assert "<controlBand>450,550,1000,1020,1040,10500</controlBand>" in view
+    assert "<periodicNeighborCount>4</periodicNeighborCount>" in view
+    assert "<backgroundHeterogeneity>Hapke</backgroundHeterogeneity>" in view
+    assert "Smoke" not in view and "Fogbank" not in view
+    assert "<meshNames>wall,Roof</meshNames>" in view and "<method>0</method>" in view
+    xml_path = str(tmp_path / "view.xml")
+    open(xml_path, "w").write(view)
+    theirs = ref_project.load(xml_path)  # the reference's loader on the same view
+    ours = facetcu.Project(path)
+    _compare(ours, theirs)
+    assert ours.info["periodic_neighbor_count"] == 4 and ours.info["accelerated_solver"] == 1
+
+
+@pytest.mark.parametrize("case,message", [
+    ("name", "HiStream accepts project.json only"),
+    ("format", "Unsupported project format: other"),
+    ("version", "Unsupported project schemaVersion; expected 1-6"),
+    ("configuration", "project.json has no configuration object"),
+    ("pv_ground", "Photovoltaic panels must be scene objects, not background ground"),
+    ("syntax", "Invalid project.json"),
+])
+def test_project_json_errors(tmp_path, case, message):
+    import json
+    path = _project_json(tmp_path)
+    doc = json.load(open(path))
+    if case == "name":
+        os.rename(path, str(tmp_path / "scene.json"))
+        path = str(tmp_path / "scene.json")
+    elif case == "format":
+        doc["format"] = "other"
+    elif case == "version":
+        doc["schemaVersion"] = 7
+    elif case == "configuration":
+        doc["configuration"] = {}
+    elif case == "pv_ground":
+        doc["configuration"]["scene"]["background"]["materialName"] = "pvset"
+    if case in ("format", "version", "configuration", "pv_ground"):
+        json.dump(doc, open(path, "w"))
+    if case == "syntax":
+        open(path, "w").write('{"configuration": {"scene": [1, 2,, 3]}}')
+    with pytest.raises((ValueError, RuntimeError)) as e:
+        facetcu.project_xml_view(path)
+    assert str(e.value).startswith(message)

@@ -114,8 +114,8 @@ def test_cli_argument_handling():
     assert r.returncode == 3
     r = _cli("eFacetRT")
     assert r.returncode == 1 and "facetrt: FacetRT requires project.json" in r.stderr
-    r = _cli("eFacetRT", "project.json")  # only the project's XML form is read
-    assert r.returncode == 1 and r.stderr.startswith("facetrt: project.json is read through")
+    r = _cli("eFacetRT", "/nonexistent/project.json")  # read through its XML view
+    assert r.returncode == 1 and r.stderr.startswith("facetrt: Cannot open project.json: ")
     r = _cli("eFacetRT", "/nonexistent/Input.xml")
     assert r.returncode == 1 and "facetrt: Cannot open HiStream input: /nonexistent/Input.xml" in r.stderr
     r = _cli("eFacetRT", "/nonexistent/scene.obj")

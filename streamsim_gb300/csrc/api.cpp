@@ -357,6 +357,8 @@ int facetcu_destroy(facetcu_context* ctx)
                             &ctx->graph.p_packed, &ctx->graph.p_denom, &ctx->graph.p_sky})
         b->release();
     ctx->graph.perm_valid = false;
+    ctx->graph.scene_facets.clear();
+    ctx->graph.p_scene.release();
     ctx->graph_ready = false;
     for (DeviceBuffer* b : {&ctx->raster.counts, &ctx->raster.offsets, &ctx->raster.records,
                             &ctx->raster.big_list, &ctx->raster.deep_list, &ctx->raster.stats,
@@ -428,6 +430,7 @@ int facetcu_set_geometry(facetcu_context* ctx, const facetcu_vertex* vertices,
         ctx->graph_ready = false;
         ctx->graph.packed_valid = false;
         ctx->graph.perm_valid = false;
+        ctx->graph.scene_facets.clear();
         ctx->bvh_ready = false;
         ctx->facets = uint32_t(vertex_count / 3);
         ctx->vertices_host.assign(vertices, vertices + vertex_count);
@@ -738,6 +741,7 @@ int facetcu_set_graph(facetcu_context* ctx, uint32_t surface_count, const uint32
         upload(g.sky, sky_counts, size_t(surface_count) * 4, s);
         g.packed_valid = false;
         g.perm_valid = false;
+        g.scene_facets.clear();
         float closure;
         uint32_t sampled;
         graph_closure(g, &closure, &sampled, ctx->ws, s);
@@ -1486,6 +1490,12 @@ int facetcu_scene_batch(facetcu_context* ctx, facetcu_context* const* scenes,
         g.max_count = max_count;
         g.packed_valid = false;
         g.perm_valid = false;
+        // the scenes' facet ranges: converged scenes leave the int8 steps
+        g.scene_facets.assign(1, 0u);
+        for (uint32_t i = 0, f = 0; i < scene_count; ++i) {
+            f += scenes[i]->graph.surfaces / 2u;
+            g.scene_facets.push_back(f);
+        }
         float closure = 0.0f;
         uint32_t sampled = 0;
         graph_closure(g, &closure, &sampled, ctx->ws, s);

@@ -75,6 +75,15 @@ struct GraphView {
     const uint32_t* skyc;
     uint32_t facets;
     uint32_t nb_bits;                  // neighbour field of a packed word (count above it)
+    // scene batches (block-diagonal graphs): the scene of each facet, and per
+    // scene the int8 steps' worst per-side ratio per column and a done flag
+    const uint16_t* scene;             // null when the graph is one scene
+    uint32_t scenes;
+    uint32_t* scene_stats;             // [scenes][kMaxP] worst per-side ratio (float bits)
+    uint32_t* scene_md;                // [scenes][kMaxP] max |R| (float bits)
+    float* scene_sig;                  // two slots of [scenes][kMaxP] int8 step scales
+    float* scene_cheb;                 // [scenes][4 kMaxP] Chebyshev state (weights at 2 kMaxP)
+    uint32_t* scene_done;              // [scenes]
 };
 
 __device__ __forceinline__ void edge_at(const GraphView& g, uint32_t e, uint32_t& nb, float& c)
@@ -117,6 +126,35 @@ __device__ __forceinline__ Acc gather_narrow(const GraphView& g, uint32_t s, con
     const int grp = lane / P, col = lane % P;
     const uint32_t start = g.rows[s], end = g.rows[s + 1];
     Acc acc = 0;
+    if constexpr (P <= 4) {
+        // 8+ edge groups: each lane walks its group's edges itself, U loads
+        // in flight (a broadcast of one 32-edge chunk would leave most of
+        // the unrolled loads empty)
+        constexpr int U = 8;
+        for (uint32_t e = start + uint32_t(grp); e < end; e += uint32_t(G * U)) {
+            Acc v[U];
+            float c[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t idx = e + uint32_t(u * G);
+                v[u] = 0;
+                c[u] = 0.0f;
+                if (idx < end) {
+                    uint32_t nb;
+                    edge_at(g, idx, nb, c[u]);
+                    if constexpr (sizeof(Acc) == 8)
+                        v[u] = Acc(X[size_t(nb) * P + col]);
+                    else
+                        v[u] = Acc(load_as_float<T>(X + size_t(nb) * P + col));
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) acc += Acc(c[u]) * v[u];
+        }
+#pragma unroll
+        for (int o = P; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        return acc;
+    }
     for (uint32_t base = start; base < end; base += 32) {
         const uint32_t n = min(32u, end - base);
         uint32_t pk = 0;
@@ -180,6 +218,9 @@ template <bool kBF16> constexpr int kVecCols = kBF16 ? 8 : 4;
 #endif
 #ifndef FCU_STEP64_MIN_BLOCKS
 #define FCU_STEP64_MIN_BLOCKS 4
+#endif
+#ifndef FCU_SCENE_SKIP
+#define FCU_SCENE_SKIP 1
 #endif
 constexpr int kGatherU = FCU_GATHER_U;
 constexpr bool kPrefetch = FCU_PREFETCH != 0;
@@ -677,11 +718,12 @@ template <> struct VecN<4> {
     }
 };
 
-template <int P>
+template <int P, bool Scenes>
 __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
     GraphView g, PanelParams pp, const int8_t* __restrict__ Qin, int8_t* __restrict__ Qout,
     float* __restrict__ X, float* __restrict__ R, const float* __restrict__ sig_in,
-    const float* __restrict__ sig_out, uint32_t* stats, uint32_t* counter, const uint32_t* done)
+    const float* __restrict__ sig_out, uint32_t* stats, uint32_t* counter, const uint32_t* done,
+    const float* __restrict__ scene_sig_in, const float* __restrict__ scene_sig_out)
 {
     if (*done) return;
     constexpr int L = P / 16, G = 32 / L, NC = P / 32;
@@ -699,7 +741,45 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
         mb[k] = 0.0f;
         mr[k] = 0.0f;
     }
+    // Scene batches: each scene steps with its own int8 scales (a scale set
+    // by another scene's larger residual would round this scene's steps to
+    // zero), its worst per-side ratio and max |R| are gathered while the
+    // warp stays in that scene, and the facets of a converged scene are
+    // skipped.
+    uint32_t cur = 0xffffffffu;
+    float ms[NC], mq[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        ms[k] = 0.0f;
+        mq[k] = 0.0f;
+    }
+    auto flush = [&]() {
+        if (Scenes && cur != 0xffffffffu) {
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                atomicMax(g.scene_stats + size_t(cur) * kMaxP + col0 + k, __float_as_uint(ms[k]));
+                atomicMax(g.scene_md + size_t(cur) * kMaxP + col0 + k, __float_as_uint(mq[k]));
+            }
+        }
+    };
     for_each_facet(g.facets, counter, lane, [&](uint32_t f) {
+        if (Scenes) {
+            const uint32_t sc = __ldg(g.scene + f);
+            if (g.scene_done[sc]) return;
+            if (sc != cur) {
+                flush();
+                cur = sc;
+#pragma unroll
+                for (int k = 0; k < NC; ++k) {
+                    ms[k] = 0.0f;
+                    mq[k] = 0.0f;
+                    si[k] = scene_sig_in[size_t(sc) * kMaxP + col0 + k];
+                    const float so = scene_sig_out[size_t(sc) * kMaxP + col0 + k];
+                    inv_so[k] = so > 0.0f ? 1.0f / so : 0.0f;
+                    om[k] = g.scene_cheb[size_t(sc) * 4 * kMaxP + 2 * kMaxP + col0 + k];
+                }
+            }
+        }
         {
             float h[2][NC];
 #pragma unroll
@@ -748,6 +828,17 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
                 // next Jacobi sweep would make
                 mr[k] = fmaxf(mr[k], fmaxf(__fdividef(fabsf(e0[k]), fmaxf(fabsf(x0[k]), fl[k])),
                                            __fdividef(fabsf(e1[k]), fmaxf(fabsf(x1[k]), fl[k]))));
+                if (Scenes) {
+                    // a zero residual passes (the column test's md == 0 case)
+                    const float a0 = fabsf(e0[k]) > 0.0f
+                                         ? __fdividef(fabsf(e0[k]), fmaxf(fabsf(x0[k]), fl[k]))
+                                         : 0.0f;
+                    const float a1 = fabsf(e1[k]) > 0.0f
+                                         ? __fdividef(fabsf(e1[k]), fmaxf(fabsf(x1[k]), fl[k]))
+                                         : 0.0f;
+                    ms[k] = fmaxf(ms[k], fmaxf(a0, a1));
+                    mq[k] = fmaxf(mq[k], fmaxf(fabsf(e0[k]), fabsf(e1[k])));
+                }
             }
             VecN<NC>::st(X + i0, x0);
             VecN<NC>::st(X + i1, x1);
@@ -757,20 +848,98 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
             VecN<NC>::stq(Qout + i1, q1);
         }
     });
+    flush();
     publish_cols<NC>(md, mb, mr, col0, true, P, stats);
+}
+
+__device__ __forceinline__ float cheb_advance(float* cheb, int c, int mode, float md);
+
+// After an int8 step of a scene batch: a scene whose worst per-side ratio is
+// within the tolerance in every column is done (its facets are skipped by
+// the following steps); the others advance their own Chebyshev schedule
+// (their own spectral-radius estimate, as if solved alone) and get the scale
+// of their step after next from their own max |R|, as the column check forms
+// them for the whole panel.  The step records are cleared for the next step.
+__global__ void k_scene_check(uint32_t* ratio, uint32_t* mdr, float* sig_write,
+                              const float* sig_prev, uint32_t* done, float* cheb, int P,
+                              float tol)
+{
+    __shared__ int bad;
+    const uint32_t sc = blockIdx.x;
+    const uint32_t c = threadIdx.x;
+    if (c == 0) bad = 0;
+    __syncthreads();
+    if (c < uint32_t(P)) {
+        const size_t i = size_t(sc) * kMaxP + c;
+        const float r = __uint_as_float(ratio[i]);
+        const float md = __uint_as_float(mdr[i]);
+        ratio[i] = 0u;
+        mdr[i] = 0u;
+        if (!(r <= tol)) bad = 1;
+        if (!done[sc]) {
+            const float w = cheb_advance(cheb + size_t(sc) * 4 * kMaxP, int(c), 2, md);
+            float sigma = md / 127.0f;
+            if (w != 1.0f) sigma = (w * md + (w - 1.0f) * 127.0f * sig_prev[i]) / 127.0f;
+            sig_write[i] = sigma;
+        }
+    }
+    __syncthreads();
+    if (c == 0 && !bad) done[sc] = 1u;
+}
+
+// At the start of an int8 phase of a scene batch: max |Y - X| per scene and
+// column (a block per run of sides, a thread per column), then the scenes'
+// first scales.
+__global__ void k_scene_init_md(const float* __restrict__ X, const float* __restrict__ Y,
+                                const uint16_t* __restrict__ scene, uint32_t S, int P,
+                                uint32_t* mdr)
+{
+    constexpr uint32_t kRun = 256;
+    const uint32_t c = threadIdx.x;
+    if (c >= uint32_t(P)) return;
+    const uint32_t s0 = blockIdx.x * kRun, s1 = min(S, s0 + kRun);
+    uint32_t cur = 0xffffffffu;
+    float m = 0.0f;
+    for (uint32_t sd = s0; sd < s1; ++sd) {
+        const uint32_t sc = scene[sd >> 1];
+        if (sc != cur) {
+            if (cur != 0xffffffffu) atomicMax(mdr + size_t(cur) * kMaxP + c, __float_as_uint(m));
+            cur = sc;
+            m = 0.0f;
+        }
+        const size_t i = size_t(sd) * P + c;
+        m = fmaxf(m, fabsf(Y[i] - X[i]));
+    }
+    if (cur != 0xffffffffu) atomicMax(mdr + size_t(cur) * kMaxP + c, __float_as_uint(m));
+}
+
+// both scale slots (step 0 reads slot 0 and writes with slot 1) and a fresh
+// Chebyshev schedule per scene
+__global__ void k_scene_init_sigma(uint32_t* mdr, float* sig, float* cheb, uint32_t scenes, int P)
+{
+    const size_t i = size_t(blockIdx.x) * kMaxP + threadIdx.x;
+    if (threadIdx.x >= uint32_t(P)) return;
+    const float md = __uint_as_float(mdr[i]);
+    const float sigma = md / 127.0f;
+    sig[i] = sigma;
+    sig[size_t(scenes) * kMaxP + i] = sigma;
+    cheb_advance(cheb + size_t(blockIdx.x) * 4 * kMaxP, int(threadIdx.x), 1, md);
+    mdr[i] = 0u;
 }
 
 // R = Y - X and Q = round(R / sigma) for the first int8 step (X unchanged).
 __global__ void k_init_i8(const float* __restrict__ X, const float* __restrict__ Y,
                           float* __restrict__ R, int8_t* __restrict__ Q,
                           const float* __restrict__ sig, size_t n, int P, uint32_t* it_dev,
-                          uint32_t it)
+                          uint32_t it, const uint16_t* __restrict__ scene = nullptr,
+                          const float* __restrict__ scene_sig = nullptr)
 {
     const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i == 0) *it_dev = it;  // sweep index of the first step's check
     if (i >= n) return;
     const float r = Y[i] - X[i];
-    const float sg = sig[i % size_t(P)];
+    const size_t c = i % size_t(P);
+    const float sg = scene ? scene_sig[size_t(scene[(i / size_t(P)) >> 1]) * kMaxP + c] : sig[c];
     R[i] = r;
     Q[i] = int8_t(sg > 0.0f ? max(-127, min(127, __float2int_rn(r / sg))) : 0);
 }
@@ -1052,6 +1221,14 @@ __global__ void k_perm_lengths(const uint32_t* order, uint32_t S, const uint32_t
     psky[s] = sky[so];
 }
 
+// The scene of each renumbered facet.
+__global__ void k_perm_scene(const uint32_t* __restrict__ order, const uint16_t* __restrict__ scene,
+                             uint32_t F, uint16_t* __restrict__ out)
+{
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < F) out[f] = scene[order[f]];
+}
+
 __global__ void k_perm_copy(const uint32_t* order, const uint32_t* rank, uint32_t S,
                             const uint32_t* rows, const uint32_t* packed, const uint32_t* prows,
                             uint32_t* ppacked, uint32_t nb_bits)
@@ -1145,32 +1322,64 @@ void launch_defect(int P, const GraphView& g, const PanelParams& pp, const __nv_
     FCU_LAUNCH("k_sweep_defect");
 }
 
-template <int P>
+template <int P, bool Scenes>
 int step_grid()
 {
-    static const int grid = grid_for(k_step_i8<P>);
+    static const int grid = grid_for(k_step_i8<P, Scenes>);
     return grid;
 }
 
+// parity: the step's index modulo 2 (its input scales are slot `parity`,
+// its output scales slot `parity ^ 1`)
 void launch_step_i8(int P, const GraphView& g, const PanelParams& pp, const int8_t* qin,
                     int8_t* qout, float* X, float* R, const float* sin, const float* sout,
-                    uint32_t* stats, uint32_t* counter, const uint32_t* done, cudaStream_t s)
+                    uint32_t* stats, uint32_t* counter, const uint32_t* done, uint32_t parity,
+                    cudaStream_t s)
 {
+    const bool sc = g.scene != nullptr;
+    const size_t slot = size_t(g.scenes) * kMaxP;
+    const float* ssin = sc ? g.scene_sig + (parity & 1u) * slot : nullptr;
+    const float* ssout = sc ? g.scene_sig + ((parity + 1u) & 1u) * slot : nullptr;
     switch (P) {
     case 32:
-        k_step_i8<32><<<step_grid<32>(), kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin, sout,
-                                                              stats, counter, done);
+        if (sc)
+            k_step_i8<32, true><<<step_grid<32, true>(), kWarps * 32, 0, s>>>(
+                g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
+        else
+            k_step_i8<32, false><<<step_grid<32, false>(), kWarps * 32, 0, s>>>(
+                g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
         break;
     case 64:
-        k_step_i8<64><<<step_grid<64>(), kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin, sout,
-                                                              stats, counter, done);
+        if (sc)
+            k_step_i8<64, true><<<step_grid<64, true>(), kWarps * 32, 0, s>>>(
+                g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
+        else
+            k_step_i8<64, false><<<step_grid<64, false>(), kWarps * 32, 0, s>>>(
+                g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
         break;
     default:
-        k_step_i8<128><<<step_grid<128>(), kWarps * 32, 0, s>>>(g, pp, qin, qout, X, R, sin,
-                                                                sout, stats, counter, done);
+        if (sc)
+            k_step_i8<128, true><<<step_grid<128, true>(), kWarps * 32, 0, s>>>(
+                g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
+        else
+            k_step_i8<128, false><<<step_grid<128, false>(), kWarps * 32, 0, s>>>(
+                g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
         break;
     }
     FCU_LAUNCH("k_step_i8");
+}
+
+// The scene check after step `parity` (after the column check): writes the
+// scales of slot `parity`, reading slot `parity ^ 1`.
+void launch_scene_check(const GraphView& g, int P, uint32_t parity, float tol, cudaStream_t s)
+{
+    if (!g.scene) return;
+    const size_t slot = size_t(g.scenes) * kMaxP;
+    k_scene_check<<<g.scenes, kMaxP, 0, s>>>(g.scene_stats, g.scene_md,
+                                              g.scene_sig + (parity & 1u) * slot,
+                                              g.scene_sig + ((parity + 1u) & 1u) * slot,
+                                              g.scene_done, g.scene_cheb, P, tol);
+    FCU_LAUNCH("k_scene_check");
 }
 
 // One batch of kStepBatch int8 steps, each followed by its check, as a CUDA
@@ -1203,12 +1412,13 @@ void record_steps(const StepGraphKey& k, cudaStream_t s)
     uint32_t* counter = k.flag + 8;
     for (uint32_t j = 0; j < kStepBatch; ++j) {
         launch_step_i8(k.P, k.g, k.pp, qb[j & 1u], qb[(j + 1) & 1u], k.X, k.R, slot[j & 1u],
-                       slot[(j + 1) & 1u], k.stats, counter, k.flag + 3, s);
+                       slot[(j + 1) & 1u], k.stats, counter, k.flag + 3, j & 1u, s);
         float* colmax = reinterpret_cast<float*>(k.flag + 16);
         k_check<<<1, kMaxP, 0, s>>>(k.stats, k.flag + 3, k.P, k.tol, 0u, counter, slot[j & 1u],
                                     nullptr, k.flag + 12, true, colmax, colmax + 3 * kMaxP, 2,
                                     slot[(j + 1) & 1u]);
         FCU_LAUNCH("k_check");
+        launch_scene_check(k.g, k.P, j & 1u, k.tol, s);
     }
 }
 
@@ -1218,9 +1428,9 @@ cudaGraphExec_t step_graph(BatchState& st, const StepGraphKey& key)
         return st.step_graph;
     release_graphs(st);
     switch (key.P) {  // size the grids before capture starts
-    case 32: step_grid<32>(); break;
-    case 64: step_grid<64>(); break;
-    default: step_grid<128>(); break;
+    case 32: step_grid<32, false>(); step_grid<32, true>(); break;
+    case 64: step_grid<64, false>(); step_grid<64, true>(); break;
+    default: step_grid<128, false>(); step_grid<128, true>(); break;
     }
     cudaGraph_t graph = nullptr;
     FCU_CHECK(cudaStreamBeginCapture(key.stream, cudaStreamCaptureModeThreadLocal));
@@ -1284,6 +1494,19 @@ void ensure_permuted(DeviceGraph& gr, const BatchProblem& p, Workspace& ws, cuda
         order, rank, S, gr.row_offsets.as<uint32_t>(), gr.packed.as<uint32_t>(), prows, ppk,
         gr.nb_bits);
     FCU_LAUNCH("k_perm_copy");
+    const size_t scenes = gr.scene_facets.size() >= 3 ? gr.scene_facets.size() - 1 : 0;
+    if (scenes >= 2 && scenes <= 65535 && gr.scene_facets.back() == F) {
+        std::vector<uint16_t> h(F);
+        for (size_t k = 0; k < scenes; ++k)
+            for (uint32_t f = gr.scene_facets[k]; f < gr.scene_facets[k + 1]; ++f) h[f] = uint16_t(k);
+        uint16_t* d_orig = static_cast<uint16_t*>(ws.e.reserve(size_t(F) * 2 + 64));
+        uint16_t* d_perm = static_cast<uint16_t*>(gr.p_scene.reserve(size_t(F) * 2 + 64));
+        FCU_CHECK(cudaMemcpyAsync(d_orig, h.data(), size_t(F) * 2, cudaMemcpyHostToDevice, s));
+        k_perm_scene<<<blocks_for(F, 256), 256, 0, s>>>(order, d_orig, F, d_perm);
+        FCU_LAUNCH("k_perm_scene");
+    } else {
+        gr.p_scene.release();
+    }
     FCU_CHECK(cudaStreamSynchronize(s));
     gr.perm_valid = true;
 }
@@ -1367,6 +1590,27 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
     g.skyc = perm ? gr.p_sky.as<uint32_t>() : gr.sky.as<uint32_t>();
     g.facets = S / 2u;
     g.nb_bits = gr.nb_bits;
+    g.scene = nullptr;
+    g.scenes = 0;
+    g.scene_stats = nullptr;
+    g.scene_md = nullptr;
+    g.scene_sig = nullptr;
+    g.scene_cheb = nullptr;
+    g.scene_done = nullptr;
+    if (FCU_SCENE_SKIP && perm && mixed && gr.p_scene.ptr && gr.p_scene.bytes >= size_t(S / 2u) * 2 &&
+        gr.scene_facets.size() >= 3) {
+        // scene batch: converged scenes leave the int8 steps
+        g.scene = gr.p_scene.as<uint16_t>();
+        g.scenes = uint32_t(gr.scene_facets.size() - 1);
+        // [scenes][kMaxP] ratio, [scenes][kMaxP] max|R|, 2 x [scenes][kMaxP]
+        // scales, [scenes][4 kMaxP] Chebyshev state, [scenes] done
+        g.scene_stats = static_cast<uint32_t*>(
+            st.scene_state.reserve(size_t(g.scenes) * (8 * kMaxP + 1) * 4));
+        g.scene_md = g.scene_stats + size_t(g.scenes) * kMaxP;
+        g.scene_sig = reinterpret_cast<float*>(g.scene_md + size_t(g.scenes) * kMaxP);
+        g.scene_cheb = g.scene_sig + size_t(g.scenes) * 2 * kMaxP;
+        g.scene_done = g.scene_stats + size_t(g.scenes) * 8 * kMaxP;
+    }
     const uint32_t cap = fp64 ? 32u : uint32_t(kMaxP);
     const int Pmax = panel_width(R, cfg.panel_width, cap);
     const size_t cells_max = size_t(S) * Pmax;
@@ -1541,8 +1785,21 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                     std::swap(X, Y);
                     continue;
                 }
+                if (g.scene) {
+                    // every scene takes part in a new int8 phase, with its
+                    // own first scales max|Y - X| / 127
+                    FCU_CHECK(cudaMemsetAsync(g.scene_stats, 0,
+                                              size_t(g.scenes) * (8 * kMaxP + 1) * 4, s));
+                    k_scene_init_md<<<(S + 255) / 256, P, 0, s>>>(X, Y, g.scene, S, P, g.scene_md);
+                    FCU_LAUNCH("k_scene_init_md");
+                    k_scene_init_sigma<<<g.scenes, kMaxP, 0, s>>>(g.scene_md, g.scene_sig,
+                                                                  g.scene_cheb, g.scenes, P);
+                    FCU_LAUNCH("k_scene_init_sigma");
+                    launches += 2;
+                }
                 k_init_i8<<<blocks_for(cells, 256), 256, 0, s>>>(X, Y, rbuf, qb[0], slot[0], cells,
-                                                                 P, flag + 12, it);
+                                                                 P, flag + 12, it, g.scene,
+                                                                 g.scene_sig);
                 FCU_LAUNCH("k_init_i8");
                 ++launches;
                 uint32_t j = 0;
@@ -1567,7 +1824,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                         key.tol = step_tol;
                         key.stream = s;
                         FCU_CHECK(cudaGraphLaunch(step_graph(st, key), s));
-                        launches += 2 * kStepBatch;
+                        launches += (g.scene ? 3 : 2) * kStepBatch;
                         sweeps += kStepBatch;
                         ++graph_launches;
                         j += kStepBatch;
@@ -1577,7 +1834,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                         const float* sout = slot[(j + 1) & 1u];
                         timed_sweep(true, [&] {
                             launch_step_i8(P, g, pp, qb[j & 1u], qb[(j + 1) & 1u], X, rbuf, sin,
-                                           sout, stats, counter, flag + 3, s);
+                                           sout, stats, counter, flag + 3, j & 1u, s);
                         });
                         // slot j & 1 (sigma of the panel just consumed) takes
                         // max|R_new| / 127 for the step after next
@@ -1585,7 +1842,8 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                                                     counter, slot[j & 1u], nullptr, nullptr,
                                                     true, colmax, cheb, 2, slot[(j + 1) & 1u]);
                         FCU_LAUNCH("k_check");
-                        ++launches;
+                        launch_scene_check(g, P, j & 1u, step_tol, s);
+                        launches += g.scene ? 2 : 1;
                     }
                     it += batch;
                     uint32_t sub_flag[3];
@@ -1650,7 +1908,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                                                     it + k, counter, nullptr, nullptr, nullptr,
                                                     false, colmax);
                         FCU_LAUNCH("k_check");
-                        ++launches;
+                        launches += g.scene ? 2 : 1;
                     }
                     it += batch;
                     FCU_CHECK(cudaMemcpyAsync(sub_flag, flag + 3, 12, cudaMemcpyDeviceToHost, s));

@@ -180,6 +180,7 @@ void graph_from_pairs(uint64_t* d_pairs, size_t n, int side_bits, DeviceGraph& g
     FCU_CHECK(cudaStreamSynchronize(s));
     g.packed_valid = false;
     g.perm_valid = false;
+    g.scene_facets.clear();
 }
 
 void graph_closure(const DeviceGraph& g, float* closure, uint32_t* sampled, Workspace& ws,

@@ -148,6 +148,10 @@ struct DeviceGraph {
     DeviceBuffer order;         // new facet -> old facet
     DeviceBuffer rank;          // old facet -> new facet
     DeviceBuffer p_rows, p_packed, p_denom, p_sky;
+    // Scene batches: the first facet of every scene and the total (empty for
+    // one scene); with the Morton copy, the scene of each renumbered facet.
+    std::vector<uint32_t> scene_facets;
+    DeviceBuffer p_scene;       // F u16, built with the Morton copy for 2..65535 scenes
 };
 // Sort undirected pair keys, count runs, emit the symmetric CSR.
 void graph_from_pairs(uint64_t* d_pairs, size_t pair_count, int side_bits, DeviceGraph& g,
@@ -195,6 +199,7 @@ struct BatchState {
     DeviceBuffer q;             // source term per panel
     DeviceBuffer corr;          // residual / correction panel
     DeviceBuffer i8;            // int8 step panels (two)
+    DeviceBuffer scene_state;   // scene batches: [scenes][kMaxP] step records + [scenes] done
     cudaGraphExec_t step_graph = nullptr;  // captured batch of int8 steps
     alignas(8) unsigned char step_graph_key[256] = {};
 };

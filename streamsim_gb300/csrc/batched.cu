@@ -1044,7 +1044,10 @@ __global__ void k_defect_init(const float* Bold, const float* Bnew, __nv_bfloat1
 // in colmax (the next sweep's floor) and clears the stats.  With scale_a /
 // scale_b, also stores max|dB| / 127 per column there (the int8 step
 // scales).
-constexpr float kChebWarm = 4.0f;  // plain int8 steps before c is estimated
+#ifndef FCU_CHEB_WARM
+#define FCU_CHEB_WARM 4
+#endif
+constexpr float kChebWarm = float(FCU_CHEB_WARM);  // plain int8 steps before c is estimated
 constexpr float kChebMax = 0.7f;   // largest c for which the weights are used
 
 // Chebyshev state per column (cheb[0..4 kMaxP)): previous max|R|, c (-1 =

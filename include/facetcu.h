@@ -637,10 +637,11 @@ int facetcu_render_sensor_image(facetcu_context *ctx, const facetcu_sensor *sens
  * (facetrtcore.cpp:2038-3025): objects from OBJ files (groups bound to
  * materials by mesh name) or cubes, placed from position files (x y z
  * [scale [rotation]]) and clipped to the scene domain, then a flat ground
- * grid; materials from custom, file, PROSPECT and BSM spectra (the models'
- * optipar.txt beside the sun spectrum), thermal blocks, soil sets and
- * surface-energy blocks.  DEM files and physical textures need GDAL and are
- * refused with the reference's messages.  A project.json is read through
+ * grid, raised by the project's DEM (facetcu_dem_height_field) under the
+ * ground and every placement; materials from custom, file, PROSPECT and BSM
+ * spectra (the models' optipar.txt beside the sun spectrum), thermal blocks,
+ * soil sets and surface-energy blocks.  Physical textures need GDAL and are
+ * refused with the reference's message.  A project.json is read through
  * its XML view (facetcu_project_xml_view).  Host only; errors through
  * facetcu_host_last_error(). */
 typedef struct facetcu_project facetcu_project;
@@ -678,6 +679,18 @@ int facetcu_project_get_material(const facetcu_project *project, uint32_t index,
  * be NULL to ask for the length. */
 int facetcu_project_xml_view(const char *path, char *buffer, uint64_t capacity,
                              uint64_t *length);
+/* A DEM height field as readDemHeightField makes it (facetrtcore.cpp:
+ * 2618-2697, which reads band 1 with GDAL): values[height][width] in
+ * metres, rows from north to south, nodata and non-finite cells set to
+ * *minimum, the minimum of the valid cells.  Reads ESRI ASCII grids and
+ * baseline GeoTIFF (classic or BigTIFF, strips or tiles, no compression,
+ * LZW, deflate or PackBits, predictors 1-3, integer or IEEE samples, the
+ * GDAL_NODATA tag).  values may be NULL to ask for the size; capacity is
+ * its length in floats.  FACETCU_RUNTIME_ERROR with the reference's
+ * messages ("Cannot open DEM: ", "Cannot read DEM elevations: ", "DEM must
+ * contain at least 2 x 2 cells: ", "DEM contains no valid elevations: "). */
+int facetcu_dem_height_field(const char *path, int32_t *width, int32_t *height, float *minimum,
+                             float *values, uint64_t capacity);
 /* The project's FacetRTParameters and scene fields as spectral parameters
  * for facetcu_spectral_optics / facetcu_solve_bands. */
 int facetcu_project_spectral_parameters(const facetcu_project *project,

@@ -8,6 +8,7 @@
 #include <array>
 #include <chrono>
 #include <cstdint>
+#include <filesystem>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -62,6 +63,24 @@ struct Context {
 };
 
 }  // namespace host
+
+namespace dem {
+// DemHeightField (facetrtcore.cpp:2618-2650): band 1 as float32, nodata and
+// non-finite cells replaced by the minimum of the valid ones.
+struct HeightField {
+    int width = 0, height = 0;
+    float minimum = 0.0f;
+    std::vector<float> values;
+    bool valid() const
+    {
+        return width >= 2 && height >= 2 && values.size() == size_t(width) * size_t(height);
+    }
+    float above_minimum(float north_x, float east_z, float scene_width, float scene_depth) const;
+};
+// readDemHeightField's file step (facetrtcore.cpp:2660-2696) over ESRI ASCII
+// grids and baseline GeoTIFF; throws the reference's messages.
+HeightField read_height_field(const std::filesystem::path& path);
+}  // namespace dem
 
 namespace project {
 // The XML view of a project.json (facetInputView, facetrtcore.cpp:1888-2036).

@@ -20,10 +20,11 @@
 // pow) resolve to the C library's double functions; here they are written as
 // std::fn(double(x)) with the same float/double promotions.
 //
-// Not supported, as GDAL is not available: DEM height fields and physical
-// reflectance textures (both fail with the reference's message).  A
-// project.json is read through its XML view (project_json.cpp), as the
-// reference's readTextFile does.
+// DEM height fields are read by dem.cpp (ESRI ASCII grids and baseline
+// GeoTIFF, the formats GDAL would open for the reference).  Not supported, as
+// GDAL is not available: physical reflectance textures (they fail with the
+// reference's message).  A project.json is read through its XML view
+// (project_json.cpp), as the reference's readTextFile does.
 #include <algorithm>
 #include <array>
 #include <cctype>
@@ -798,7 +799,7 @@ Geometry cube(const std::string& obj)
 }
 
 void append_ground(host::HostScene& sc, float width, float depth, float voxel, uint32_t max_grid,
-                   uint32_t material)
+                   uint32_t material, const dem::HeightField& dem)
 {
     const float x0 = -width * 0.5f, z0 = -depth * 0.5f;
     const uint32_t want_cols = std::max(1u, uint32_t(std::ceil(width / voxel)));
@@ -806,16 +807,21 @@ void append_ground(host::HostScene& sc, float width, float depth, float voxel, u
     const uint32_t cols = std::clamp(want_cols, 1u, max_grid);
     const uint32_t rows = std::clamp(want_rows, 1u, max_grid);
     const float cw = width / float(cols), cd = depth / float(rows);
-    // flat ground: the DEM height above its minimum is 0, 1 cm below y = 0
-    const float h = 0.0f - 0.01f;
+    // the whole DEM is stretched over the domain, 1 cm below its height
     for (uint32_t r = 0; r < rows; ++r) {
         const float za = z0 + cd * float(r);
         const float zb = r + 1 == rows ? z0 + depth : z0 + cd * float(r + 1);
         for (uint32_t c = 0; c < cols; ++c) {
             const float xa = x0 + cw * float(c);
             const float xb = c + 1 == cols ? x0 + width : x0 + cw * float(c + 1);
-            host::push_triangle(sc, {xa, h, za}, {xb, h, zb}, {xb, h, za}, material);
-            host::push_triangle(sc, {xa, h, za}, {xa, h, zb}, {xb, h, zb}, material);
+            const float sxa = xa + width * 0.5f, sxb = xb + width * 0.5f;
+            const float sza = za + depth * 0.5f, szb = zb + depth * 0.5f;
+            const float haa = dem.above_minimum(sxa, sza, width, depth) - 0.01f;
+            const float hab = dem.above_minimum(sxa, szb, width, depth) - 0.01f;
+            const float hba = dem.above_minimum(sxb, sza, width, depth) - 0.01f;
+            const float hbb = dem.above_minimum(sxb, szb, width, depth) - 0.01f;
+            host::push_triangle(sc, {xa, haa, za}, {xb, hbb, zb}, {xb, hba, za}, material);
+            host::push_triangle(sc, {xa, haa, za}, {xa, hab, zb}, {xb, hbb, zb}, material);
         }
     }
 }
@@ -840,11 +846,11 @@ Project load(const std::string& path)
     const float depth = std::max(0.01f, xml_float(xml, "sceneSizeY", 8.0f));
     const float height = std::max(0.01f, xml_float(xml, "Height", 4.0f));
     const float voxel = std::max(0.01f, xml_float(xml, "voxelSize", 1.0f));
+    dem::HeightField dem;  // readDemHeightField (facetrtcore.cpp:2652-2697)
     const std::string dem_enabled = trim(first_tag(xml, "isDEM"));
     if (dem_enabled.empty() || dem_enabled == "1") {
-        const std::string dem = trim(first_tag(xml, "DEM"));
-        if (!dem.empty())  // the reference opens it with GDAL, which is not available
-            throw std::runtime_error("Cannot open DEM: " + resolve(input, dem).string());
+        const std::string file = trim(first_tag(xml, "DEM"));
+        if (!file.empty()) dem = dem::read_height_field(resolve(input, file));
     }
     Project P;
     P.periodic = uint32_t(
@@ -913,13 +919,15 @@ Project load(const std::string& path)
         std::string file = trim(first_tag(obj, "fileName"));
         if (file.empty()) file = trim(first_tag(obj, "objectfile"));
         const Geometry g = file.empty() ? cube(obj) : read_obj(resolve(input, file));
-        for (Placement pl : read_placements(input, obj, width, depth))
+        for (Placement pl : read_placements(input, obj, width, depth)) {
+            pl.z += dem.above_minimum(pl.x, pl.y, width, depth);
             append_geometry(sc, g, pl, width, depth, height, bindings);
+        }
     }
     sc.leaf = sc.facets();
     const uint32_t ground = uint32_t(P.materials.size());
     P.materials.push_back(P.params.ground);
-    append_ground(sc, width, depth, voxel, P.raster / 4u, ground);
+    append_ground(sc, width, depth, voxel, P.raster / 4u, ground, dem);
     const uint32_t initial = P.layers;
     P.layers = adaptive_layers(sc.facets(), P.periodic, P.raster, P.layers);
     if (P.layers != initial)

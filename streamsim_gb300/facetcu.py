@@ -313,6 +313,8 @@ SIGNATURES.update({
                                                C.POINTER(_u32)]),
     "facetcu_project_spectral_parameters": (C.c_int, [_vp, C.POINTER(SpectralParameters)]),
     "facetcu_project_xml_view": (C.c_int, [C.c_char_p, _vp, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "facetcu_dem_height_field": (C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                           C.POINTER(C.c_float), _vp, C.c_uint64]),
 })
 SIGNATURES["facetcu_render_sensor_image"] = (C.c_int, [_ctx, C.POINTER(Sensor), _vp, _u32, _vp, _vp,
                                                       _vp, C.POINTER(ImageInfo)])
@@ -588,6 +590,20 @@ def project_xml_view(path):
     buf = C.create_string_buffer(n.value + 1)
     _host_check(lib.facetcu_project_xml_view(os.fsencode(path), buf, n.value + 1, C.byref(n)))
     return buf.value.decode("utf-8")
+
+
+def dem_height_field(path):
+    """A DEM as the project loader reads it (readDemHeightField):
+    (values (height, width) float32, rows north to south, with nodata set to
+    the minimum; minimum)."""
+    lib = load()
+    w, h, lo = C.c_int32(0), C.c_int32(0), C.c_float(0)
+    path = os.fsencode(path)
+    _host_check(lib.facetcu_dem_height_field(path, C.byref(w), C.byref(h), C.byref(lo), None, 0))
+    out = np.empty((h.value, w.value), np.float32)
+    _host_check(lib.facetcu_dem_height_field(path, C.byref(w), C.byref(h), C.byref(lo),
+                                             out.ctypes.data, out.size))
+    return out, float(lo.value)
 
 
 class Project:

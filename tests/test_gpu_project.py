@@ -3,7 +3,7 @@ facetRTParametersFromInput and runGpu's spectral band loop,
 models/histream/src/facetrt/facetrtcore.cpp:1621-1780, 2880-3025,
 3116-3161) through facetcu_run_facetrt_core, against the reference's own
 makeSpectralOptics and solveCpu (oracle/_ref) run band by band on the same
-scene, graph and sun raster.
+scene, graph and sun raster; on flat ground and on a DEM (a GeoTIFF hill).
 
 Tolerances: band radiosity within 1e-5 relative (FP32 gather vs the
 reference's FP64-accumulated gather), the integer graph and the sunlit
@@ -15,18 +15,27 @@ import pytest
 
 from oracle.pyoracle import Graph
 from streamsim_gb300 import facetcu, scenes
+from tests import tiff_writer
 from tests.gpu_helpers import model_for, require_gpu
 from tests.test_project_host import _write_project
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def project(tmp_path_factory):
+@pytest.fixture(scope="module", params=["flat", "dem"])
+def project(tmp_path_factory, request):
     require_gpu()
     root = tmp_path_factory.mktemp("project")
+    control, scene = "<periodicNeighborCount>4</periodicNeighborCount>", ""
+    if request.param == "dem":  # a hill under the ground grid and the objects
+        y, x = np.mgrid[0:21, 0:17] / np.array([20.0, 16.0])[:, None, None]
+        z = 80.0 + 1.5 * np.exp(-((x - 0.3) ** 2 + (y - 0.6) ** 2) / 0.08)
+        tiff_writer.write(str(root / "hill.tif"), z.astype(np.float32), compression=8,
+                          predictor=3, tile=(16, 16))
+        control += "<isDEM>1</isDEM>"
+        scene = "<DEM>hill.tif</DEM>"
     path = _write_project(root, coefficients=False, bands="450,550,0.865,1650,10500",
-                          extra_control="<periodicNeighborCount>4</periodicNeighborCount>")
+                          extra_control=control, extra_scene=scene)
     return path, facetcu.Project(path)
 
 

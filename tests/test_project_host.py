@@ -77,7 +77,7 @@ def _spectra(coefficients):
 
 def _write_project(root, *, bands="450,550,0.865,1650,10500", size=(8.0, 6.0), voxel=0.5,
                    coefficients=True, extra_control="", heterogeneity="Hapke", objects=None,
-                   extra_spectral=""):
+                   extra_spectral="", extra_scene=""):
     root = str(root)
     for d in ("models", "positions", "spectra", "defined"):
         os.makedirs(os.path.join(root, d), exist_ok=True)
@@ -112,7 +112,7 @@ def _write_project(root, *, bands="450,550,0.865,1650,10500", size=(8.0, 6.0), v
 <Scene><sceneSizeX>{size[0]}</sceneSizeX><sceneSizeY>{size[1]}</sceneSizeY><Height>5</Height>
 <voxelSize>{voxel}</voxelSize><bgSpectral>soil</bgSpectral><bgThermal>soil_temperature</bgThermal>
 <bgBioName>soilset</bgBioName><backgroundHeterogeneity>{heterogeneity}</backgroundHeterogeneity>
-<backgroundAngularStrength>0.4</backgroundAngularStrength>
+<backgroundAngularStrength>0.4</backgroundAngularStrength>{extra_scene}
 <Object>{objects}</Object></Scene>
 <Attribute><Optical>{_spectra(coefficients)}{extra_spectral}</Optical><Thermal>
 <thermal name="building_temperature"><sunlitTemperature>310</sunlitTemperature>

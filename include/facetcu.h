@@ -594,6 +594,30 @@ int facetcu_faceteb_node(facetcu_context *ctx, const facetcu_energy_parameters *
                          const float *band_diffuse, facetcu_energy_fields *fields,
                          facetcu_energy_result *result);
 
+/* The sun of a FacetEB node.  The reference calls NREL's SPA (the vendored
+ * thirdparty/spa.h, SPA_ZA) from updateSolarPosition
+ * (facetrtcore.cpp:3290-3327); here the sun's coordinates follow Meeus's
+ * published formulas (about 0.01 deg from SPA) with SPA's input ranges,
+ * error codes and refraction.  facetcu_solar_input holds spa_data's inputs
+ * (spa.h: local time, hours east of UTC, degrees east/north, metres,
+ * millibars, degrees Celsius, delta_t in seconds).  zenith and azimuth
+ * (eastward from north) in degrees; *spa_error = SPA's error code (0, or
+ * 1-16 with FACETCU_INVALID_ARGUMENT). */
+typedef struct {
+    int32_t year, month, day, hour, minute, second;
+    double delta_t, timezone, longitude, latitude, elevation, pressure, temperature;
+    double atmos_refract;
+} facetcu_solar_input;
+int facetcu_solar_position(const facetcu_solar_input *input, double *zenith, double *azimuth,
+                           int32_t *spa_error);
+/* updateSolarPosition on one meteorology row: day of year and local time
+ * from julian_time (2019, UTC+8, whole minutes), the site's latitude and
+ * longitude, the row's pressure (at least 100 mbar) and air temperature.
+ * FACETCU_RUNTIME_ERROR "FacetEB solar-position calculation failed" as the
+ * reference throws. */
+int facetcu_faceteb_sun(float julian_time, float latitude, float longitude, float pressure,
+                        float air_temperature, float *zenith, float *azimuth);
+
 /* ---- sensor images (server.mjs:1127-1600, writeRadiosityTiffForAngle) ---- */
 /* The sensor of a project: image size, parallel or perspective projection,
  * view angles, field of view, scene extent and sensor position.  Values

@@ -213,12 +213,81 @@ def compile_project():
     subprocess.run(cmd, check=True)
 
 
+# The sun of a FacetEB node: the reference's vendored SPA
+# (thirdparty/spa.cpp, compiled where it lies) under runFacetEBCore's
+# MeteoStep and updateSolarPosition (facetrtcore.cpp:3172-3181, 3290-3327)
+# and the Utils date helpers they call (utils.cpp:572-632).
+SPA_SRC = os.path.join(OUT, "spa_ref.cpp")
+SPA_LIB = os.path.join(OUT, "libspa_ref.so")
+THIRDPARTY = os.path.join(REFERENCE, "models", "histream", "src", "thirdparty")
+SPA_RANGES = [
+    ("@", 0, 0, "declarations", None),
+    ("base/utils.cpp", 572, 632, None, None),
+    ("@", 0, 0, "open", None),
+    ("facetrt/facetrtcore.cpp", 3172, 3181, None, None),
+    ("facetrt/facetrtcore.cpp", 3290, 3327, None, None),
+    ("@", 0, 0, "close", None),
+]
+SPA_ANCHORS = [
+    ("base/utils.cpp", 572, "double Utils::calculateDeltaT(int year, int month) {"),
+    ("base/utils.cpp", 611, "bool Utils::isLeapYear(int year) {"),
+    ("base/utils.cpp", 615, "void Utils::calculateMonthAndDay(int kyear, int kdoy, int *kmonth"),
+    ("base/utils.cpp", 632, "}"),
+    ("facetrt/facetrtcore.cpp", 3172, "struct MeteoStep {"),
+    ("facetrt/facetrtcore.cpp", 3290, "const auto updateSolarPosition = [&](const MeteoStep& step) {"),
+    ("facetrt/facetrtcore.cpp", 3327, "};"),
+]
+
+
+def _sections(name):
+    with open(os.path.join(HERE, name), encoding="utf-8") as f:
+        text = f.read()
+    sections, current = {}, None
+    for line in text.split("\n"):
+        if line.startswith("//@@ "):
+            current = line[5:].strip()
+            sections[current] = []
+        elif current:
+            sections[current].append(line)
+    return sections
+
+
+def generate_spa():
+    src = os.path.join(REFERENCE, "models", "histream", "src")
+    read = lambda name: open(os.path.join(src, name), encoding="utf-8").read().split("\n")
+    cache = {}
+    for name, line, text in SPA_ANCHORS:
+        lines = cache.setdefault(name, read(name))
+        if not lines[line - 1].lstrip().startswith(text):
+            raise SystemExit(f"build_ref: {name}:{line} does not start with {text!r}")
+    sections = _sections("ref_spa_shim.inc")
+    parts = [PRELUDE]
+    for name, lo, hi, before, _ in SPA_RANGES:
+        if name == "@":
+            parts.extend(sections[before])
+            continue
+        parts.append(f"// ---- {name}:{lo}-{hi}")
+        parts.extend(cache.setdefault(name, read(name))[lo - 1:hi])
+    os.makedirs(OUT, exist_ok=True)
+    with open(SPA_SRC, "w", encoding="utf-8") as f:
+        f.write("\n".join(parts) + "\n")
+
+
+def compile_spa():
+    cmd = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-fPIC", "-shared", "-w",
+           "-I", THIRDPARTY, SPA_SRC, os.path.join(THIRDPARTY, "spa.cpp"), "-o", SPA_LIB]
+    subprocess.run(cmd, check=True)
+
+
 def main():
     if os.path.isdir(FACETRT):
         generate()
-        # the project loader oracle is used by CPU tests only, here
+        # the project loader and solar-position oracles are used by CPU
+        # tests only, here
         generate_project()
         compile_project()
+        generate_spa()
+        compile_spa()
     elif not os.path.exists(SRC):
         print("build_ref: reference tree absent and no generated source; skipping",
               file=sys.stderr)

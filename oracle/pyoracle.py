@@ -685,3 +685,41 @@ class ReferenceProject:
         return dict(info=d, vertices=vertices, material_indices=mi, materials=materials,
                     object=params[0], ground=params[1], wavelengths=wavelengths,
                     texture_factors=tex)
+
+
+SPA_LIB = os.path.join(HERE, "_ref", "libspa_ref.so")
+
+
+class ReferenceSun:
+    """The reference's own SPA (thirdparty/spa.cpp) and FacetEB
+    updateSolarPosition (compiled by oracle/build_ref.py into
+    oracle/_ref/libspa_ref.so; built only where the reference tree is
+    present)."""
+
+    def __init__(self, path=SPA_LIB):
+        self.lib = C.CDLL(path)
+        self.lib.ref_faceteb_sun.argtypes = [C.c_float] * 5 + [C.POINTER(C.c_float)] * 2
+        self.lib.ref_spa_za.argtypes = [C.c_int] * 6 + [C.c_double] * 8 + \
+            [C.POINTER(C.c_double)] * 2
+        self.lib.ref_delta_t.restype = C.c_double
+        self.lib.ref_delta_t.argtypes = [C.c_int, C.c_int]
+
+    def faceteb_sun(self, julian_time, latitude, longitude, pressure, air_temperature):
+        """(zenith, azimuth) as float32, or None where the reference throws."""
+        z, a = C.c_float(), C.c_float()
+        if self.lib.ref_faceteb_sun(julian_time, latitude, longitude, pressure, air_temperature,
+                                    C.byref(z), C.byref(a)):
+            return None
+        return np.float32(z.value), np.float32(a.value)
+
+    def spa_za(self, year, month, day, hour, minute, second, *, delta_t, timezone, longitude,
+               latitude, elevation, pressure, temperature, atmos_refract):
+        """(SPA error code, zenith, azimuth)."""
+        z, a = C.c_double(), C.c_double()
+        err = self.lib.ref_spa_za(year, month, day, hour, minute, second, delta_t, timezone,
+                                  longitude, latitude, elevation, pressure, temperature,
+                                  atmos_refract, C.byref(z), C.byref(a))
+        return err, z.value, a.value
+
+    def delta_t(self, year, month):
+        return self.lib.ref_delta_t(year, month)

@@ -224,6 +224,13 @@ def sensor(width=512, height=512, perspective=False, vza=0.0, vaa=0.0, fov=0.0, 
                   (C.c_double * 3)(*position), sky_temperature, 1 if temperature_output else 0)
 
 
+class SolarInput(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("year", "month", "day", "hour", "minute", "second")] + \
+               [(n, C.c_double) for n in ("delta_t", "timezone", "longitude", "latitude",
+                                          "elevation", "pressure", "temperature",
+                                          "atmos_refract")]
+
+
 class ProjectInfo(C.Structure):
     _fields_ = [("facet_count", C.c_uint32), ("leaf_facet_count", C.c_uint32),
                 ("material_count", C.c_uint32), ("band_count", C.c_uint32),
@@ -313,6 +320,10 @@ SIGNATURES.update({
                                                C.POINTER(_u32)]),
     "facetcu_project_spectral_parameters": (C.c_int, [_vp, C.POINTER(SpectralParameters)]),
     "facetcu_project_xml_view": (C.c_int, [C.c_char_p, _vp, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "facetcu_solar_position": (C.c_int, [C.POINTER(SolarInput), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+    "facetcu_faceteb_sun": (C.c_int, [C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                      C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "facetcu_dem_height_field": (C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                            C.POINTER(C.c_float), _vp, C.c_uint64]),
 })
@@ -590,6 +601,28 @@ def project_xml_view(path):
     buf = C.create_string_buffer(n.value + 1)
     _host_check(lib.facetcu_project_xml_view(os.fsencode(path), buf, n.value + 1, C.byref(n)))
     return buf.value.decode("utf-8")
+
+
+def solar_position(year, month, day, hour, minute, second, *, timezone, longitude, latitude,
+                   delta_t=0.0, elevation=0.0, pressure=1010.0, temperature=10.0,
+                   atmos_refract=0.5667):
+    """The sun's topocentric (zenith, azimuth) in degrees, azimuth eastward
+    from north (spa_data's inputs and SPA_ZA's outputs)."""
+    lib = load()
+    inp = SolarInput(year, month, day, hour, minute, second, delta_t, timezone, longitude,
+                     latitude, elevation, pressure, temperature, atmos_refract)
+    z, a, err = C.c_double(), C.c_double(), C.c_int32()
+    _host_check(lib.facetcu_solar_position(C.byref(inp), C.byref(z), C.byref(a), C.byref(err)))
+    return z.value, a.value
+
+
+def faceteb_sun(julian_time, latitude, longitude, pressure, air_temperature):
+    """updateSolarPosition: a FacetEB node's (zenith, azimuth) as float32."""
+    lib = load()
+    z, a = C.c_float(), C.c_float()
+    _host_check(lib.facetcu_faceteb_sun(julian_time, latitude, longitude, pressure,
+                                        air_temperature, C.byref(z), C.byref(a)))
+    return np.float32(z.value), np.float32(a.value)
 
 
 def dem_height_field(path):

@@ -18,9 +18,13 @@ formats:
                                            float32 little-endian)
   faceteb.json                             :4085-4139
 
-The sun position of each node comes from the caller (the reference computes
-it with NREL's solar position algorithm from the node's date and the site's
-latitude and longitude; that algorithm is not part of this package).
+  solar_sun                                :3290-3327 (updateSolarPosition)
+
+The sun of each node is the caller's sun_for(row) or, by default,
+updateSolarPosition's: the node's date and local time (2019, UTC+8) at the
+site's latitude and longitude, through facetcu_faceteb_sun (the reference
+calls NREL's SPA there; the library follows Meeus's published solar
+formulas, about 0.01 deg from SPA).
 """
 import json
 import math
@@ -71,6 +75,15 @@ def time_token(julian_time):
         day += minutes // 1440
         minutes %= 1440
     return f"DOY{day}_{minutes // 60:02d}-{minutes % 60:02d}"
+
+
+def solar_sun(latitude=40.0, longitude=116.0):
+    """sun_for(row) -> (zenith, azimuth) of updateSolarPosition at the site
+    (<Latitude>, <Longitude>; the reference's defaults 40 N, 116 E)."""
+    def sun_for(row):
+        return facetcu.faceteb_sun(row["julian_time"], latitude, longitude, row["pressure"],
+                                   row["air_temperature"])
+    return sun_for
 
 
 def _meteo(row):
@@ -129,11 +142,13 @@ class Run:
                                              windows if count else None, temperature, bd, bf)
         return fields, res, lit
 
-    def run(self, meteorology, sun_for, start_node=0, end_node=None, output_dir=None,
-            vertices=None, graph=None, progress=print):
+    def run(self, meteorology, sun_for=None, start_node=0, end_node=None, output_dir=None,
+            vertices=None, graph=None, progress=print, latitude=40.0, longitude=116.0):
         """Nodes [start_node, end_node) of the meteorology rows.  Writes the
         reference's step records and faceteb.json under output_dir when
-        given.  Returns the per-node results and the last node's fields."""
+        given.  sun_for defaults to solar_sun(latitude, longitude).  Returns
+        the per-node results and the last node's fields."""
+        sun_for = sun_for or solar_sun(latitude, longitude)
         end_node = len(meteorology) if end_node is None else end_node
         if end_node > len(meteorology):
             raise RuntimeError("FacetEB time range exceeds meteorology rows")

@@ -251,3 +251,26 @@ def test_node_sequence_writes_the_reference_records(reference, site, tmp_path):
     doc = json.loads((tmp_path / "faceteb.json").read_text())
     assert doc["time"] == "DOY172_21-00" and len(doc["temperature"]) == sc.surface_count
     assert len(doc["vertexPositions"]) == 9 * sc.facet_count
+
+
+def test_node_sequence_places_the_sun_by_date(site, tmp_path):
+    """Without a caller's sun, each node's sun is updateSolarPosition's for
+    the row's date and local time at the site (facetcu_faceteb_sun): the
+    step records' sunlit column is the raster of that sun."""
+    from streamsim_gb300 import faceteb
+    sc, m = site["scene"], site["model"]
+    rows = [dict(DAY, node=0, julian_time=172.375), dict(DAY, node=1, julian_time=172.5)]
+    run = faceteb.Run(m, sc.leaf_count, site["materials"], site["mi"], site["tex"],
+                      spectrum=site["spectrum"], coupling_iterations=3)
+    results, _ = run.run(rows, output_dir=str(tmp_path), progress=None, latitude=35.0,
+                         longitude=110.0)
+    assert len(results) == 2
+    for r in rows:
+        zen, az = facetcu.faceteb_sun(r["julian_time"], 35.0, 110.0, r["pressure"],
+                                      r["air_temperature"])
+        assert 0.0 < zen < 80.0
+        lit = m.computeSunlitFraction(facetcu.sun_direction(zen, az))
+        rec = np.fromfile(tmp_path / ".facet_steps" /
+                          f"energy_T={faceteb.time_token(r['julian_time'])}.bin",
+                          "<f4").reshape(sc.surface_count, 9)
+        assert np.array_equal(rec[:, 8], lit) and lit.max() > 0.0

@@ -409,7 +409,9 @@ __device__ __forceinline__ void publish_stats(const float* md, const float* mb, 
     publish_cols<NC>(md, mb, mr, lane * NC, lane < P, P, stats);
 }
 
-// One full FP32 sweep B_out = Q + K B_in over a wide panel.
+// One full FP32 sweep B_out = Q + K B_in over a wide panel.  Bin == nullptr
+// stands for B_in = 0 (the first sweep of a solve that starts from zero):
+// the gather is skipped, which gives the same bits as gathering zeros.
 template <int P>
 __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_sweep_wide(GraphView g, PanelParams pp,
                                                             const float* __restrict__ Bin,
@@ -441,7 +443,7 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_sweep_wide(GraphVie
                 float acc[CPL];
 #pragma unroll
                 for (int k = 0; k < CPL; ++k) acc[k] = 0.0f;
-                gather_split<P, false>(g.rows, g.packed, g.edges, g.nb_bits, s, Bin, lane, acc);
+                if (Bin) gather_split<P, false>(g.rows, g.packed, g.edges, g.nb_bits, s, Bin, lane, acc);
                 const uint32_t d = __ldg(g.denom + s);
                 const float skyc = float(__ldg(g.skyc + s));
                 float dir[CPL];
@@ -460,8 +462,13 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_sweep_wide(GraphVie
                 load4(pp.rho + i1, r1);
                 load4(pp.tau + i0, t0);
                 load4(pp.tau + i1, t1);
-                load4(Bin + i0, o0);
-                load4(Bin + i1, o1);
+                if (Bin) {
+                    load4(Bin + i0, o0);
+                    load4(Bin + i1, o1);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < CPL; ++k) o0[k] = o1[k] = 0.0f;
+                }
 #pragma unroll
                 for (int k = 0; k < CPL; ++k) {
                     b0[k] = e0[k] + r0[k] * h[0][k] + t0[k] * h[1][k];
@@ -944,7 +951,8 @@ __global__ void k_init_i8(const float* __restrict__ X, const float* __restrict__
     Q[i] = int8_t(sg > 0.0f ? max(-127, min(127, __float2int_rn(r / sg))) : 0);
 }
 
-// Narrow-panel sweep (FP32 or FP64 state; also used for the FP64 truth).
+// Narrow-panel sweep (FP32 or FP64 state; also used for the FP64 truth);
+// Bin == nullptr stands for B_in = 0, as in the wide sweep.
 template <int P, typename T>
 __global__ void __launch_bounds__(kWarps * 32) k_sweep(GraphView g, PanelParams pp, const T* Bin,
                                                        T* Bout, uint32_t* stats,
@@ -965,7 +973,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep(GraphView g, PanelParams 
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             const uint32_t s = s0 + k;
-            const Acc acc = gather_narrow<P, T, Acc>(g, s, Bin, lane);
+            const Acc acc = Bin ? gather_narrow<P, T, Acc>(g, s, Bin, lane) : Acc(0);
             const uint32_t d = g.denom[s];
             const Acc dir = Acc(pp.direct[size_t(s) * P + col]);
             h[k] = (d == 0u ? L : (Acc(g.skyc[s]) * L + acc) / Acc(d)) + dir;
@@ -974,7 +982,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep(GraphView g, PanelParams 
             const size_t i0 = size_t(s0) * P + col, i1 = size_t(s1) * P + col;
             const Acc b0 = Acc(pp.emis[i0]) + Acc(pp.rho[i0]) * h[0] + Acc(pp.tau[i0]) * h[1];
             const Acc b1 = Acc(pp.emis[i1]) + Acc(pp.rho[i1]) * h[1] + Acc(pp.tau[i1]) * h[0];
-            const Acc o0 = Bin[i0], o1 = Bin[i1];
+            const Acc o0 = Bin ? Bin[i0] : Acc(0), o1 = Bin ? Bin[i1] : Acc(0);
             Bout[i0] = b0;
             Bout[i1] = b1;
             md[0] = fmaxf(md[0], fmaxf(absf(b0 - o0), absf(b1 - o1)));
@@ -1712,6 +1720,8 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
             k_panel_in<float><<<blocks_for(cells, 256), 256, 0, s>>>(
                 init, S, R, c0, P, order, reinterpret_cast<float*>(x0));
         FCU_LAUNCH("k_panel_in");
+        // A solve from zero: its first sweep gathers nothing (null input).
+        const bool zero_start = init == nullptr;
 
         uint32_t it = 0;
         int cur = 0;
@@ -1721,7 +1731,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                 const uint32_t batch = std::min(timed ? 1u : check_every, max_it - it);
                 for (uint32_t k = 0; k < batch; ++k) {
                     const uint32_t sweep = it + k;
-                    char* in = (sweep & 1u) ? x1 : x0;
+                    char* in = sweep == 0 && zero_start ? nullptr : (sweep & 1u) ? x1 : x0;
                     char* out = (sweep & 1u) ? x0 : x1;
                     timed_sweep(false, [&] {
                         if (fp64)
@@ -1765,7 +1775,8 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
             float* slot[2] = {sig, sig + kMaxP};
             while (it < max_it) {
                 timed_sweep(false, [&] {
-                    launch_sweep<float>(P, g, pp, X, Y, stats, counter, flag, s);
+                    launch_sweep<float>(P, g, pp, it == 0 && zero_start ? nullptr : X, Y, stats,
+                                        counter, flag, s);
                 });
                 k_check<<<1, kMaxP, 0, s>>>(stats, flag, P, tol, it, counter, slot[0], slot[1],
                                             nullptr, true, colmax, cheb, 1);
@@ -1870,7 +1881,8 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
             float* Y = reinterpret_cast<float*>(x1);
             while (it < max_it) {
                 timed_sweep(false, [&] {
-                    launch_sweep<float>(P, g, pp, X, Y, stats, counter, flag, s);
+                    launch_sweep<float>(P, g, pp, it == 0 && zero_start ? nullptr : X, Y, stats,
+                                        counter, flag, s);
                 });
                 k_check<<<1, kMaxP, 0, s>>>(stats, flag, P, tol, it, counter, nullptr, nullptr,
                                             nullptr, true, colmax);

@@ -102,7 +102,87 @@ def barrier(world):
 
 
 # ---- clocks ------------------------------------------------------------------
-class ClockSampler:
+class NvmlClocks:
+    """Read-only NVML queries (the driver's libnvidia-ml through ctypes): the
+    SM clock, its maximum and the active clock-event reasons, every 2 ms
+    from a thread while the timed region runs."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, gpu):
+        import ctypes as C
+
+        import torch
+        self.C = C
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.lib = lib
+        self.handle = C.c_void_p()
+        bus = None
+        try:
+            props = torch.cuda.get_device_properties(gpu)
+            bus = "%08x:%02x:%02x.0" % (props.pci_domain_id, props.pci_bus_id,
+                                        props.pci_device_id)
+        except (AttributeError, RuntimeError):
+            pass
+        rc = 1
+        if bus:
+            rc = lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), C.byref(self.handle))
+        if rc != 0:
+            rc = lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(gpu), C.byref(self.handle))
+        if rc != 0:
+            raise OSError("no NVML handle")
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.reasons_fn = reasons
+        mx = C.c_uint(0)
+        lib.nvmlDeviceGetMaxClockInfo(self.handle, C.c_int(1), C.byref(mx))  # NVML_CLOCK_SM
+        self.max_mhz = float(mx.value)
+        self.samples = []
+        self.stop = threading.Event()
+
+    def _run(self):
+        C = self.C
+        mhz, mask = C.c_uint(0), C.c_ulonglong(0)
+        while not self.stop.is_set():
+            if self.lib.nvmlDeviceGetClockInfo(self.handle, C.c_int(1), C.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.handle, C.byref(mask)) == 0:
+                self.samples.append((float(mhz.value), int(mask.value)))
+            time.sleep(0.002)
+
+    def __enter__(self):
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        self.thread.start()
+        return self
+
+    def __exit__(self, *exc):
+        self.stop.set()
+        self.thread.join(timeout=5)
+        self.lib.nvmlShutdown()
+
+    def summary(self):
+        reasons = set()
+        for _, mask in self.samples:
+            for bit, name in self.REASONS.items():
+                if mask & bit:
+                    reasons.add(name)
+        sm = [m for m, _ in self.samples]
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvml, 2 ms"}
+
+
+def ClockSampler(gpu):
+    """Clock sampling for the timed region: NVML when the driver library
+    loads, else nvidia-smi."""
+    try:
+        return NvmlClocks(gpu)
+    except Exception:  # no driver library or symbol: nvidia-smi instead
+        return SmiClockSampler(gpu)
+
+
+class SmiClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -154,7 +234,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi, 200 ms"}
 
 
 # ---- workload ---------------------------------------------------------------

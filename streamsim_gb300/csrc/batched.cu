@@ -516,7 +516,7 @@ __device__ __forceinline__ void edge_word_i(const uint32_t* __restrict__ packed,
                                             uint32_t e, uint32_t nb_bits, uint32_t& nb, int& c)
 {
     if (packed) {
-        const uint32_t w = __ldg(packed + e);
+        const uint32_t w = __ldcs(packed + e);  // read once per step: evict first
         nb = w & ((1u << nb_bits) - 1u);
         c = int(w >> nb_bits);
     } else {
@@ -610,7 +610,7 @@ __device__ __forceinline__ void gather_i8(const uint32_t* __restrict__ rows,
             const uint32_t nb = __shfl_sync(0xffffffffu, nbv[(u * G) >> 5], src);
             c[u] = __shfl_sync(0xffffffffu, cv[(u * G) >> 5], src);
             if (base + uint32_t(u * G + grp) < end) {
-                q[u] = __ldg(Q16 + size_t(nb) * L + sub);
+                q[u] = __ldcg(Q16 + size_t(nb) * L + sub);  // L2 only: rows rarely repeat in L1
             } else {
                 q[u] = make_uint4(0u, 0u, 0u, 0u);
                 c[u] = 0;
@@ -679,23 +679,28 @@ __device__ __forceinline__ int i8_offset(int grp)
     return off;
 }
 
+// Per-cell planes of the int8 step (rho, tau, X, R) are read and written
+// once per step: streaming loads and stores (evict first), so that L2 keeps
+// the gathered int8 rows.  The gather itself loads through L2 only (__ldcg)
+// and the packed edge words stream (__ldcs): 4 % faster at 64 columns on
+// the config-2 forest than plain loads.
 template <int N> struct VecN;
 template <> struct VecN<1> {
-    static __device__ __forceinline__ void ld(const float* p, float* v) { v[0] = *p; }
-    static __device__ __forceinline__ void st(float* p, const float* v) { *p = v[0]; }
+    static __device__ __forceinline__ void ld(const float* p, float* v) { v[0] = __ldcs(p); }
+    static __device__ __forceinline__ void st(float* p, const float* v) { __stcs(p, v[0]); }
     static __device__ __forceinline__ void ldq(const int8_t* p, int* v) { v[0] = *p; }
     static __device__ __forceinline__ void stq(int8_t* p, const int* v) { *p = int8_t(v[0]); }
 };
 template <> struct VecN<2> {
     static __device__ __forceinline__ void ld(const float* p, float* v)
     {
-        const float2 q = *reinterpret_cast<const float2*>(p);
+        const float2 q = __ldcs(reinterpret_cast<const float2*>(p));
         v[0] = q.x;
         v[1] = q.y;
     }
     static __device__ __forceinline__ void st(float* p, const float* v)
     {
-        *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+        __stcs(reinterpret_cast<float2*>(p), make_float2(v[0], v[1]));
     }
     static __device__ __forceinline__ void ldq(const int8_t* p, int* v)
     {
@@ -709,8 +714,18 @@ template <> struct VecN<2> {
     }
 };
 template <> struct VecN<4> {
-    static __device__ __forceinline__ void ld(const float* p, float* v) { load4(p, v); }
-    static __device__ __forceinline__ void st(float* p, const float* v) { store4(p, v); }
+    static __device__ __forceinline__ void ld(const float* p, float* v)
+    {
+        const float4 q = __ldcs(reinterpret_cast<const float4*>(p));
+        v[0] = q.x;
+        v[1] = q.y;
+        v[2] = q.z;
+        v[3] = q.w;
+    }
+    static __device__ __forceinline__ void st(float* p, const float* v)
+    {
+        __stcs(reinterpret_cast<float4*>(p), make_float4(v[0], v[1], v[2], v[3]));
+    }
     static __device__ __forceinline__ void ldq(const int8_t* p, int* v)
     {
         const char4 q = *reinterpret_cast<const char4*>(p);

@@ -270,6 +270,57 @@ def build_workload(args, fc, scenes, oracle_mod=None):
                 sun=sun, lit=lit)
 
 
+def energy_metrics(m, w, solutions, dev):
+    """FP64 energy accounting of radiosity solutions (bands, S) on the
+    solver's own graph, computed with a torch sparse matrix on the device
+    (independent of the library's kernels).  Per band b, with the graph's
+    counts, denominators and sky counts:
+      H_s = (sky_s L_b + sum_e count_e B_n) / denom_s + D_s   (L_b + D_s when
+            denom_s = 0),   D_s = beam_b dgeo_s,
+      T(B)_s = rho_s H_s + tau_s H_(s^1)   (no emission here);
+    closure_b = |sum_s w_s (T(B) - B)_s| / (sum_s w_s D_s + sum_s sky_s L_b)
+    with w_s = denom_s: for symmetric counts and equal denominators on the
+    two sides of a facet (the raster graph) this is exactly the relative
+    defect of the energy balance sum w D + sum sky L = sum w (1 - rho -
+    tau_(s^1)) H + sum sky B; absorbed_b = sum_s A_s (1 - rho_s -
+    tau_(s^1)) H_s with A_s the facet's area.  Returns one dict per
+    solution: max closure over bands and the absorbed energy per band."""
+    import warnings
+
+    import torch
+    rows, nbrs, counts, denom, skyc = m.graph()
+    S = len(denom)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")  # torch's beta notice for sparse CSR
+        A = torch.sparse_csr_tensor(torch.from_numpy(rows.astype(np.int64)),
+                                    torch.from_numpy(nbrs.astype(np.int64)),
+                                    torch.from_numpy(counts.astype(np.float64)),
+                                    size=(S, S)).to(dev)
+    den = torch.from_numpy(denom.astype(np.float64)).to(dev)[:, None]
+    skv = torch.from_numpy(skyc.astype(np.float64)).to(dev)[:, None]
+    L = torch.from_numpy(np.asarray(w["sky"], np.float64)).to(dev)[None, :]
+    D = torch.from_numpy(np.asarray(w["dgeo"][0], np.float64)).to(dev)[:, None] * \
+        torch.from_numpy(np.asarray(w["beam"], np.float64)).to(dev)[None, :]
+    rho = torch.from_numpy(np.ascontiguousarray(w["rho"].T, np.float64)).to(dev)
+    tau = torch.from_numpy(np.ascontiguousarray(w["tau"].T, np.float64)).to(dev)
+    pair = torch.arange(S, device=dev) ^ 1
+    v = np.asarray(w["scene"].vertices, np.float64).reshape(-1, 3, 6)[:, :, :3]
+    area = 0.5 * np.linalg.norm(np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]), axis=1)
+    area = torch.from_numpy(np.repeat(area, 2)).to(dev)[:, None]
+    sources = (den * D).sum(0) + (skv * L).sum(0)
+    out = []
+    for sol in solutions:
+        Bm = torch.from_numpy(np.ascontiguousarray(np.asarray(sol, np.float64).T)).to(dev)
+        G = torch.sparse.mm(A, Bm)
+        H = torch.where(den > 0, (skv * L + G) / den.clamp(min=1.0), L) + D
+        r = rho * H + tau * H[pair] - Bm
+        closure = ((den * r).sum(0).abs() / sources).max().item()
+        absorbed = (area * (1.0 - rho - tau[pair]) * H).sum(0)
+        out.append({"closure": closure, "absorbed": absorbed.cpu().numpy()})
+    del A
+    return out
+
+
 def workload_name(args, w):
     sc = w["scene"]
     return (f"{'config1' if args.quick else 'config2'} forest: {sc.facet_count:,} facets, "
@@ -374,6 +425,17 @@ def run_gpu(args, rank, world, local):
     err_out = out.cpu().numpy()
     scale = np.maximum(np.abs(truth), 1e-6 * np.abs(truth).max())
     err = float(np.max(np.abs(err_out - truth) / scale))
+    # per side and band against the band's own floor (1e-6 of its max)
+    rel = np.abs(err_out - truth) / np.maximum(np.abs(truth),
+                                               1e-6 * np.abs(truth).max(1, keepdims=True))
+    ours_e, truth_e = energy_metrics(m, w, [err_out, truth], dev)
+    energy = {"closure_residual": ours_e["closure"],
+              "closure_residual_fp64": truth_e["closure"],
+              "absorbed_rel_err_vs_fp64": float(np.max(np.abs(ours_e["absorbed"] - truth_e["absorbed"]) /
+                                                      np.abs(truth_e["absorbed"]))),
+              "weights": "closure: count weights w_s = denom_s over sources; absorbed: facet areas",
+              "rel_err_per_side": {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
+                                   "floor": "1e-6 of the band's max"}}
 
     times = []
     launches = []
@@ -501,7 +563,8 @@ def run_gpu(args, rank, world, local):
                            "iterations_from_zero": cold["iterations"] if cold else None,
                            "weights": "streamsim_gb300/data/mlp_warm_start.npy"
                            if use_mlp else None},
-            "roofline": roofline, "e2e": e2e, "gpu_launches": int(np.mean(launches)),
+            "roofline": roofline, "e2e": e2e, "energy": energy,
+            "gpu_launches": int(np.mean(launches)),
             "clocks": clocks.summary(), "plain_fp32": plain,
             "speedup_vs_plain_fp32": (value / plain["value"]) if plain else None,
             "cpu_baseline": cpu,

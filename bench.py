@@ -270,21 +270,23 @@ def build_workload(args, fc, scenes, oracle_mod=None):
                 sun=sun, lit=lit)
 
 
-def energy_metrics(m, w, solutions, dev):
-    """FP64 energy accounting of radiosity solutions (bands, S) on the
-    solver's own graph, computed with a torch sparse matrix on the device
-    (independent of the library's kernels).  Per band b, with the graph's
-    counts, denominators and sky counts:
+def energy_metrics(m, vertices, rho, tau, sky, beam, dgeo, solutions, dev, emission=None):
+    """FP64 energy accounting of radiosity solutions (bands, S) of one sun
+    (direct geometry dgeo, S) on the solver's own graph, computed with a
+    torch sparse matrix on the device (independent of the library's
+    kernels).  Per band b, with the graph's counts, denominators and sky
+    counts:
       H_s = (sky_s L_b + sum_e count_e B_n) / denom_s + D_s   (L_b + D_s when
             denom_s = 0),   D_s = beam_b dgeo_s,
-      T(B)_s = rho_s H_s + tau_s H_(s^1)   (no emission here);
-    closure_b = |sum_s w_s (T(B) - B)_s| / (sum_s w_s D_s + sum_s sky_s L_b)
-    with w_s = denom_s: for symmetric counts and equal denominators on the
-    two sides of a facet (the raster graph) this is exactly the relative
-    defect of the energy balance sum w D + sum sky L = sum w (1 - rho -
-    tau_(s^1)) H + sum sky B; absorbed_b = sum_s A_s (1 - rho_s -
-    tau_(s^1)) H_s with A_s the facet's area.  Returns one dict per
-    solution: max closure over bands and the absorbed energy per band."""
+      T(B)_s = e_s + rho_s H_s + tau_s H_(s^1);
+    closure_b = |sum_s w_s (T(B) - B)_s| / (sum_s w_s (D_s + e_s) +
+    sum_s sky_s L_b) with w_s = denom_s: for symmetric counts and equal
+    denominators on the two sides of a facet (the raster graph) this is
+    exactly the relative defect of the energy balance sum w D + sum sky L +
+    sum w e = sum w (1 - rho - tau_(s^1)) H + sum sky B; absorbed_b =
+    sum_s A_s (1 - rho_s - tau_(s^1)) H_s with A_s the facet's area.
+    Returns one dict per solution: max closure over bands and the absorbed
+    energy per band."""
     import warnings
 
     import torch
@@ -296,29 +298,56 @@ def energy_metrics(m, w, solutions, dev):
                                     torch.from_numpy(nbrs.astype(np.int64)),
                                     torch.from_numpy(counts.astype(np.float64)),
                                     size=(S, S)).to(dev)
-    den = torch.from_numpy(denom.astype(np.float64)).to(dev)[:, None]
-    skv = torch.from_numpy(skyc.astype(np.float64)).to(dev)[:, None]
-    L = torch.from_numpy(np.asarray(w["sky"], np.float64)).to(dev)[None, :]
-    D = torch.from_numpy(np.asarray(w["dgeo"][0], np.float64)).to(dev)[:, None] * \
-        torch.from_numpy(np.asarray(w["beam"], np.float64)).to(dev)[None, :]
-    rho = torch.from_numpy(np.ascontiguousarray(w["rho"].T, np.float64)).to(dev)
-    tau = torch.from_numpy(np.ascontiguousarray(w["tau"].T, np.float64)).to(dev)
+    del rows, nbrs, counts
+    f64 = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.float64))).to(dev)
+    den = f64(denom)[:, None]
+    skv = f64(skyc)[:, None]
+    L = f64(sky)[None, :]
+    D = f64(dgeo)[:, None] * f64(beam)[None, :]
+    rho_t = f64(np.asarray(rho).T)
+    tau_t = f64(np.asarray(tau).T)
+    e = f64(np.asarray(emission).T) if emission is not None else torch.zeros_like(rho_t)
     pair = torch.arange(S, device=dev) ^ 1
-    v = np.asarray(w["scene"].vertices, np.float64).reshape(-1, 3, 6)[:, :, :3]
+    v = np.asarray(vertices, np.float64).reshape(-1, 3, 6)[:, :, :3]
     area = 0.5 * np.linalg.norm(np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]), axis=1)
-    area = torch.from_numpy(np.repeat(area, 2)).to(dev)[:, None]
-    sources = (den * D).sum(0) + (skv * L).sum(0)
+    area = f64(np.repeat(area, 2))[:, None]
+    sources = (den * (D + e)).sum(0) + (skv * L).sum(0)
     out = []
     for sol in solutions:
-        Bm = torch.from_numpy(np.ascontiguousarray(np.asarray(sol, np.float64).T)).to(dev)
+        Bm = f64(np.asarray(sol).T)
         G = torch.sparse.mm(A, Bm)
         H = torch.where(den > 0, (skv * L + G) / den.clamp(min=1.0), L) + D
-        r = rho * H + tau * H[pair] - Bm
+        r = e + rho_t * H + tau_t * H[pair] - Bm
         closure = ((den * r).sum(0).abs() / sources).max().item()
-        absorbed = (area * (1.0 - rho - tau[pair]) * H).sum(0)
+        absorbed = (area * (1.0 - rho_t - tau_t[pair]) * H).sum(0)
         out.append({"closure": closure, "absorbed": absorbed.cpu().numpy()})
+        del Bm, G, H, r
     del A
+    torch.cuda.empty_cache()
     return out
+
+
+def energy_report(m, vertices, rho, tau, sky, beam, dgeo_rows, got, truth, dev, emission=None):
+    """The bench line's energy object: solutions (suns x bands, S) in
+    sun-major blocks of len(sky) bands, one direct-geometry row per sun."""
+    B = len(sky)
+    closure = closure64 = absorbed_err = 0.0
+    for k, dgeo in enumerate(dgeo_rows):
+        sl = slice(k * B, (k + 1) * B)
+        ours_e, truth_e = energy_metrics(m, vertices, rho, tau, sky, beam, dgeo,
+                                         [got[sl], truth[sl]], dev, emission)
+        closure = max(closure, ours_e["closure"])
+        closure64 = max(closure64, truth_e["closure"])
+        absorbed_err = max(absorbed_err, float(np.max(
+            np.abs(ours_e["absorbed"] - truth_e["absorbed"]) / np.abs(truth_e["absorbed"]))))
+    # per side and band against the band's own floor (1e-6 of its max)
+    rel = np.abs(got - truth) / np.maximum(np.abs(truth),
+                                           1e-6 * np.abs(truth).max(1, keepdims=True))
+    return {"closure_residual": closure, "closure_residual_fp64": closure64,
+            "absorbed_rel_err_vs_fp64": absorbed_err,
+            "weights": "closure: count weights w_s = denom_s over sources; absorbed: facet areas",
+            "rel_err_per_side": {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
+                                 "floor": "1e-6 of the band's max"}}
 
 
 def workload_name(args, w):
@@ -425,17 +454,8 @@ def run_gpu(args, rank, world, local):
     err_out = out.cpu().numpy()
     scale = np.maximum(np.abs(truth), 1e-6 * np.abs(truth).max())
     err = float(np.max(np.abs(err_out - truth) / scale))
-    # per side and band against the band's own floor (1e-6 of its max)
-    rel = np.abs(err_out - truth) / np.maximum(np.abs(truth),
-                                               1e-6 * np.abs(truth).max(1, keepdims=True))
-    ours_e, truth_e = energy_metrics(m, w, [err_out, truth], dev)
-    energy = {"closure_residual": ours_e["closure"],
-              "closure_residual_fp64": truth_e["closure"],
-              "absorbed_rel_err_vs_fp64": float(np.max(np.abs(ours_e["absorbed"] - truth_e["absorbed"]) /
-                                                      np.abs(truth_e["absorbed"]))),
-              "weights": "closure: count weights w_s = denom_s over sources; absorbed: facet areas",
-              "rel_err_per_side": {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
-                                   "floor": "1e-6 of the band's max"}}
+    energy = energy_report(m, sc.vertices, w["rho"], w["tau"], w["sky"], w["beam"], w["dgeo"],
+                           err_out, truth, dev)
 
     times = []
     launches = []
@@ -653,6 +673,8 @@ def run_c3(args, rank, world, local):
 
     step_s, res, clocks = timed(fc.PRECISION_MIXED, args.steps, args.warmup)
     err = error()
+    energy = energy_report(m, sc.vertices, rho, tau, sky, beam, dgeo[pick],
+                           out[torch.from_numpy(rows).to(dev)].cpu().numpy(), truth, dev)
     # the same solve in plain FP32 to the same per-side rule (it meets the bar too)
     fp32_s, res32, _ = timed(fc.PRECISION_FP32, 1, 0)
     err32 = error()
@@ -679,6 +701,7 @@ def run_c3(args, rank, world, local):
                                     "build_s": build_s, "sun_rasters_s": sun_s},
                    "l2": "inputs and outputs far larger than L2 (no flush needed)"},
         "max_rel_err_vs_fp64": err, "error_columns": "suns 0 and 255 x 64 bands",
+        "energy": energy,
         "iterations": res["iterations"], "residual_corrections": res["residual_corrections"],
         "batched_fp32": {"value": units / fp32_s, "ms_per_step": fp32_s * 1e3,
                          "iterations": res32["iterations"], "max_rel_err_vs_fp64": err32},
@@ -808,6 +831,9 @@ def run_c5(args, rank, world, local):
                                      tolerance=1e-12, maximum_iterations=4000)
     scale = np.maximum(np.abs(truth), 1e-6 * np.abs(truth).max(axis=1, keepdims=True))
     err = float(np.max(np.abs(got - truth) / scale))
+    energy = energy_report(batch, np.concatenate([sc.vertices for sc in parts]), cat(rho),
+                           cat(tau), sky, beam, cat(dgeo)[None, :], got, truth, dev,
+                           emission=cat(emis))
     line = {
         "metric": METRIC, "value": units / step_s, "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
@@ -824,7 +850,7 @@ def run_c5(args, rank, world, local):
                                     "build_s_all_scenes": build_s},
                    "generation_s": gen_s,
                    "l2": "inputs far larger than L2 (no flush needed)"},
-        "max_rel_err_vs_fp64": err, "iterations": res["iterations"],
+        "max_rel_err_vs_fp64": err, "energy": energy, "iterations": res["iterations"],
         "graph_launches": res["graph_launches"], "gpu_launches": int(res["kernel_launches"]),
         "autotuned_panel_width": tuned, "wall_ms_per_step": wall_s * 1e3,
         "scenes_one_by_one": {"value": units / seq_s, "ms_per_step": seq_s * 1e3,

@@ -606,6 +606,51 @@ void ensure_bvh(facetcu_context* ctx)
 }
 }  // namespace
 
+}  // extern "C"
+
+namespace {
+
+// The rays of each sample set in the order of their directions: a Morton
+// curve over the direction's tangent-plane components (dx, dy), 8 bits each.
+// A warp traces 32 consecutive rays at a time, so neighbouring directions
+// keep its BVH traversal coherent.  A side's row depends only on the set of
+// its rays (hits are sorted and counted), so the graph is unchanged.
+void order_samples(const float* uv, const float* dir, uint32_t sets, uint32_t rays,
+                   std::vector<float>& uv_out, std::vector<float>& dir_out)
+{
+    const size_t n = size_t(sets) * rays;
+    uv_out.resize(n * 2);
+    dir_out.resize(n * 3);
+    std::vector<uint32_t> key(rays), idx(rays);
+    auto q8 = [](float v) {
+        const float c = std::isfinite(v) ? std::min(1.0f, std::max(-1.0f, v)) : 0.0f;
+        return uint32_t((c + 1.0f) * 127.5f);
+    };
+    for (uint32_t set = 0; set < sets; ++set) {
+        const size_t b = size_t(set) * rays;
+        for (uint32_t j = 0; j < rays; ++j) {
+            const uint32_t x = q8(dir[3 * (b + j)]), y = q8(dir[3 * (b + j) + 1]);
+            uint32_t k = 0;
+            for (int bit = 0; bit < 8; ++bit)
+                k |= ((x >> bit) & 1u) << (2 * bit) | ((y >> bit) & 1u) << (2 * bit + 1);
+            key[j] = k;
+            idx[j] = j;
+        }
+        std::stable_sort(idx.begin(), idx.end(),
+                         [&](uint32_t a, uint32_t c) { return key[a] < key[c]; });
+        for (uint32_t j = 0; j < rays; ++j) {
+            const size_t from = b + idx[j], to = b + j;
+            uv_out[2 * to] = uv[2 * from];
+            uv_out[2 * to + 1] = uv[2 * from + 1];
+            for (int c = 0; c < 3; ++c) dir_out[3 * to + c] = dir[3 * from + c];
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
 int facetcu_build_hemisphere_graph(facetcu_context* ctx, const facetcu_hemisphere_config* config,
                                    const float* sample_uv, const float* sample_dir,
                                    facetcu_graph_diagnostics* diagnostics, uint64_t* dropped)
@@ -626,8 +671,12 @@ int facetcu_build_hemisphere_graph(facetcu_context* ctx, const facetcu_hemispher
         cudaStream_t s = ctx->stream;
         ctx->graph_ready = false;
         const size_t n = size_t(config->sample_sets) * config->rays_per_side;
-        upload(ctx->samples_uv, sample_uv, n * 8, s);
-        upload(ctx->samples_dir, sample_dir, n * 12, s);
+        std::vector<float> uv_sorted, dir_sorted;
+        order_samples(sample_uv, sample_dir, config->sample_sets, config->rays_per_side,
+                      uv_sorted, dir_sorted);
+        upload(ctx->samples_uv, uv_sorted.data(), n * 8, s);
+        upload(ctx->samples_dir, dir_sorted.data(), n * 12, s);
+        FCU_CHECK(cudaStreamSynchronize(s));  // the host tables go out of scope
         ensure_bvh(ctx);
         DeviceGraph& g = ctx->graph;
         unsigned long long drop = 0;

@@ -327,6 +327,66 @@ __device__ __forceinline__ void gather_split(const uint32_t* __restrict__ rows,
         for (int k = 0; k < CPL; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
 }
 
+// The same product for 8 or 16 FP32 columns: L = P / 4 lanes per row, so one
+// load instruction covers G = 32 / L = 16 or 8 edges, and a round of
+// 32 * G / 4 edges (128 or 64, G / 4 packed words per lane) gives every lane
+// eight 16-byte loads in flight (a 32-edge chunk would fill only two or four
+// of them).  Afterwards every lane holds the sums of its 4 columns
+// (col0 = (lane % L) * 4).
+template <int P>
+__device__ __forceinline__ void gather_rounds(const uint32_t* __restrict__ rows,
+                                              const uint32_t* __restrict__ packed,
+                                              const facetcu_csr_edge* __restrict__ edges,
+                                              uint32_t nb_bits, uint32_t s, const float* X,
+                                              int lane, float* acc)
+{
+    constexpr int L = P / 4;
+    constexpr int G = 32 / L;
+    constexpr int W = G / 4;   // packed words per lane per round
+    constexpr int E = 32 * W;  // edges per round
+    constexpr int U = E / G;   // loads per lane per round (8)
+    static_assert(P == 8 || P == 16, "rounds of 8 loads for 8 or 16 columns");
+    const int grp = lane / L, sub = lane % L;
+    const float4* __restrict__ X4 = reinterpret_cast<const float4*>(X);
+    const uint32_t start = __ldg(rows + s), end = __ldg(rows + s + 1);
+    for (uint32_t base = start; base < end; base += E) {
+        uint32_t nbv[W];
+        float cv[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            nbv[w] = 0u;
+            cv[w] = 0.0f;
+            const uint32_t e = base + uint32_t(w * 32 + lane);
+            if (e < end) edge_word(packed, edges, e, nb_bits, nbv[w], cv[w]);
+        }
+        float4 q[U];
+        float c[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int idx = u * G + grp;
+            const uint32_t nb = __shfl_sync(0xffffffffu, nbv[idx >> 5], idx & 31);
+            c[u] = __shfl_sync(0xffffffffu, cv[idx >> 5], idx & 31);
+            if (base + uint32_t(idx) < end) {
+                q[u] = __ldg(X4 + size_t(nb) * L + sub);
+            } else {
+                q[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                c[u] = 0.0f;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            acc[0] += c[u] * q[u].x;
+            acc[1] += c[u] * q[u].y;
+            acc[2] += c[u] * q[u].z;
+            acc[3] += c[u] * q[u].w;
+        }
+    }
+#pragma unroll
+    for (int o = L; o < 32; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+}
+
 // Dynamic hand-out of facet chunks (contiguous in Morton order); the counter
 // is reset by k_check after every sweep.
 constexpr uint32_t kChunk = 8;
@@ -443,7 +503,13 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_sweep_wide(GraphVie
                 float acc[CPL];
 #pragma unroll
                 for (int k = 0; k < CPL; ++k) acc[k] = 0.0f;
-                if (Bin) gather_split<P, false>(g.rows, g.packed, g.edges, g.nb_bits, s, Bin, lane, acc);
+                if (Bin) {
+                    if constexpr (P < 32)
+                        gather_rounds<P>(g.rows, g.packed, g.edges, g.nb_bits, s, Bin, lane, acc);
+                    else
+                        gather_split<P, false>(g.rows, g.packed, g.edges, g.nb_bits, s, Bin, lane,
+                                               acc);
+                }
                 const uint32_t d = __ldg(g.denom + s);
                 const float skyc = float(__ldg(g.skyc + s));
                 float dir[CPL];
@@ -1295,6 +1361,18 @@ void launch_sweep(int P, const GraphView& g, const PanelParams& pp, const T* in,
                   uint32_t* stats, uint32_t* counter, const uint32_t* done, cudaStream_t s)
 {
     if constexpr (sizeof(T) == 4) {
+        if (P == 8 || P == 16) {
+            // 16-byte row vectors in rounds of 8 loads per lane
+            if (P == 8) {
+                static const int grid = grid_for(k_sweep_wide<8>);
+                k_sweep_wide<8><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, counter, done);
+            } else {
+                static const int grid = grid_for(k_sweep_wide<16>);
+                k_sweep_wide<16><<<grid, kWarps * 32, 0, s>>>(g, pp, in, out, stats, counter, done);
+            }
+            FCU_LAUNCH("k_sweep_wide");
+            return;
+        }
         if (P >= 32) {
             switch (P) {
             case 32: {

@@ -43,6 +43,9 @@ namespace {
 
 constexpr int kWarps = 8;  // warps per CTA
 constexpr int kMaxP = 128;
+#ifndef FCU_NARROW_U
+#define FCU_NARROW_U 8  // loads in flight per lane for 1-4 column panels (12 ties, 16 is slower)
+#endif
 
 struct PanelParams {
     // per side and column, [S][P]
@@ -130,7 +133,7 @@ __device__ __forceinline__ Acc gather_narrow(const GraphView& g, uint32_t s, con
         // 8+ edge groups: each lane walks its group's edges itself, U loads
         // in flight (a broadcast of one 32-edge chunk would leave most of
         // the unrolled loads empty)
-        constexpr int U = 8;
+        constexpr int U = FCU_NARROW_U;
         for (uint32_t e = start + uint32_t(grp); e < end; e += uint32_t(G * U)) {
             Acc v[U];
             float c[U];

@@ -476,6 +476,7 @@ def run_gpu(args, rank, world, local):
             launches.append(res["kernel_launches"])
     torch.cuda.synchronize()
     barrier(world)
+    print("timed steps (ms): " + " ".join(f"{t * 1e3:.3f}" for t in times), file=sys.stderr)
     step_s = allreduce_max(float(np.mean(times)), world)
     units = sc.facet_count * B * 1
     value = units * world / step_s

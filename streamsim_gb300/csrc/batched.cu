@@ -392,7 +392,20 @@ __device__ __forceinline__ void gather_rounds(const uint32_t* __restrict__ rows,
 
 // Dynamic hand-out of facet chunks (contiguous in Morton order); the counter
 // is reset by k_check after every sweep.
-constexpr uint32_t kChunk = 8;
+// Facets per hand-out: 2 measured best on the config-2 forest (64-column
+// step 0.648 ms at 8 facets, 0.626 at 4, 0.623 at 2, 0.632 at 1; whole
+// solve 11.80 -> 11.35 ms), finer chunks evening out the warps' rows.
+// Scene batches hand out 8: a warp that moves into another scene publishes
+// its per-scene statistics (atomics per column), and small chunks scatter a
+// warp over many scenes (C5: 235 ms at 8 facets, 252 at 2, 236 at 32).
+#ifndef FCU_CHUNK
+#define FCU_CHUNK 2
+#endif
+#ifndef FCU_SCENE_CHUNK
+#define FCU_SCENE_CHUNK 8
+#endif
+constexpr uint32_t kChunk = FCU_CHUNK;
+constexpr uint32_t kSceneChunk = FCU_SCENE_CHUNK;
 __device__ __forceinline__ uint32_t next_chunk(uint32_t* counter, int lane)
 {
     uint32_t c = 0;
@@ -403,14 +416,14 @@ __device__ __forceinline__ uint32_t next_chunk(uint32_t* counter, int lane)
 // Every warp takes chunks of kChunk consecutive facets until none are left.
 // (Handing a CTA a larger run for its warps to share, for L1 reuse of
 // neighbour rows, measured slower at 64-256 facets per CTA.)
-template <typename F>
+template <uint32_t C = kChunk, typename F>
 __device__ __forceinline__ void for_each_facet(uint32_t facets, uint32_t* counter, int lane,
                                                F&& body)
 {
-    const uint32_t chunks = (facets + kChunk - 1) / kChunk;
+    const uint32_t chunks = (facets + C - 1) / C;
     for (uint32_t ch = next_chunk(counter, lane); ch < chunks; ch = next_chunk(counter, lane)) {
-        const uint32_t fe = min(facets, (ch + 1) * kChunk);
-        for (uint32_t f = ch * kChunk; f < fe; ++f) body(f);
+        const uint32_t fe = min(facets, (ch + 1) * C);
+        for (uint32_t f = ch * C; f < fe; ++f) body(f);
     }
 }
 
@@ -853,7 +866,7 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
             }
         }
     };
-    for_each_facet(g.facets, counter, lane, [&](uint32_t f) {
+    for_each_facet<Scenes ? kSceneChunk : kChunk>(g.facets, counter, lane, [&](uint32_t f) {
         if (Scenes) {
             const uint32_t sc = __ldg(g.scene + f);
             if (g.scene_done[sc]) return;

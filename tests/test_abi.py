@@ -91,3 +91,26 @@ def test_cpp_wrapper_compiles_and_maps_errors(tmp_path, lib):
                     "-lfacetcu", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def _build_module_check(tmp_path):
+    import os
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = tmp_path / "module_check"
+    libdir = os.path.join(root, "streamsim_gb300")
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(root, "include"),
+                    os.path.join(root, "tests", "cpp", "module_check.cpp"), "-L", libdir,
+                    "-lfacetcu", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    return str(exe)
+
+
+def test_module_seam_readiness_chain(tmp_path, lib):
+    """include/facetcu_module.hpp: the reference's Facetrt / FacetrtIO
+    (facetrt.h:14-29, facetrtio.h:7-21) and its readiness flags, no run."""
+    import subprocess
+    r = subprocess.run([_build_module_check(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0 and "module seam ok" in r.stdout, r.stdout + r.stderr

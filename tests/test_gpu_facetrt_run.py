@@ -94,3 +94,17 @@ def test_cli_executable_end_to_end(tmp_path):
     default_out = tmp_path / "facetrt.json"
     assert r.stdout.splitlines()[-1] == f"RESULT\t{default_out}"
     _check_result(json.loads(default_out.read_text()))
+
+
+def test_module_seam_runs_the_scene(tmp_path):
+    """include/facetcu_module.hpp: setup, upload, create and run of the
+    reference's Facetrt on the validation scene write the same facetrt.json
+    layout (command.cpp:16-24: runFacetRTCore(...) == 0)."""
+    require_gpu()
+    from tests.test_abi import _build_module_check
+    exe = _build_module_check(tmp_path)
+    out = tmp_path / "module.json"
+    r = subprocess.run([exe, OBJ, str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert f"RESULT\t{out}" in r.stdout and "module seam ok" in r.stdout
+    _check_result(json.load(open(out)))

@@ -5,9 +5,10 @@
 // (models/histream/src/main.cpp:56-80, base/engine.cpp:162-165): an unknown
 // mode prints the usage and exits 2; eFacetRT runs runFacetRTCore
 // (facetrtcore.cpp:3116-3161) through facetcu_run_facetrt_core and exits 0 on
-// success, 1 on failure.  The other reference modes (voxel and ray-tracing
-// engines, FacetEB) are not built on this backend and exit 3, the code the
-// reference uses when engine resources cannot be created.
+// success, 1 on failure.  The other reference modes exit 3, the code the
+// reference uses when engine resources cannot be created: the voxel and
+// ray-tracing engines are not built on this backend, and eFacetEB runs from
+// Python (python -m streamsim_gb300.faceteb, the same library).
 #include <iostream>
 #include <string>
 
@@ -26,7 +27,9 @@ int main(int argc, char** argv)
     }
     if (mode != "eFacetRT") {
         std::cerr << "Failed to create engine resources for " << mode
-                  << ": only eFacetRT runs on the CUDA backend\n";
+                  << ": only eFacetRT runs in this executable";
+        if (mode == "eFacetEB") std::cerr << " (eFacetEB: python -m streamsim_gb300.faceteb)";
+        std::cerr << '\n';
         return 3;
     }
     return facetcu_run_facetrt_core(input.c_str(), "", output.c_str()) == 0 ? 0 : 1;

@@ -29,6 +29,8 @@ formulas, about 0.01 deg from SPA).
 import json
 import math
 import os
+import re
+import sys
 
 import numpy as np
 
@@ -229,3 +231,198 @@ class Run:
         }
         with open(path, "w") as f:
             json.dump(doc, f)
+
+
+# ---- the process entry: runFacetEBCore on an XML project or an OBJ ---------
+_ENTITIES = {"&lt;": "<", "&gt;": ">", "&quot;": '"', "&apos;": "'", "&amp;": "&"}
+_FLOAT = re.compile(r"[+-]?(?:\d+\.?\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|inf(?:inity)?|nan)",
+                    re.IGNORECASE)
+
+
+def first_xml_tag(xml, tag):
+    """firstXmlTag (facetrtcore.cpp:2068-2085): the text of the first
+    <tag ...>...</tag>, entities decoded; '' when absent."""
+    begin = xml.find("<" + tag)
+    if begin < 0:
+        return ""
+    content = xml.find(">", begin + len(tag) + 1)
+    if content < 0:
+        return ""
+    end = xml.find("</" + tag + ">", content + 1)
+    if end < 0:
+        return ""
+    return re.sub("&(lt|gt|quot|apos|amp);", lambda m: _ENTITIES[m.group(0)], xml[content + 1:end])
+
+
+def xml_float(xml, tag, fallback):
+    """xmlFloat (:2098-2110): std::stof of the trimmed text (its longest
+    number prefix), the fallback when empty, unparsable or not finite."""
+    text = first_xml_tag(xml, tag).strip()
+    m = _FLOAT.match(text)
+    if not m:
+        return float(fallback)
+    v = float(np.float32(float(m.group(0))))
+    return v if math.isfinite(v) else float(fallback)
+
+
+def _scalar_spectrum(path):
+    """readScalarSpectrum (:2499-2509): numbers until the first that does not
+    parse, negatives and non-finite values as 0, at most 2001."""
+    values = []
+    try:
+        text = open(path).read()
+    except OSError:
+        return np.zeros(0, np.float32)
+    for token in text.split():
+        m = _FLOAT.fullmatch(token)
+        if not m:
+            break
+        v = float(np.float32(float(token)))
+        values.append(max(0.0, v) if math.isfinite(v) else 0.0)
+        if len(values) == 2001:
+            break
+    return np.asarray(values, np.float32)
+
+
+def _resolve(input_path, value):
+    p = value.strip()
+    return p if os.path.isabs(p) else os.path.normpath(os.path.join(os.path.dirname(input_path), p))
+
+
+def _surface(d):
+    keys = ("surface_resistance", "specific_heat", "density", "thermal_conductivity",
+            "soil_moisture", "heat_capacity_per_area", "soil_temperature_method", "pv_eta25",
+            "pv_gamma", "pv_bifaciality", "convective_scale")
+    m = facetcu.EnergySurface(d["reflectance"], d["transmittance"], d["tir_reflectance"],
+                              d["tir_transmittance"], d["sunlit_temperature"],
+                              d["shaded_temperature"], d["energy_reflectance"],
+                              d["energy_transmittance"], photovoltaic=bool(d["photovoltaic"]),
+                              vegetation=bool(d["vegetation"]), **{k: d[k] for k in keys})
+    m.output_component = int(d["output_component"])
+    return m
+
+
+def run_faceteb_core(input_path, output_file="", progress=print):
+    """runFacetEBCore (facetrtcore.cpp:3164-4154) on an XML project (or a
+    project.json through its XML view) or an OBJ scene: the scene and
+    materials (loadProjectScene / loadTreeWithSoil), the settings of
+    :3194-3240 (startTimeNode, endTimeNode, dTime, couplingIterations,
+    temperatureTolerance, temperatureRelaxation, spectralAccelerationWidth,
+    vegetationTemperatureMethod, Latitude, Longitude, skyTemperature,
+    directScatteringRatio), the shortwave spectrum (loadShortwaveSpectrum,
+    :2499-2541), the meteorology rows (:3243-3273), one shared visibility
+    graph of the 40 hemisphere directions (:3329-3371), then the node
+    sequence of Run with each node's sun from its date.  Writes
+    .facet_steps/components.bin, .facet_steps/energy_T=<time>.bin per node
+    and faceteb.json; prints PROGRESS lines and RESULT\t<path>.  Not
+    written: faceteb_run.json, photovoltaic_summary.csv, the process/
+    folder and images.  Returns the result file."""
+    ext = os.path.splitext(input_path)[1].lower()
+    is_obj = ext == ".obj"
+    if ext == ".json":
+        xml = facetcu.project_xml_view(input_path)
+    else:
+        with open(input_path, encoding="utf-8", errors="replace") as f:
+            xml = f.read()
+    if output_file:
+        result_file = output_file
+    else:
+        out_dir = first_xml_tag(xml, "outDir") or os.path.dirname(input_path)
+        result_file = os.path.normpath(os.path.join(out_dir, "faceteb.json"))
+    out_dir = os.path.dirname(result_file) or "."
+    os.makedirs(out_dir, exist_ok=True)
+
+    start = max(0, int(round(xml_float(xml, "startTimeNode", 0.0))))
+    end = max(start + 1, int(round(xml_float(xml, "endTimeNode", float(start + 1)))))
+    dtime = max(1.0, xml_float(xml, "dTime", 1800.0))
+    settings = dict(
+        coupling_iterations=int(np.clip(round(xml_float(xml, "couplingIterations", 20.0)), 1, 100)),
+        temperature_tolerance=float(np.clip(xml_float(xml, "temperatureTolerance", 0.05),
+                                            0.001, 10.0)),
+        temperature_relaxation=float(np.clip(xml_float(xml, "temperatureRelaxation", 0.5),
+                                             0.05, 1.0)),
+        vegetation_temperature_method=int(np.clip(
+            round(xml_float(xml, "vegetationTemperatureMethod", 0.0)), 0, 1)),
+        sky_temperature=float(np.clip(xml_float(xml, "skyTemperature", 250.0), 150.0, 350.0)),
+        time_step=dtime)
+    width = int(np.clip(round(xml_float(xml, "spectralAccelerationWidth", 100.0)), 1, 1000))
+    latitude = xml_float(xml, "Latitude", 40.0)
+    longitude = xml_float(xml, "Longitude", 116.0)
+    direct_fraction = float(np.clip(xml_float(xml, "directScatteringRatio", 0.8), 0.0, 1.0))
+    esun, esky = first_xml_tag(xml, "esunFileName").strip(), first_xml_tag(xml, "eskyFileName").strip()
+    spectrum = None
+    if esun and esky:
+        spectrum = (_scalar_spectrum(_resolve(input_path, esun)),
+                    _scalar_spectrum(_resolve(input_path, esky)))
+
+    meteo_name = first_xml_tag(xml, "filePath").strip()
+    if meteo_name:
+        path = _resolve(input_path, meteo_name)
+        if not os.path.exists(path):
+            raise RuntimeError("FacetEB cannot open meteorology: " + meteo_name)
+        meteorology = read_meteorology(path)
+    else:
+        meteorology = []
+    if not meteorology:
+        meteorology = default_meteorology(end, dtime)
+    if end > len(meteorology):
+        raise RuntimeError("FacetEB time range exceeds meteorology rows")
+
+    if is_obj:
+        vertices, mi, leaf, _, _ = facetcu.load_tree_with_soil(input_path)
+        raster, layers, periodic = 1024, 64, (0, 1.0, 1.0)
+        materials, mi, tex, strength, wavelengths = [], None, None, 0.0, [550.0]
+    else:
+        project = facetcu.Project(input_path)
+        info = project.info
+        vertices, leaf = project.vertices, info["leaf_facet_count"]
+        raster, layers = info["raster_size"], info["raster_layers"]
+        periodic = (info["periodic_neighbor_count"], info["periodic_size_x"],
+                    info["periodic_size_z"])
+        materials = [_surface(project.material(i)) for i in range(info["material_count"])]
+        mi, tex = project.material_indices, project.texture_factors
+        strength = info["background_angular_strength"]
+        sp = project.spectral_parameters()
+        wl = facetcu.C.cast(sp.wavelengths, facetcu.C.POINTER(facetcu.C.c_float))
+        wavelengths = [float(wl[i]) for i in range(sp.band_count)]
+        project.close()
+    if progress:
+        progress("PROGRESS\t3\tFacetEB scene and meteorology loaded")
+    model = facetcu.FacetrtCuda()
+    model.initialize(raster, raster, layers, 0, *periodic)
+    model.setGeometry(vertices)
+    if progress:
+        progress("PROGRESS\t10\tshared facet visibility graph")
+    diag = model.buildVisibilityGraph(facetcu.hemisphere_directions())
+    run = Run(model, leaf, materials, mi, tex, wavelengths=wavelengths, spectrum=spectrum,
+              direct_fraction=direct_fraction, window_width=width,
+              background_angular_strength=strength, **settings)
+    run.run(meteorology, None, start, end, output_dir=out_dir, vertices=vertices, graph=diag,
+            progress=progress, latitude=latitude, longitude=longitude)
+    written = os.path.join(out_dir, "faceteb.json")
+    if os.path.abspath(written) != os.path.abspath(result_file):
+        os.replace(written, result_file)
+    model.close()
+    if progress:
+        progress("RESULT\t" + result_file)
+    return result_file
+
+
+def main(argv=None):
+    """`python -m streamsim_gb300.faceteb <Input.xml|project.json|scene.obj>
+    [faceteb.json]`: the eFacetEB process mode (runFacetEBCore); exit 0, or
+    1 with `faceteb: <message>` on stderr."""
+    argv = sys.argv[1:] if argv is None else argv
+    if not argv:
+        print("Usage: python -m streamsim_gb300.faceteb <project> [faceteb.json]", file=sys.stderr)
+        return 2
+    try:
+        run_faceteb_core(argv[0], argv[1] if len(argv) > 1 else "")
+        return 0
+    except Exception as e:  # the reference prints and returns 1
+        print(f"faceteb: {e}", file=sys.stderr)
+        return 1
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -274,3 +274,46 @@ def test_node_sequence_places_the_sun_by_date(site, tmp_path):
                           f"energy_T={faceteb.time_token(r['julian_time'])}.bin",
                           "<f4").reshape(sc.surface_count, 9)
         assert np.array_equal(rec[:, 8], lit) and lit.max() > 0.0
+
+
+def test_faceteb_process_entry_on_an_xml_project(tmp_path):
+    """runFacetEBCore's process entry (faceteb.run_faceteb_core) on an XML
+    project: its settings, meteorology file and site, one shared graph,
+    two nodes; the records, components and faceteb.json are written, and
+    every node's sunlit column is the raster of that node's dated sun."""
+    import json
+    from streamsim_gb300 import faceteb
+    from tests.test_project_host import _write_project
+    require_gpu()
+    (tmp_path / "met.txt").write_text("julian Ta ea Pa u Rs Rl\n"
+                                      "172.375 22 14 1005 2.0 520 340\n"
+                                      "172.5 26 15 1003 2.5 800 350\n")
+    path = _write_project(tmp_path, coefficients=False, bands="550,865,11000",
+                          extra_control="<endTimeNode>2</endTimeNode><dTime>10800</dTime>"
+                                        "<filePath>met.txt</filePath><Latitude>35</Latitude>"
+                                        "<Longitude>110</Longitude>"
+                                        "<couplingIterations>6</couplingIterations>")
+    out = faceteb.run_faceteb_core(path, str(tmp_path / "out" / "faceteb.json"), progress=None)
+    doc = json.load(open(out))
+    p = facetcu.Project(path)
+    info = p.info
+    F = info["facet_count"]
+    assert doc["facetCount"] == F and doc["leafFacetCount"] == info["leaf_facet_count"]
+    assert doc["time"] == faceteb.time_token(172.5) and len(doc["temperature"]) == 2 * F
+    steps = tmp_path / "out" / ".facet_steps"
+    comp = np.fromfile(steps / "components.bin", np.uint8)
+    assert comp.size == F and np.all(comp[info["leaf_facet_count"]:] == 1)
+    pv = [i for i in range(info["material_count"]) if p.material(i)["photovoltaic"]]
+    assert pv and np.any(comp == 4)  # the project's PV panel
+    m = facetcu.FacetrtCuda()
+    m.initialize(info["raster_size"], info["raster_size"], info["raster_layers"], 0,
+                 info["periodic_neighbor_count"], info["periodic_size_x"],
+                 info["periodic_size_z"])
+    m.setGeometry(p.vertices)
+    for jt, ta, pa in ((172.375, 22.0, 1005.0), (172.5, 26.0, 1003.0)):
+        rec = np.fromfile(steps / f"energy_T={faceteb.time_token(jt)}.bin",
+                          "<f4").reshape(2 * F, 9 + 3)
+        zen, az = facetcu.faceteb_sun(jt, 35.0, 110.0, pa, ta)
+        assert np.array_equal(rec[:, 8], m.computeSunlitFraction(facetcu.sun_direction(zen, az)))
+        assert np.all(np.isfinite(rec)) and 250.0 < rec[:, 0].min() and rec[:, 0].max() < 360.0
+    m.close()

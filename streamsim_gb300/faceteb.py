@@ -17,6 +17,8 @@ formats:
                                            latent, storage, sunlit, then bands;
                                            float32 little-endian)
   faceteb.json                             :4085-4139
+  photovoltaic_node_<node>.csv,
+  photovoltaic_summary.csv                 :3433-3435, 3847-3860
 
   solar_sun                                :3290-3327 (updateSolarPosition)
 
@@ -86,6 +88,29 @@ def solar_sun(latitude=40.0, longitude=116.0):
         return facetcu.faceteb_sun(row["julian_time"], latitude, longitude, row["pressure"],
                                    row["air_temperature"])
     return sun_for
+
+
+def facet_areas(vertices):
+    """facetArea (facetrtcore.cpp:704-716) of every facet, in float32 with
+    the reference's operation order: 0.5 sqrt(c . c), c = (b - a) x (c - a)."""
+    v = np.asarray(vertices, np.float32).reshape(-1, 3, 6)[:, :, :3]
+    ea, eb = v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]
+    c0 = ea[:, 1] * eb[:, 2] - ea[:, 2] * eb[:, 1]
+    c1 = ea[:, 2] * eb[:, 0] - ea[:, 0] * eb[:, 2]
+    c2 = ea[:, 0] * eb[:, 1] - ea[:, 1] * eb[:, 0]
+    return np.float32(0.5) * np.sqrt((c0 * c0 + c1 * c1) + c2 * c2)
+
+
+def _g(x):
+    """A number as std::ostream writes it by default (6 significant digits)."""
+    return format(float(x), ".6g")
+
+
+PV_SUMMARY_HEADER = ("node,time,area_m2,temperature_C,incident_W,absorbed_W,electric_W,"
+                     "net_longwave_W,sensible_W,storage_W,max_residual_W_m2,energy_kWh\n")
+PV_NODE_HEADER = ("area_m2,temperature_C,incident_W_m2,absorbed_W_m2,electric_W_m2,residual_W_m2,"
+                  "latent_W_m2,effective_W_m2,net_longwave_W_m2,sensible_W_m2,storage_W_m2,"
+                  "facet_index\n")
 
 
 def _meteo(row):
@@ -165,6 +190,13 @@ class Run:
         results = []
         last = None
         all_converged = True
+        pv = self._pv_facets() if output_dir else []
+        area = facet_areas(vertices) if output_dir and vertices is not None else None
+        summary = None
+        if output_dir:
+            summary = open(os.path.join(output_dir, "photovoltaic_summary.csv"), "w")
+            summary.write(PV_SUMMARY_HEADER)
+        energy_kwh = 0.0
         for node in range(start_node, end_node):
             row = meteorology[node]
             if temperature is None:
@@ -186,15 +218,71 @@ class Run:
                     cols += list(fields["band_output"])
                 rec = np.stack([np.asarray(c, np.float32) for c in cols], 1)
                 rec.astype("<f4").tofile(os.path.join(steps, f"energy_T={token}.bin"))
+            if output_dir and area is not None:
+                energy_kwh = self._write_pv(output_dir, node, token, fields, area, pv, summary,
+                                            energy_kwh)
             if progress:
                 progress(f"FACET_CONVERGENCE\t{node}\t{int(res['converged'])}\t"
                          f"{res['coupling_iterations']}\t{res['max_temperature_delta']}\t"
                          f"{res['max_energy_residual']}\t{res['max_energy_residual_equivalent']}")
             last = (fields, res, lit, token)
+        if summary is not None:
+            summary.close()
         if output_dir and last is not None:
             self._write_result(os.path.join(output_dir, "faceteb.json"), last, all_converged,
                                vertices, graph)
         return results, (last[0] if last else None)
+
+    def _pv_facets(self):
+        """Object facets whose material is photovoltaic (surfaceForFacet)."""
+        out = []
+        if self.mi is None:
+            return out
+        for f in range(self.leaf):
+            m = int(self.mi[f])
+            if m < len(self.materials) and self.materials[m].photovoltaic:
+                out.append((f, float(np.float32(self.materials[m].pv_bifaciality))))
+        return out
+
+    def _write_pv(self, output_dir, node, token, fields, area, pv, summary, energy_kwh):
+        """photovoltaic_node_<node>.csv and the photovoltaic_summary.csv row
+        (facetrtcore.cpp:3847-3860): per PV facet its area, front-side
+        temperature and fluxes, float arithmetic, double area-weighted sums,
+        6 significant digits."""
+        f32 = np.float32
+        T, ab_, inc_ = fields["temperature"], fields["absorbed_shortwave"], fields["incident_shortwave"]
+        pvp, net = fields["photovoltaic_power"], fields["net_radiation"]
+        sens, lat, stor = fields["sensible_heat"], fields["latent_heat"], fields["storage_heat"]
+        pa = pt = pg = pab = pp = plw = ph = ps = pres = 0.0
+        lines = [PV_NODE_HEADER]
+        for f, bif in pv:
+            k = 2 * f
+            a = f32(area[f])
+            ab = f32(ab_[k] + ab_[k + 1])
+            inc = f32(inc_[k] + inc_[k + 1])
+            power = f32(pvp[k])
+            lw = f32(net[k] - ab)
+            res = f32(f32(f32(f32(net[k] - sens[k]) - lat[k]) - stor[k]) - power)
+            tc = f32(T[k] - f32(273.15))
+            eff = f32(inc_[k] + f32(f32(bif) * inc_[k + 1]))
+            lines.append(",".join(_g(x) for x in (a, tc, inc, ab, power, res, lat[k], eff, lw,
+                                                  sens[k], stor[k])) + f",{f}\n")
+            pa += float(a)
+            pt += float(f32(a * tc))
+            pg += float(f32(a * inc))
+            pab += float(f32(a * ab))
+            pp += float(f32(a * power))
+            plw += float(f32(a * lw))
+            ph += float(f32(a * f32(sens[k])))
+            ps += float(f32(a * f32(stor[k])))
+            pres = max(pres, abs(float(res)))
+        with open(os.path.join(output_dir, f"photovoltaic_node_{node}.csv"), "w") as f:
+            f.write("".join(lines))
+        if pa > 0:
+            energy_kwh += pp * float(self.settings.get("time_step", 1800.0)) / 3600000.0
+            summary.write(",".join([str(node), token] + [_g(x) for x in (
+                pa, pt / pa, pg, pab, pp, plw, ph, ps, pres, energy_kwh)]) + "\n")
+        return energy_kwh
 
     def _write_result(self, path, last, all_converged, vertices, graph):
         fields, res, lit, token = last
@@ -314,9 +402,9 @@ def run_faceteb_core(input_path, output_file="", progress=print):
     graph of the 40 hemisphere directions (:3329-3371), then the node
     sequence of Run with each node's sun from its date.  Writes
     .facet_steps/components.bin, .facet_steps/energy_T=<time>.bin per node
-    and faceteb.json; prints PROGRESS lines and RESULT\t<path>.  Not
-    written: faceteb_run.json, photovoltaic_summary.csv, the process/
-    folder and images.  Returns the result file."""
+    and faceteb.json, the photovoltaic node and summary tables; prints
+    PROGRESS lines and RESULT\t<path>.  Not written: faceteb_run.json, the
+    process/ folder and images.  Returns the result file."""
     ext = os.path.splitext(input_path)[1].lower()
     is_obj = ext == ".obj"
     if ext == ".json":

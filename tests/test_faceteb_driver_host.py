@@ -44,3 +44,47 @@ def test_missing_meteorology_and_short_tables(tmp_path):
     with pytest.raises(RuntimeError, match="^FacetEB time range exceeds meteorology rows$"):
         faceteb.run_faceteb_core(str(xml), "", progress=None)
     assert faceteb.main([]) == 2
+
+
+def test_photovoltaic_tables(tmp_path):
+    """photovoltaic_node_<node>.csv and photovoltaic_summary.csv
+    (facetrtcore.cpp:3847-3860) from one node's fields: PV facets only,
+    front-side values, area-weighted sums, the energy running over nodes."""
+    from streamsim_gb300 import facetcu
+    F, leaf = 4, 3
+    v = np.zeros((3 * F, 6), np.float32)
+    for f in range(F):  # right triangles of legs 1 and f + 1: area (f + 1) / 2
+        v[3 * f + 1, 0] = 1.0
+        v[3 * f + 2, 2] = f + 1.0
+    assert np.array_equal(faceteb.facet_areas(v), np.float32([0.5, 1.0, 1.5, 2.0]))
+    mats = [facetcu.EnergySurface(), facetcu.EnergySurface(photovoltaic=True, pv_bifaciality=0.25)]
+
+    class Model:
+        facet_count = F
+
+        def computeSunlitFraction(self, sun):  # not called here
+            raise AssertionError
+
+    run = faceteb.Run(Model(), leaf, mats, np.array([1, 0, 1, 0], np.uint32), time_step=3600.0)
+    S = 2 * F
+    fields = {k: np.arange(S, dtype=np.float32) + 1 for k in
+              ("absorbed_shortwave", "incident_shortwave", "photovoltaic_power", "net_radiation",
+               "sensible_heat", "latent_heat", "storage_heat")}
+    fields["temperature"] = np.full(S, 300.0, np.float32)
+    with open(tmp_path / "photovoltaic_summary.csv", "w") as summary:
+        summary.write(faceteb.PV_SUMMARY_HEADER)
+        e = run._write_pv(str(tmp_path), 0, "DOY1_00-00", fields, faceteb.facet_areas(v),
+                          run._pv_facets(), summary, 0.0)
+        e = run._write_pv(str(tmp_path), 1, "DOY1_01-00", fields, faceteb.facet_areas(v),
+                          run._pv_facets(), summary, e)
+    rows = (tmp_path / "photovoltaic_node_0.csv").read_text().splitlines()
+    assert rows[0] == faceteb.PV_NODE_HEADER.strip() and len(rows) == 3  # facets 0 and 2
+    first = rows[1].split(",")
+    # facet 0: area 0.5, 26.85 C, incident 1 + 2, absorbed 3, power 1, net - absorbed
+    assert first[:5] == ["0.5", "26.85", "3", "3", "1"] and first[-1] == "0"
+    assert first[5] == "-3" and first[7] == "1.5"  # residual 1-1-1-1-1; 1 + 0.25 * 2
+    assert first[8] == "-2"  # net longwave: net - absorbed
+    summ = (tmp_path / "photovoltaic_summary.csv").read_text().splitlines()
+    assert len(summ) == 3 and summ[1].split(",")[:3] == ["0", "DOY1_00-00", "2"]
+    # electric power: 0.5 * 1 + 1.5 * 5 = 8 W per node; 3600 s each
+    assert summ[1].split(",")[6] == "8" and summ[2].split(",")[-1] == faceteb._g(2 * 8 / 1000.0)

@@ -317,3 +317,14 @@ def test_faceteb_process_entry_on_an_xml_project(tmp_path):
         assert np.array_equal(rec[:, 8], m.computeSunlitFraction(facetcu.sun_direction(zen, az)))
         assert np.all(np.isfinite(rec)) and 250.0 < rec[:, 0].min() and rec[:, 0].max() < 360.0
     m.close()
+    # the project's PV panel: a node table per node and one summary row per node
+    summary = (tmp_path / "out" / "photovoltaic_summary.csv").read_text().splitlines()
+    assert summary[0].startswith("node,time,area_m2") and len(summary) == 3
+    assert [r.split(",")[1] for r in summary[1:]] == [faceteb.time_token(172.375),
+                                                      faceteb.time_token(172.5)]
+    node = (tmp_path / "out" / "photovoltaic_node_1.csv").read_text().splitlines()
+    pv_facets = int(np.sum(comp == 4))
+    assert len(node) == pv_facets + 1
+    area = sum(float(r.split(",")[0]) for r in node[1:])
+    assert abs(area - float(summary[2].split(",")[2])) <= 1e-4 * area
+    assert float(summary[2].split(",")[-1]) > float(summary[1].split(",")[-1]) > 0.0

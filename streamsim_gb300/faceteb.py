@@ -19,6 +19,7 @@ formats:
   faceteb.json                             :4085-4139
   photovoltaic_node_<node>.csv,
   photovoltaic_summary.csv                 :3433-3435, 3847-3860
+  faceteb_run.json                         :58-73, 3213-3222, 4030-4041, 4144-4147
 
   solar_sun                                :3290-3327 (updateSolarPosition)
 
@@ -113,6 +114,64 @@ PV_NODE_HEADER = ("area_m2,temperature_C,incident_W_m2,absorbed_W_m2,electric_W_
                   "facet_index\n")
 
 
+def utc_timestamp():
+    """utcTimestamp (facetrtcore.cpp:42-53): %Y-%m-%dT%H:%M:%SZ."""
+    import time
+    return time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())
+
+
+class RunIndex:
+    """faceteb_run.json (FacetRunIndex, facetrtcore.cpp:58-73, 3213-3222,
+    3436-3437, 4030-4041, 4144-4147): rewritten after every node, keys in
+    sorted order with two-space indents as nlohmann::json writes them; a run
+    that stops before its end is marked failed."""
+
+    def __init__(self, path, input_path, start, end, tolerance, budget):
+        self.path = path
+        self.value = {
+            "kind": "faceteb-run", "schemaVersion": 1, "status": "running",
+            "startedAt": utc_timestamp(), "input": input_path,
+            "requested": {"startNode": start, "endNodeExclusive": end},
+            "convergence": {"temperatureTolerance_K": float(np.float32(tolerance)),
+                            "iterationBudget": budget,
+                            "criterion": "temperatureDelta and residual/thermal-response "
+                                         "<= temperatureTolerance"},
+            "completed": [], "products": []}
+        self.write()
+
+    def write(self):
+        with open(self.path, "w") as f:
+            f.write(json.dumps(self.value, indent=2, sort_keys=True, ensure_ascii=False) + "\n")
+
+    def node(self, node, token, julian_time, res, tolerance, budget):
+        self.value["products"] += [f".facet_steps/energy_T={token}.bin",
+                                   f"photovoltaic_node_{node}.csv"]
+        f32 = lambda x: float(np.float32(x))
+        self.value["completed"].append({
+            "node": node, "token": token, "julianTime": f32(julian_time),
+            "converged": bool(res["converged"]), "iterations": int(res["coupling_iterations"]),
+            "iterationBudget": budget, "temperatureDelta": f32(res["max_temperature_delta"]),
+            "temperatureTolerance": f32(tolerance),
+            "energyResidual": f32(res["max_energy_residual"]), "energyResidualUnits": "W m-2",
+            "energyResidualTemperatureEquivalent": f32(res["max_energy_residual_equivalent"])})
+        self.write()
+
+    def finish(self, result_name, converged):
+        self.value["products"].append(result_name)
+        self.value["status"] = "completed" if converged else "non_converged"
+        self.value["finishedAt"] = utc_timestamp()
+        self.write()
+
+    def fail(self):
+        if self.value.get("status") == "running":
+            self.value["status"] = "failed"
+            self.value["finishedAt"] = utc_timestamp()
+            try:
+                self.write()
+            except OSError:
+                pass
+
+
 def _meteo(row):
     return {k: float(row[k]) for k in ("air_temperature", "vapor_pressure", "pressure",
                                         "wind_speed", "shortwave", "longwave")}
@@ -170,7 +229,8 @@ class Run:
         return fields, res, lit
 
     def run(self, meteorology, sun_for=None, start_node=0, end_node=None, output_dir=None,
-            vertices=None, graph=None, progress=print, latitude=40.0, longitude=116.0):
+            vertices=None, graph=None, progress=print, latitude=40.0, longitude=116.0,
+            run_index=None):
         """Nodes [start_node, end_node) of the meteorology rows.  Writes the
         reference's step records and faceteb.json under output_dir when
         given.  sun_for defaults to solar_sun(latitude, longitude).  Returns
@@ -196,6 +256,9 @@ class Run:
         if output_dir:
             summary = open(os.path.join(output_dir, "photovoltaic_summary.csv"), "w")
             summary.write(PV_SUMMARY_HEADER)
+            if run_index is not None:
+                run_index.value["products"] += ["photovoltaic_summary.csv",
+                                                ".facet_steps/components.bin"]
         energy_kwh = 0.0
         for node in range(start_node, end_node):
             row = meteorology[node]
@@ -221,6 +284,9 @@ class Run:
             if output_dir and area is not None:
                 energy_kwh = self._write_pv(output_dir, node, token, fields, area, pv, summary,
                                             energy_kwh)
+            if run_index is not None:
+                run_index.node(node, token, row["julian_time"], res,
+                               self.params.temperature_tolerance, self.params.coupling_iterations)
             if progress:
                 progress(f"FACET_CONVERGENCE\t{node}\t{int(res['converged'])}\t"
                          f"{res['coupling_iterations']}\t{res['max_temperature_delta']}\t"
@@ -402,9 +468,9 @@ def run_faceteb_core(input_path, output_file="", progress=print):
     graph of the 40 hemisphere directions (:3329-3371), then the node
     sequence of Run with each node's sun from its date.  Writes
     .facet_steps/components.bin, .facet_steps/energy_T=<time>.bin per node
-    and faceteb.json, the photovoltaic node and summary tables; prints
-    PROGRESS lines and RESULT\t<path>.  Not written: faceteb_run.json, the
-    process/ folder and images.  Returns the result file."""
+    and faceteb.json, the photovoltaic node and summary tables and the run
+    index faceteb_run.json; prints PROGRESS lines and RESULT\t<path>.  Not
+    written: the process/ folder and images.  Returns the result file."""
     ext = os.path.splitext(input_path)[1].lower()
     is_obj = ext == ".obj"
     if ext == ".json":
@@ -433,6 +499,19 @@ def run_faceteb_core(input_path, output_file="", progress=print):
             round(xml_float(xml, "vegetationTemperatureMethod", 0.0)), 0, 1)),
         sky_temperature=float(np.clip(xml_float(xml, "skyTemperature", 250.0), 150.0, 350.0)),
         time_step=dtime)
+    index = RunIndex(os.path.join(out_dir, "faceteb_run.json"), input_path, start, end,
+                     settings["temperature_tolerance"], settings["coupling_iterations"])
+    try:
+        return _run_faceteb(xml, input_path, result_file, out_dir, start, end, dtime, settings,
+                            index, progress)
+    finally:
+        index.fail()
+
+
+def _run_faceteb(xml, input_path, result_file, out_dir, start, end, dtime, settings, index,
+                 progress):
+    """run_faceteb_core after its settings (the run index is open)."""
+    is_obj = os.path.splitext(input_path)[1].lower() == ".obj"
     width = int(np.clip(round(xml_float(xml, "spectralAccelerationWidth", 100.0)), 1, 1000))
     latitude = xml_float(xml, "Latitude", 40.0)
     longitude = xml_float(xml, "Longitude", 116.0)
@@ -482,15 +561,19 @@ def run_faceteb_core(input_path, output_file="", progress=print):
     if progress:
         progress("PROGRESS\t10\tshared facet visibility graph")
     diag = model.buildVisibilityGraph(facetcu.hemisphere_directions())
-    run = Run(model, leaf, materials, mi, tex, wavelengths=wavelengths, spectrum=spectrum,
-              direct_fraction=direct_fraction, window_width=width,
-              background_angular_strength=strength, **settings)
-    run.run(meteorology, None, start, end, output_dir=out_dir, vertices=vertices, graph=diag,
-            progress=progress, latitude=latitude, longitude=longitude)
-    written = os.path.join(out_dir, "faceteb.json")
-    if os.path.abspath(written) != os.path.abspath(result_file):
-        os.replace(written, result_file)
-    model.close()
+    try:
+        run = Run(model, leaf, materials, mi, tex, wavelengths=wavelengths, spectrum=spectrum,
+                  direct_fraction=direct_fraction, window_width=width,
+                  background_angular_strength=strength, **settings)
+        results, _ = run.run(meteorology, None, start, end, output_dir=out_dir,
+                             vertices=vertices, graph=diag, progress=progress,
+                             latitude=latitude, longitude=longitude, run_index=index)
+        written = os.path.join(out_dir, "faceteb.json")
+        if os.path.abspath(written) != os.path.abspath(result_file):
+            os.replace(written, result_file)
+        index.finish(os.path.basename(result_file), all(r["converged"] for r in results))
+    finally:
+        model.close()
     if progress:
         progress("RESULT\t" + result_file)
     return result_file

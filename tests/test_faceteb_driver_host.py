@@ -38,6 +38,11 @@ def test_missing_meteorology_and_short_tables(tmp_path):
                    "</Meteorology></HiStreamProject>")
     with pytest.raises(RuntimeError, match="^FacetEB cannot open meteorology: met/none.txt$"):
         faceteb.run_faceteb_core(str(xml), str(tmp_path / "out" / "faceteb.json"), progress=None)
+    import json
+    index = json.loads((tmp_path / "out" / "faceteb_run.json").read_text())
+    assert index["status"] == "failed" and index["kind"] == "faceteb-run"
+    assert index["requested"] == {"endNodeExclusive": 1, "startNode": 0}
+    assert list(index) == sorted(index) and "finishedAt" in index
     (tmp_path / "met.txt").write_text("header\n1.5 20 15 1000 2 300 330\n")
     xml.write_text("<HiStreamProject><filePath>met.txt</filePath><endTimeNode>3</endTimeNode>"
                    "</HiStreamProject>")

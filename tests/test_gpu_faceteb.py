@@ -328,3 +328,9 @@ def test_faceteb_process_entry_on_an_xml_project(tmp_path):
     area = sum(float(r.split(",")[0]) for r in node[1:])
     assert abs(area - float(summary[2].split(",")[2])) <= 1e-4 * area
     assert float(summary[2].split(",")[-1]) > float(summary[1].split(",")[-1]) > 0.0
+    index = json.loads((tmp_path / "out" / "faceteb_run.json").read_text())
+    assert index["status"] in ("completed", "non_converged") and len(index["completed"]) == 2
+    assert [c["token"] for c in index["completed"]] == [faceteb.time_token(172.375),
+                                                        faceteb.time_token(172.5)]
+    assert index["products"][:2] == ["photovoltaic_summary.csv", ".facet_steps/components.bin"]
+    assert index["products"][-1] == "faceteb.json" and index["convergence"]["iterationBudget"] == 6

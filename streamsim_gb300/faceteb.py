@@ -20,6 +20,7 @@ formats:
   photovoltaic_node_<node>.csv,
   photovoltaic_summary.csv                 :3433-3435, 3847-3860
   faceteb_run.json                         :58-73, 3213-3222, 4030-4041, 4144-4147
+  process/<model>_T=<time>.bin / .json     :3936-4021
 
   solar_sun                                :3290-3327 (updateSolarPosition)
 
@@ -230,7 +231,7 @@ class Run:
 
     def run(self, meteorology, sun_for=None, start_node=0, end_node=None, output_dir=None,
             vertices=None, graph=None, progress=print, latitude=40.0, longitude=116.0,
-            run_index=None):
+            run_index=None, process=(False, False)):
         """Nodes [start_node, end_node) of the meteorology rows.  Writes the
         reference's step records and faceteb.json under output_dir when
         given.  sun_for defaults to solar_sun(latitude, longitude).  Returns
@@ -282,8 +283,13 @@ class Run:
                 rec = np.stack([np.asarray(c, np.float32) for c in cols], 1)
                 rec.astype("<f4").tofile(os.path.join(steps, f"energy_T={token}.bin"))
             if output_dir and area is not None:
-                energy_kwh = self._write_pv(output_dir, node, token, fields, area, pv, summary,
-                                            energy_kwh)
+                energy_kwh, pv_area = self._write_pv(output_dir, node, token, fields, area, pv,
+                                                     summary, energy_kwh)
+                for kind, on in (("radiation", process[0]), ("energy", process[1]),
+                                 ("photovoltaic", pv_area > 0)):
+                    if on:
+                        self._write_process(output_dir, kind, node, row, token, zenith, azimuth,
+                                            fields, res, F, run_index)
             if run_index is not None:
                 run_index.node(node, token, row["julian_time"], res,
                                self.params.temperature_tolerance, self.params.coupling_iterations)
@@ -348,7 +354,64 @@ class Run:
             energy_kwh += pp * float(self.settings.get("time_step", 1800.0)) / 3600000.0
             summary.write(",".join([str(node), token] + [_g(x) for x in (
                 pa, pt / pa, pg, pab, pp, plw, ph, ps, pres, energy_kwh)]) + "\n")
-        return energy_kwh
+        return energy_kwh, pa
+
+    def _write_process(self, output_dir, kind, node, row, token, zenith, azimuth, fields, res,
+                       facet_count, run_index):
+        """process/<model>_T=<token>.bin and .json (facetrtcore.cpp:3936-4021):
+        per side 3 floats (radiation: shortwave, final longwave radiosity, net
+        radiation; photovoltaic: PV power, temperature, absorbed shortwave)
+        or 5 (energy: latent, sensible, storage, temperature, net
+        radiation), float32 little-endian, and the metadata."""
+        model = "facetrt" if kind == "radiation" else "faceteb"
+        stem = model + ("_pv_T=" if kind == "photovoltaic" else "_T=") + token
+        folder = os.path.join(output_dir, "process")
+        os.makedirs(folder, exist_ok=True)
+        if run_index is not None:
+            run_index.value["products"] += [f"process/{stem}.bin", f"process/{stem}.json"]
+        cols = {"radiation": ("shortwave_radiosity", "longwave_radiosity", "net_radiation"),
+                "photovoltaic": ("photovoltaic_power", "temperature", "absorbed_shortwave"),
+                "energy": ("latent_heat", "sensible_heat", "storage_heat", "temperature",
+                           "net_radiation")}[kind]
+        rec = np.stack([np.asarray(fields[c], np.float32) for c in cols], 1)
+        rec.astype("<f4").tofile(os.path.join(folder, stem + ".bin"))
+        g9 = lambda x: format(float(x), ".9g")
+        labels = {
+            "photovoltaic": '[{"id":"photovoltaicPower","label":"光伏功率 [W m⁻²]","offset":0},'
+                            '{"id":"temperature","label":"温度 [K]","offset":1},'
+                            '{"id":"absorbedShortwave","label":"单面吸收短波 [W m⁻²]","offset":2}]',
+            "radiation": '[{"id":"shortwaveRadiation","label":"短波辐射 [W m⁻²]","offset":0},'
+                         '{"id":"longwaveRadiation","label":"长波辐射 [W m⁻²]","offset":1},'
+                         '{"id":"netRadiation","label":"净辐射 [W m⁻²]","offset":2}]',
+            "energy": '[{"id":"latentHeat","label":"潜热 [W m⁻²]","offset":0},'
+                      '{"id":"sensibleHeat","label":"显热 [W m⁻²]","offset":1},'
+                      '{"id":"surfaceHeatFlux","label":"表面热通量 [W m⁻²]","offset":2},'
+                      '{"id":"temperature","label":"温度 [K]","offset":3},'
+                      '{"id":"netRadiation","label":"净辐射 [W m⁻²]","offset":4}]'}[kind]
+        f32 = np.float32
+        text = (
+            "{\n" + f'  "kind": "facet-{kind}-process",\n' + f'  "model": "{model}",\n'
+            + f'  "processType": "{kind}",\n' + '  "geometry": "facet",\n'
+            + f'  "node": {node},\n' + f'  "julianTime": {g9(f32(row["julian_time"]))},\n'
+            + f'  "time": "{token}",\n' + f'  "solarZenith": {g9(f32(zenith))},\n'
+            + f'  "solarAzimuth": {g9(f32(azimuth))},\n' + f'  "facetCount": {facet_count},\n'
+            + f'  "surfaceCount": {2 * facet_count},\n'
+            + '  "geometryFile": "../faceteb.json",\n'
+            + '  "componentFile": "../.facet_steps/components.bin",\n'
+            + f'  "dataFile": "{stem}.bin",\n' + '  "dataType": "float32-little-endian",\n'
+            + '  "layout": "surface-interleaved",\n' + f'  "recordFloats": {len(cols)},\n'
+            + f'  "couplingIterations": {int(res["coupling_iterations"])},\n'
+            + f'  "temperatureDelta": {g9(f32(res["max_temperature_delta"]))}'
+            + f',\n  "converged": {"true" if res["converged"] else "false"}'
+            + f',\n  "energyResidual": {g9(f32(res["max_energy_residual"]))}'
+            + ',\n  "energyResidualUnits": "W m-2"'
+            + f',\n  "energyResidualTemperatureEquivalent": '
+              f'{g9(f32(res["max_energy_residual_equivalent"]))}'
+            + f',\n  "temperatureTolerance": {g9(f32(self.params.temperature_tolerance))}'
+            + f',\n  "iterationBudget": {self.params.coupling_iterations},\n  "fields": '
+            + labels + "\n}\n")
+        with open(os.path.join(folder, stem + ".json"), "w", encoding="utf-8") as f:
+            f.write(text)
 
     def _write_result(self, path, last, all_converged, vertices, graph):
         fields, res, lit, token = last
@@ -468,9 +531,11 @@ def run_faceteb_core(input_path, output_file="", progress=print):
     graph of the 40 hemisphere directions (:3329-3371), then the node
     sequence of Run with each node's sun from its date.  Writes
     .facet_steps/components.bin, .facet_steps/energy_T=<time>.bin per node
-    and faceteb.json, the photovoltaic node and summary tables and the run
-    index faceteb_run.json; prints PROGRESS lines and RESULT\t<path>.  Not
-    written: the process/ folder and images.  Returns the result file."""
+    and faceteb.json, the photovoltaic node and summary tables, the run
+    index faceteb_run.json and the process/ records (radiation and energy
+    when the project asks, photovoltaic when it has PV); prints PROGRESS
+    lines and RESULT\t<path>.  Not written: images.  Returns the result
+    file."""
     ext = os.path.splitext(input_path)[1].lower()
     is_obj = ext == ".obj"
     if ext == ".json":
@@ -512,6 +577,12 @@ def _run_faceteb(xml, input_path, result_file, out_dir, start, end, dtime, setti
                  progress):
     """run_faceteb_core after its settings (the run index is open)."""
     is_obj = os.path.splitext(input_path)[1].lower() == ".obj"
+    # isRadiationProcess / isEnergyProcess, isProcess meaning energy (:3199-3205)
+    save_radiation = first_xml_tag(xml, "isRadiationProcess").strip() == "1"
+    save_energy = first_xml_tag(xml, "isEnergyProcess").strip() == "1"
+    if not save_radiation and not save_energy and first_xml_tag(xml, "isProcess").strip() == "1":
+        save_energy = True
+    process = (save_radiation, save_energy)
     width = int(np.clip(round(xml_float(xml, "spectralAccelerationWidth", 100.0)), 1, 1000))
     latitude = xml_float(xml, "Latitude", 40.0)
     longitude = xml_float(xml, "Longitude", 116.0)
@@ -567,7 +638,8 @@ def _run_faceteb(xml, input_path, result_file, out_dir, start, end, dtime, setti
                   background_angular_strength=strength, **settings)
         results, _ = run.run(meteorology, None, start, end, output_dir=out_dir,
                              vertices=vertices, graph=diag, progress=progress,
-                             latitude=latitude, longitude=longitude, run_index=index)
+                             latitude=latitude, longitude=longitude, run_index=index,
+                             process=process)
         written = os.path.join(out_dir, "faceteb.json")
         if os.path.abspath(written) != os.path.abspath(result_file):
             os.replace(written, result_file)

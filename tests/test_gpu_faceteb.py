@@ -292,7 +292,9 @@ def test_faceteb_process_entry_on_an_xml_project(tmp_path):
                           extra_control="<endTimeNode>2</endTimeNode><dTime>10800</dTime>"
                                         "<filePath>met.txt</filePath><Latitude>35</Latitude>"
                                         "<Longitude>110</Longitude>"
-                                        "<couplingIterations>6</couplingIterations>")
+                                        "<couplingIterations>6</couplingIterations>"
+                                        "<isRadiationProcess>1</isRadiationProcess>"
+                                        "<isEnergyProcess>1</isEnergyProcess>")
     out = faceteb.run_faceteb_core(path, str(tmp_path / "out" / "faceteb.json"), progress=None)
     doc = json.load(open(out))
     p = facetcu.Project(path)
@@ -334,3 +336,21 @@ def test_faceteb_process_entry_on_an_xml_project(tmp_path):
                                                         faceteb.time_token(172.5)]
     assert index["products"][:2] == ["photovoltaic_summary.csv", ".facet_steps/components.bin"]
     assert index["products"][-1] == "faceteb.json" and index["convergence"]["iterationBudget"] == 6
+    # process records of the last node: the same fields as its step record
+    tok = faceteb.time_token(172.5)
+    rec = np.fromfile(steps / f"energy_T={tok}.bin", "<f4").reshape(2 * F, 12)
+    proc = tmp_path / "out" / "process"
+    rad = np.fromfile(proc / f"facetrt_T={tok}.bin", "<f4").reshape(2 * F, 3)
+    eng = np.fromfile(proc / f"faceteb_T={tok}.bin", "<f4").reshape(2 * F, 5)
+    pvr = np.fromfile(proc / f"faceteb_pv_T={tok}.bin", "<f4").reshape(2 * F, 3)
+    assert np.array_equal(rad, rec[:, [2, 3, 4]])        # shortwave, longwave, net
+    assert np.array_equal(eng, rec[:, [6, 5, 7, 0, 4]])  # latent, sensible, storage, T, net
+    assert np.array_equal(pvr[:, 1], rec[:, 0])
+    meta = json.loads((proc / f"faceteb_T={tok}.json").read_text(encoding="utf-8"))
+    assert meta["kind"] == "facet-energy-process" and meta["recordFloats"] == 5
+    assert meta["surfaceCount"] == 2 * F and meta["time"] == tok and meta["node"] == 1
+    assert [f["id"] for f in meta["fields"]] == ["latentHeat", "sensibleHeat", "surfaceHeatFlux",
+                                                 "temperature", "netRadiation"]
+    zen, az = facetcu.faceteb_sun(172.5, 35.0, 110.0, 1003.0, 26.0)
+    assert abs(meta["solarZenith"] - float(zen)) < 1e-5 and abs(meta["solarAzimuth"] - float(az)) < 1e-4
+    assert f"process/facetrt_T={tok}.bin" in index["products"]

@@ -78,10 +78,11 @@ def test_photovoltaic_tables(tmp_path):
     fields["temperature"] = np.full(S, 300.0, np.float32)
     with open(tmp_path / "photovoltaic_summary.csv", "w") as summary:
         summary.write(faceteb.PV_SUMMARY_HEADER)
-        e = run._write_pv(str(tmp_path), 0, "DOY1_00-00", fields, faceteb.facet_areas(v),
-                          run._pv_facets(), summary, 0.0)
-        e = run._write_pv(str(tmp_path), 1, "DOY1_01-00", fields, faceteb.facet_areas(v),
-                          run._pv_facets(), summary, e)
+        e, pa = run._write_pv(str(tmp_path), 0, "DOY1_00-00", fields, faceteb.facet_areas(v),
+                              run._pv_facets(), summary, 0.0)
+        assert pa == 2.0  # PV facets 0 and 2: 0.5 + 1.5
+        e, _ = run._write_pv(str(tmp_path), 1, "DOY1_01-00", fields, faceteb.facet_areas(v),
+                             run._pv_facets(), summary, e)
     rows = (tmp_path / "photovoltaic_node_0.csv").read_text().splitlines()
     assert rows[0] == faceteb.PV_NODE_HEADER.strip() and len(rows) == 3  # facets 0 and 2
     first = rows[1].split(",")

@@ -251,11 +251,15 @@ def build_workload(args, fc, scenes, oracle_mod=None):
     t0 = time.perf_counter()
     if mode == "hemisphere":
         uv, dirs = scenes.hemisphere_samples(args.rays, 32, seed=7)
+        tg = time.perf_counter()
         diag, dropped = m.buildHemisphereGraph(uv, dirs, args.rays, args.top_k, 32)
+        graph_s = time.perf_counter() - tg  # the call returns with the graph on the device
         suv, _ = scenes.hemisphere_samples(256, 32, seed=8)
         lit = m.hemisphereSunlit(sun, suv, 256, 32)
+        rays = args.rays * 2.0 * sc.facet_count
         vf = {"mode": "hemisphere", "rays_per_side": args.rays, "top_k": args.top_k,
-              "dropped_ray_fraction": dropped / (args.rays * 2.0 * sc.facet_count)}
+              "dropped_ray_fraction": dropped / rays, "graph_s": graph_s,
+              "rays_per_s": rays / graph_s}
     else:
         diag = m.buildVisibilityGraph(scenes.hemisphere_directions())
         lit = m.computeSunlitFraction(sun)

@@ -664,8 +664,8 @@ int facetcu_render_sensor_image(facetcu_context *ctx, const facetcu_sensor *sens
  * grid, raised by the project's DEM (facetcu_dem_height_field) under the
  * ground and every placement; materials from custom, file, PROSPECT and BSM
  * spectra (the models' optipar.txt beside the sun spectrum), thermal blocks,
- * soil sets and surface-energy blocks.  Physical textures need GDAL and are
- * refused with the reference's message.  A project.json is read through
+ * soil sets and surface-energy blocks, physical reflectance textures (ESRI
+ * ASCII grids and baseline GeoTIFF, as the DEM).  A project.json is read through
  * its XML view (facetcu_project_xml_view).  Host only; errors through
  * facetcu_host_last_error(). */
 typedef struct facetcu_project facetcu_project;

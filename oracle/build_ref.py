@@ -133,9 +133,10 @@ def compile_lib():
 # reference's XML input) with the CPU span it builds on and the spectral
 # models it calls (Compo::resolveSpectrals with fluspect and bsm,
 # compo.cpp; Utils::expint, utils.cpp; their types from structs.h and
-# structs_cg.h).  GDAL (DEM and texture files) and the project.json view
-# (nlohmann::json) are not available here: oracle/ref_project_stubs.inc
-# declares stand-ins that fail loudly, so projects using them are refused.
+# structs_cg.h).  GDAL is not available here: oracle/ref_project_stubs.inc
+# declares a stand-in that opens ESRI ASCII grids (DEM and texture files in
+# that format), and one for the project.json view (nlohmann::json) that
+# fails loudly.
 PROJECT_RANGES = [
     ("base/structs.h", 122, 128, None, None),
     ("base/structs.h", 148, 186, None, None),
@@ -149,7 +150,7 @@ PROJECT_RANGES = [
     ("facetrt/facetrt_vulkan.h", 15, 62, "namespace facetvk {", "}"),
     ("facetrt/facetrtcore.cpp", 39, 53, "namespace {", None),
     ("facetrt/facetrtcore.cpp", 74, 630, None, None),
-    ("@", 0, 0, "texture", None),
+    ("facetrt/facetrtcore.cpp", 631, 702, None, None),
     ("facetrt/facetrtcore.cpp", 703, 1620, None, None),
     ("@", 0, 0, "view", None),
     ("facetrt/facetrtcore.cpp", 2038, 3025, None, "}  // namespace"),
@@ -164,6 +165,8 @@ PROJECT_ANCHORS = [
     ("base/compo.cpp", 152, "float Compo::calctav(float alfa,float nr)"),
     ("base/compo.cpp", 275, "std::vector<Spectral> Compo::resolveSpectrals("),
     ("base/compo.cpp", 436, "void Compo::bsm(OptCoeff bsmCoeff,BSMParam bsm,std::vector<Spectral>& spectrals){"),
+    ("facetrt/facetrtcore.cpp", 631,
+     "std::shared_ptr<const ReflectanceVarianceTexture> loadReflectanceVarianceTexture("),
     ("facetrt/facetrtcore.cpp", 2038, "std::string readTextFile(const std::string& path)"),
     ("facetrt/facetrtcore.cpp", 2880, "Scene loadProjectScene(const std::string& inputFile)"),
     ("facetrt/facetrtcore.cpp", 3025, "}"),

@@ -54,6 +54,7 @@ struct ReadError : std::runtime_error {
 // A raster as GDAL hands it over: band 1 converted to float32, its nodata.
 struct Raster {
     int width = 0, height = 0;
+    int bands = 1;  // raster bands (samples per pixel)
     bool has_nodata = false;
     double nodata = 0.0;
     std::vector<float> values;
@@ -497,7 +498,7 @@ float double_to_float(double d)
     return float(d);
 }
 
-Raster read_tiff(const std::vector<uint8_t>& bytes)
+Raster read_tiff(const std::vector<uint8_t>& bytes, int band)
 {
     Tiff t{bytes};
     t.big_endian = bytes[0] == 'M';
@@ -588,12 +589,15 @@ Raster read_tiff(const std::vector<uint8_t>& bytes)
     const size_t row_bytes = size_t(cw) * pixel_bytes;
     const size_t block_bytes = row_bytes * size_t(ch);
     if (offsets.size() < per_plane * (planar == 1 ? 1 : spp)) throw OpenError("tiff: offsets");
-    if (!counts.empty() && counts.size() < per_plane) throw OpenError("tiff: byte counts");
+    if (!counts.empty() && counts.size() < per_plane * (planar == 1 ? 1 : spp))
+        throw OpenError("tiff: byte counts");
     if (counts.empty() && compression != 1) throw OpenError("tiff: byte counts");
 
+    if (band < 0 || uint64_t(band) >= spp) throw ReadError("tiff: band");
     Raster r;
     r.width = int(width);
     r.height = int(height);
+    r.bands = int(spp);
     if (seen[15] && tags[15].type == 2) {
         std::string s(reinterpret_cast<const char*>(bytes.data() + tags[15].data),
                       size_t(tags[15].count));
@@ -602,12 +606,15 @@ Raster read_tiff(const std::vector<uint8_t>& bytes)
         r.nodata = std::strtod(s.c_str(), nullptr);
     }
     r.values.assign(size_t(width) * size_t(height), 0.0f);
-    for (uint64_t bi = 0; bi < per_plane; ++bi) {  // band 1: the first plane
-        const uint64_t off = offsets[size_t(bi)];
+    // the band's plane (planar) or its sample within each pixel (chunky)
+    const uint64_t plane0 = planar == 2 ? uint64_t(band) * per_plane : 0;
+    const size_t sample0 = planar == 2 ? 0 : size_t(band) * sample_bytes;
+    for (uint64_t bi = 0; bi < per_plane; ++bi) {
+        const uint64_t off = offsets[size_t(plane0 + bi)];
         const uint64_t rows_here =
             tiled ? ch : std::min<uint64_t>(ch, height - (bi / across) * ch);
         const size_t want = tiled ? block_bytes : row_bytes * size_t(rows_here);
-        const uint64_t cnt = counts.empty() ? want : counts[size_t(bi)];
+        const uint64_t cnt = counts.empty() ? want : counts[size_t(plane0 + bi)];
         if (off + cnt > bytes.size()) throw ReadError("tiff: block outside the file");
         const uint8_t* src = bytes.data() + off;
         std::vector<uint8_t> block;
@@ -658,7 +665,7 @@ Raster read_tiff(const std::vector<uint8_t>& bytes)
             if (by + y >= height) break;
             for (size_t x = 0; x < size_t(cw); ++x) {
                 if (bx + x >= width) break;
-                const size_t at = y * row_bytes + x * pixel_bytes;  // sample 0 of the pixel
+                const size_t at = y * row_bytes + x * pixel_bytes + sample0;
                 uint64_t raw = 0;
                 for (size_t k = 0; k < sample_bytes; ++k) {
                     const size_t kk = t.big_endian ? sample_bytes - 1 - k : k;
@@ -690,7 +697,7 @@ Raster read_tiff(const std::vector<uint8_t>& bytes)
     return r;
 }
 
-Raster read_raster(const std::filesystem::path& path)
+Raster read_raster(const std::filesystem::path& path, int band = 0)
 {
     std::ifstream in(path, std::ios::binary);
     if (!in) throw OpenError("cannot open");
@@ -698,9 +705,12 @@ Raster read_raster(const std::filesystem::path& path)
                                      std::istreambuf_iterator<char>()};
     if (bytes.size() >= 8 && ((bytes[0] == 'I' && bytes[1] == 'I') ||
                               (bytes[0] == 'M' && bytes[1] == 'M')))
-        return read_tiff(bytes);
+        return read_tiff(bytes, band);
     const std::string text(bytes.begin(), bytes.end());
-    if (looks_ascii_grid(text)) return read_ascii_grid(text);
+    if (looks_ascii_grid(text)) {
+        if (band != 0) throw ReadError("ascii grid: one band");
+        return read_ascii_grid(text);
+    }
     throw OpenError("not a raster");
 }
 
@@ -734,6 +744,36 @@ HeightField read_height_field(const std::filesystem::path& path)
     for (float& v : h.values)
         if (!std::isfinite(v) || (r.has_nodata && v == nodata)) v = h.minimum;
     return h;
+}
+
+// Up to `max_bands` bands as bytes, as a GDAL RasterIO into GDT_Byte
+// converts them: rounded to the nearest integer (halves up) and clamped to
+// [0, 255], NaN as 0.
+ByteBands read_byte_bands(const std::filesystem::path& path, int max_bands,
+                          const std::string& open_error, const std::string& read_error)
+{
+    const std::string name = path.string();
+    ByteBands out;
+    try {
+        Raster first = read_raster(path, 0);
+        out.width = first.width;
+        out.height = first.height;
+        out.count = std::min(max_bands, first.bands);
+        for (int b = 0; b < out.count; ++b) {
+            const Raster r = b == 0 ? std::move(first) : read_raster(path, b);
+            std::vector<uint8_t>& v = out.values[size_t(b)];
+            v.resize(r.values.size());
+            for (size_t i = 0; i < v.size(); ++i) {
+                const float x = r.values[i];
+                v[i] = std::isnan(x) ? 0 : x >= 255.0f ? 255 : x <= 0.0f ? 0 : uint8_t(x + 0.5f);
+            }
+        }
+    } catch (const ReadError&) {
+        throw std::runtime_error(read_error + name);
+    } catch (const std::exception&) {
+        throw std::runtime_error(open_error + name);
+    }
+    return out;
 }
 
 // DemHeightField::heightAboveMinimum (facetrtcore.cpp:2630-2649): GeoTIFF

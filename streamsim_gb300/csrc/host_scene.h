@@ -80,6 +80,14 @@ struct HeightField {
 // readDemHeightField's file step (facetrtcore.cpp:2660-2696) over ESRI ASCII
 // grids and baseline GeoTIFF; throws the reference's messages.
 HeightField read_height_field(const std::filesystem::path& path);
+// Up to max_bands raster bands as bytes (GDAL's RasterIO into GDT_Byte);
+// failures throw open_error / read_error followed by the path.
+struct ByteBands {
+    int width = 0, height = 0, count = 0;
+    std::vector<uint8_t> values[3];
+};
+ByteBands read_byte_bands(const std::filesystem::path& path, int max_bands,
+                          const std::string& open_error, const std::string& read_error);
 }  // namespace dem
 
 namespace project {

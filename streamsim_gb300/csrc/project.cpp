@@ -20,11 +20,13 @@
 // pow) resolve to the C library's double functions; here they are written as
 // std::fn(double(x)) with the same float/double promotions.
 //
-// DEM height fields are read by dem.cpp (ESRI ASCII grids and baseline
-// GeoTIFF, the formats GDAL would open for the reference).  Not supported, as
-// GDAL is not available: physical reflectance textures (they fail with the
-// reference's message).  A project.json is read through its XML view
-// (project_json.cpp), as the reference's readTextFile does.
+// DEM height fields and physical reflectance textures are read by dem.cpp
+// (ESRI ASCII grids and baseline GeoTIFF, the formats GDAL would open for the
+// reference); the texture steps (loadReflectanceVarianceTexture,
+// sampledReflectanceVariance, finalizeReflectanceTextureFactors,
+// facetrtcore.cpp:623-846) are restated here.  A project.json is read
+// through its XML view (project_json.cpp), as the reference's readTextFile
+// does.
 #include <algorithm>
 #include <array>
 #include <cctype>
@@ -56,6 +58,26 @@ using host::V3;
 constexpr int kSamples = 2001;  // 400..2400 nm at 1 nm (N1)
 constexpr float kPi = 3.14159265358979323846f;
 
+// ReflectanceVarianceTexture (facetrtcore.cpp:88-111): luminance deviations
+// in [-1, 1], sampled bilinearly with wrap-around.
+struct Texture {
+    int width = 0, height = 0;
+    std::vector<float> values;
+    float sample(float u, float v) const
+    {
+        if (width <= 0 || height <= 0 || values.empty()) return 0.0f;
+        const float x = (u - std::floor(u)) * float(width);
+        const float y = (v - std::floor(v)) * float(height);
+        const int x0 = int(std::floor(x)) % width, y0 = int(std::floor(y)) % height;
+        const int x1 = (x0 + 1) % width, y1 = (y0 + 1) % height;
+        const float tx = x - std::floor(x), ty = y - std::floor(y);
+        const auto at = [this](int c, int r) { return values[size_t(r) * size_t(width) + size_t(c)]; };
+        const float top = at(x0, y0) * (1.0f - tx) + at(x1, y0) * tx;
+        const float bottom = at(x0, y1) * (1.0f - tx) + at(x1, y1) * tx;
+        return top * (1.0f - ty) + bottom * ty;
+    }
+};
+
 // SurfaceParameters with the reference's defaults (facetrtcore.cpp:113-138).
 struct Surface {
     std::vector<float> r{0.10f}, t{0.05f}, er, et;
@@ -67,7 +89,54 @@ struct Surface {
     float eta25 = 0.22f, gamma = -0.0035f, bif = 0.0f, conv = 1.0f;
     uint8_t component = 0;
     float tex_strength = 0.0f, tex_repeat = 1.0f;
+    std::shared_ptr<const Texture> texture;
 };
+
+// srgbToLinear (facetrtcore.cpp:623-629).
+float srgb_to_linear(float value)
+{
+    value = std::clamp(value, 0.0f, 1.0f);
+    return value <= 0.04045f ? value / 12.92f : std::pow((value + 0.055f) / 1.055f, 2.4f);
+}
+
+// loadReflectanceVarianceTexture (facetrtcore.cpp:631-702): up to three
+// bands as bytes, linear luminance, its mean removed and the deviations
+// scaled to [-1, 1].  The raster is read by dem.cpp (ESRI ASCII grids and
+// baseline GeoTIFF, the formats GDAL would open here).
+std::shared_ptr<const Texture> load_texture(const std::filesystem::path& path)
+{
+    const std::string key = std::filesystem::absolute(path).lexically_normal().string();
+    const dem::ByteBands b = dem::read_byte_bands(key, 3,
+                                                  "Cannot open reflectance variance texture: ",
+                                                  "Cannot read reflectance variance texture: ");
+    if (b.width < 2 || b.height < 2)
+        throw std::runtime_error(
+            "Reflectance variance texture must contain at least 2 x 2 pixels: " + key);
+    auto t = std::make_shared<Texture>();
+    t->width = b.width;
+    t->height = b.height;
+    const size_t n = size_t(b.width) * size_t(b.height);
+    t->values.resize(n);
+    double mean = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        const float red = srgb_to_linear(b.values[0][i] / 255.0f);
+        const float green = b.count > 1 ? srgb_to_linear(b.values[1][i] / 255.0f) : red;
+        const float blue = b.count > 2 ? srgb_to_linear(b.values[2][i] / 255.0f) : red;
+        const float luminance = 0.2126f * red + 0.7152f * green + 0.0722f * blue;
+        t->values[i] = luminance;
+        mean += luminance;
+    }
+    mean /= double(n);
+    float max_abs = 0.0f;
+    for (float& v : t->values) {
+        v -= float(mean);
+        max_abs = std::max(max_abs, std::abs(v));
+    }
+    if (!(max_abs > 1.0e-6f))
+        throw std::runtime_error("Reflectance variance texture is effectively constant: " + key);
+    for (float& v : t->values) v /= max_abs;
+    return t;
+}
 
 struct Parameters {  // FacetRTParameters (:140-146)
     std::vector<float> wavelengths{550.0f};
@@ -588,8 +657,9 @@ void load_surface(const std::string& xml, const std::string& spectral_name,
             if (file.empty())
                 throw std::runtime_error("Physical texture is enabled but has no file: " +
                                          spectral_name);
-            throw std::runtime_error("physical texture files need GDAL: " +
-                                     resolve(input, file).string());
+            s.tex_strength = std::clamp(xml_float(sp, "physicalTextureStrength", 0.2f), 0.0f, 1.0f);
+            s.tex_repeat = std::max(0.01f, xml_float(sp, "physicalTextureRepeatSize", 2.0f));
+            s.texture = load_texture(resolve(input, file));
         }
     }
     const std::string th = named_block(xml, "thermal", thermal_name);
@@ -826,6 +896,119 @@ void append_ground(host::HostScene& sc, float width, float depth, float voxel, u
     }
 }
 
+// facetArea (facetrtcore.cpp:704-716).
+float facet_area(const host::HostScene& sc, uint32_t f)
+{
+    const float* a = sc.vertices[3 * f].position;
+    const float* b = sc.vertices[3 * f + 1].position;
+    const float* c = sc.vertices[3 * f + 2].position;
+    const V3 ea{b[0] - a[0], b[1] - a[1], b[2] - a[2]}, eb{c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+    const V3 n = host::cross3(ea, eb);
+    return 0.5f * std::sqrt(host::dot3(n, n));
+}
+
+// sampledReflectanceVariance (:718-741): the texture on the three axis
+// planes through the facet's centre, weighted by |normal|.
+float sampled_variance(const host::HostScene& sc, uint32_t f, const Surface& s)
+{
+    if (!s.texture) return 0.0f;
+    const facetcu_vertex &a = sc.vertices[3 * f], &b = sc.vertices[3 * f + 1],
+                         &c = sc.vertices[3 * f + 2];
+    const V3 centre{(a.position[0] + b.position[0] + c.position[0]) / 3.0f,
+                    (a.position[1] + b.position[1] + c.position[1]) / 3.0f,
+                    (a.position[2] + b.position[2] + c.position[2]) / 3.0f};
+    const V3 n{std::abs(a.normal[0]), std::abs(a.normal[1]), std::abs(a.normal[2])};
+    const float weight = std::max(1.0e-6f, n[0] + n[1] + n[2]);
+    const float inv = 1.0f / std::max(0.01f, s.tex_repeat);
+    const Texture& t = *s.texture;
+    return (n[0] * t.sample(centre[2] * inv, centre[1] * inv) +
+            n[1] * t.sample(centre[0] * inv, centre[2] * inv) +
+            n[2] * t.sample(centre[0] * inv, centre[1] * inv)) / weight;
+}
+
+// maximumMeanPreservingFactor (:743-762).
+float max_mean_preserving_factor(const Surface& s)
+{
+    float m = std::numeric_limits<float>::infinity();
+    const auto bands = [&m](const std::vector<float>& r, const std::vector<float>& t) {
+        for (size_t band = 0; band < r.size(); ++band) {
+            const float base = std::clamp(r[band], 0.0f, 1.0f);
+            if (!(base > 1.0e-6f)) continue;
+            const float tau =
+                t.empty() ? 0.0f : std::clamp(t[std::min(band, t.size() - 1)], 0.0f, 1.0f - base);
+            m = std::min(m, (1.0f - tau) / base);
+        }
+    };
+    bands(s.r, s.t);
+    bands(s.er, s.et);
+    return m;
+}
+
+// finalizeReflectanceTextureFactors (:764-846): per textured material the
+// area-weighted mean sample is removed and the deviations are scaled so the
+// factors stay positive and below the mean-preserving bound.
+std::vector<float> texture_factors(const host::HostScene& sc, const std::vector<Surface>& mats)
+{
+    const uint32_t F = sc.facets();
+    std::vector<float> factors(F, 1.0f);
+    if (F == 0 || mats.empty()) return factors;
+    struct Stats {
+        double area = 0.0, weighted = 0.0;
+        float min_dev = 0.0f, max_dev = 0.0f, scale = 0.0f;
+        double weighted_factor = 0.0;
+        float min_factor = std::numeric_limits<float>::infinity();
+        float max_factor = std::numeric_limits<float>::lowest();
+    };
+    std::vector<Stats> st(mats.size());
+    std::vector<float> samples(F, 0.0f), areas(F, 0.0f);
+    for (uint32_t f = 0; f < F; ++f) {
+        if (f >= sc.material.size()) continue;
+        const uint32_t m = sc.material[f];
+        if (m >= mats.size()) continue;
+        const Surface& s = mats[m];
+        if (!s.texture || !(s.tex_strength > 0.0f)) continue;
+        areas[f] = facet_area(sc, f);
+        samples[f] = sampled_variance(sc, f, s);
+        st[m].area += areas[f];
+        st[m].weighted += double(areas[f]) * samples[f];
+    }
+    for (uint32_t f = 0; f < F; ++f) {
+        if (f >= sc.material.size() || !(areas[f] > 0.0f)) continue;
+        Stats& x = st[sc.material[f]];
+        const float mean = x.area > 0.0 ? float(x.weighted / x.area) : 0.0f;
+        const float dev = samples[f] - mean;
+        samples[f] = dev;
+        x.min_dev = std::min(x.min_dev, dev);
+        x.max_dev = std::max(x.max_dev, dev);
+    }
+    for (size_t m = 0; m < mats.size(); ++m) {
+        Stats& x = st[m];
+        if (!(x.area > 0.0)) continue;
+        float scale = std::clamp(mats[m].tex_strength, 0.0f, 1.0f);
+        if (x.min_dev < 0.0f) scale = std::min(scale, 0.999f / -x.min_dev);
+        const float bound = max_mean_preserving_factor(mats[m]);
+        if (x.max_dev > 0.0f && std::isfinite(bound))
+            scale = std::min(scale, std::max(0.0f, bound - 1.0f) / x.max_dev);
+        x.scale = scale;
+    }
+    for (uint32_t f = 0; f < F; ++f) {
+        if (f >= sc.material.size() || !(areas[f] > 0.0f)) continue;
+        Stats& x = st[sc.material[f]];
+        const float factor = 1.0f + x.scale * samples[f];
+        factors[f] = factor;
+        x.weighted_factor += double(areas[f]) * factor;
+        x.min_factor = std::min(x.min_factor, factor);
+        x.max_factor = std::max(x.max_factor, factor);
+    }
+    for (size_t m = 0; m < st.size(); ++m)
+        if (st[m].area > 0.0)
+            std::cout << "facetrt: physical texture material " << m
+                      << ", area-weighted factor mean=" << st[m].weighted_factor / st[m].area
+                      << ", range=[" << st[m].min_factor << ',' << st[m].max_factor << "]"
+                      << std::endl;
+    return factors;
+}
+
 uint32_t adaptive_layers(uint32_t facets, uint32_t periodic, uint32_t raster, uint32_t layers)
 {
     const double pixels = double(raster) * raster;
@@ -941,7 +1124,7 @@ Project load(const std::string& path)
             sc.lo[a] = std::min(sc.lo[a], v.position[a]);
             sc.hi[a] = std::max(sc.hi[a], v.position[a]);
         }
-    P.texture.assign(sc.facets(), 1.0f);  // no physical textures
+    P.texture = texture_factors(sc, P.materials);
     // C views
     auto view = [](const Surface& s) {
         facetcu_surface_parameters v{};

@@ -274,3 +274,70 @@ def test_project_dem_errors_match_reference(tmp_path, ref_project):  # noqa: F81
         with pytest.raises(RuntimeError) as ours:
             facetcu.Project(path)
         assert str(ours.value) == str(theirs.value)
+
+
+# ---- physical reflectance textures (loadReflectanceVarianceTexture,
+# sampledReflectanceVariance, finalizeReflectanceTextureFactors:
+# facetrtcore.cpp:623-846), against the reference's own loader ------------
+def _texture_project(root, texture_file, strength="0.5", repeat="1.5", objects=None):
+    spectral = ("<spectral name=\"tex\" type=\"custom\"><reflectance>0.3</reflectance>"
+                "<transmittance>0.1</transmittance>"
+                "<physicalTextureEnabled>true</physicalTextureEnabled>"
+                f"<physicalTextureFile>{texture_file}</physicalTextureFile>"
+                f"<physicalTextureStrength>{strength}</physicalTextureStrength>"
+                f"<physicalTextureRepeatSize>{repeat}</physicalTextureRepeatSize></spectral>")
+    objects = objects or """
+<object objName="House"><componentType>Building</componentType><meshNames>wall, Roof</meshNames>
+<spectralNames>tex;concrete</spectralNames><bioNames>wallset</bioNames>
+<fileName>models/house.obj</fileName><objectPosition>positions/house.txt</objectPosition></object>
+<object objName="Box"><spectralNames>tex</spectralNames><bioNames>wallset</bioNames>
+<shapes>1.5,2,0.5</shapes></object>"""
+    return _write_project(root, coefficients=False, objects=objects, extra_spectral=spectral)
+
+
+def _pattern(h=23, w=31):
+    y, x = np.mgrid[0:h, 0:w]
+    # whole numbers within a byte (30 .. 230)
+    return np.floor(30 + 60 * (np.sin(x / 3.0) + 1) + 20 * ((x + y) % 5)).astype(np.float32)
+
+
+def test_textured_project_matches_reference(tmp_path, ref_project):  # noqa: F811
+    os.makedirs(tmp_path / "tex")
+    z = _pattern()
+    _write_asc(str(tmp_path / "tex" / "a.asc"), z)
+    path = _texture_project(tmp_path, "tex/a.asc")
+    theirs = ref_project.load(path)
+    ours = facetcu.Project(path)
+    _compare(ours, theirs)
+    f = ours.texture_factors
+    assert theirs["texture_factors"].size and np.any(f != 1.0) and np.all(f > 0.0)
+    # the same bytes as an 8-bit GeoTIFF give the same factors
+    tiff_writer.write(str(tmp_path / "tex" / "a.tif"), z.astype(np.uint8), rows_per_strip=4,
+                      compression=5, predictor=2)
+    tif = facetcu.Project(_texture_project(tmp_path, "tex/a.tif"))
+    assert np.array_equal(tif.texture_factors.view(np.uint32), f.view(np.uint32))
+
+
+def test_rgb_texture_loads(tmp_path):
+    os.makedirs(tmp_path / "tex")
+    z = _pattern()
+    rgb = np.stack([z, z[::-1], np.roll(z, 3, axis=1)], axis=2).astype(np.uint8)
+    tiff_writer.write(str(tmp_path / "tex" / "rgb.tif"), rgb, tile=(16, 16), compression=8)
+    f = facetcu.Project(_texture_project(tmp_path, "tex/rgb.tif")).texture_factors
+    assert np.any(f != 1.0) and np.all(np.isfinite(f)) and np.all(f > 0.0)
+
+
+@pytest.mark.parametrize("case", ["constant", "one_row", "missing"])
+def test_texture_errors_match_reference(tmp_path, ref_project, case):  # noqa: F811
+    os.makedirs(tmp_path / "tex")
+    if case == "constant":
+        _write_asc(str(tmp_path / "tex" / "t.asc"), np.full((5, 5), 128.0))
+    elif case == "one_row":
+        _write_asc(str(tmp_path / "tex" / "t.asc"), np.arange(9.0)[None, :])
+    path = _texture_project(tmp_path, "tex/t.asc")
+    with pytest.raises(RuntimeError) as theirs:
+        ref_project.load(path)
+    with pytest.raises(RuntimeError) as ours:
+        facetcu.Project(path)
+    assert str(ours.value) == str(theirs.value)
+    assert "reflectance variance texture" in str(ours.value).lower()

@@ -665,7 +665,7 @@ int facetcu_render_sensor_image(facetcu_context *ctx, const facetcu_sensor *sens
  * ground and every placement; materials from custom, file, PROSPECT and BSM
  * spectra (the models' optipar.txt beside the sun spectrum), thermal blocks,
  * soil sets and surface-energy blocks, physical reflectance textures (ESRI
- * ASCII grids and baseline GeoTIFF, as the DEM).  A project.json is read through
+ * ASCII grids, baseline GeoTIFF and PNG).  A project.json is read through
  * its XML view (facetcu_project_xml_view).  Host only; errors through
  * facetcu_host_last_error(). */
 typedef struct facetcu_project facetcu_project;

@@ -14,7 +14,9 @@
 //     tiles; chunky or planar; no compression, LZW, deflate or PackBits;
 //     predictors 1, 2 and 3; unsigned, signed and IEEE samples of 8-64 bits
 //     with float16; the GDAL_NODATA tag 42113).  Band 1 of the first image
-//     is read, as GDAL reads it.
+//     is read, as GDAL reads it;
+//   - non-interlaced PNG of 8 or 16 bits (gray, RGB, palette indices, gray
+//     + alpha, RGBA), for textures.
 // Any other file fails as the reference's GDALOpen failure does ("Cannot
 // open DEM: <path>"); a file that opens but cannot be decoded fails as its
 // RasterIO failure does ("Cannot read DEM elevations: <path>").
@@ -697,6 +699,86 @@ Raster read_tiff(const std::vector<uint8_t>& bytes, int band)
     return r;
 }
 
+// ---- PNG (ISO/IEC 15948) -----------------------------------------------------
+// Non-interlaced PNG of bit depth 8 or 16: gray (1 band), RGB (3), palette
+// (1 band of palette indices, as GDAL exposes it), gray + alpha (2), RGBA
+// (4); the five row filters undone after inflating the IDAT stream.
+Raster read_png(const std::vector<uint8_t>& b, int band)
+{
+    auto be32 = [&](size_t at) {
+        if (at + 4 > b.size()) throw OpenError("png: truncated");
+        return uint32_t(b[at]) << 24 | uint32_t(b[at + 1]) << 16 | uint32_t(b[at + 2]) << 8 | b[at + 3];
+    };
+    size_t at = 8;
+    uint32_t width = 0, height = 0;
+    int depth = 0, color = -1, interlace = 0;
+    std::vector<uint8_t> idat;
+    while (at + 8 <= b.size()) {
+        const uint32_t len = be32(at);
+        const std::string type(reinterpret_cast<const char*>(b.data() + at + 4), 4);
+        if (at + 12 + size_t(len) > b.size()) throw OpenError("png: chunk");
+        const uint8_t* d = b.data() + at + 8;
+        if (type == "IHDR") {
+            if (len < 13) throw OpenError("png: header");
+            width = be32(at + 8);
+            height = be32(at + 12);
+            depth = d[8];
+            color = d[9];
+            interlace = d[12];
+        } else if (type == "IDAT") {
+            idat.insert(idat.end(), d, d + len);
+        } else if (type == "IEND") {
+            break;
+        }
+        at += 12 + size_t(len);
+    }
+    const int channels = color == 0 ? 1 : color == 2 ? 3 : color == 3 ? 1 : color == 4 ? 2
+                         : color == 6 ? 4 : 0;
+    if (!channels || (depth != 8 && depth != 16) || interlace != 0 || width == 0 || height == 0 ||
+        uint64_t(width) * height > (uint64_t(1) << 31) || (color == 3 && depth != 8))
+        throw OpenError("png: unsupported");
+    if (band < 0 || band >= channels) throw ReadError("png: band");
+    const size_t bpp = size_t(channels) * size_t(depth / 8), stride = size_t(width) * bpp;
+    std::vector<uint8_t> raw = inflate_zlib(idat.data(), idat.size(), (stride + 1) * height);
+    if (raw.size() < (stride + 1) * height) throw ReadError("png: short image data");
+    std::vector<uint8_t> prev(stride, 0), cur(stride);
+    Raster r;
+    r.width = int(width);
+    r.height = int(height);
+    r.bands = channels;
+    r.values.resize(size_t(width) * height);
+    for (uint32_t y = 0; y < height; ++y) {
+        const uint8_t filter = raw[y * (stride + 1)];
+        const uint8_t* src = raw.data() + y * (stride + 1) + 1;
+        for (size_t i = 0; i < stride; ++i) {
+            const int a = i >= bpp ? cur[i - bpp] : 0, up = prev[i];
+            const int c = i >= bpp ? prev[i - bpp] : 0;
+            int pred = 0;
+            switch (filter) {
+            case 0: pred = 0; break;
+            case 1: pred = a; break;
+            case 2: pred = up; break;
+            case 3: pred = (a + up) / 2; break;
+            case 4: {
+                const int p = a + up - c, pa = std::abs(p - a), pb = std::abs(p - up),
+                          pc = std::abs(p - c);
+                pred = pa <= pb && pa <= pc ? a : pb <= pc ? up : c;
+                break;
+            }
+            default: throw ReadError("png: filter");
+            }
+            cur[i] = uint8_t(src[i] + pred);
+        }
+        for (uint32_t x = 0; x < width; ++x) {
+            const size_t o = size_t(x) * bpp + size_t(band) * size_t(depth / 8);
+            const float v = depth == 8 ? float(cur[o]) : float(uint32_t(cur[o]) << 8 | cur[o + 1]);
+            r.values[size_t(y) * width + x] = v;
+        }
+        std::swap(prev, cur);
+    }
+    return r;
+}
+
 Raster read_raster(const std::filesystem::path& path, int band = 0)
 {
     std::ifstream in(path, std::ios::binary);
@@ -706,6 +788,8 @@ Raster read_raster(const std::filesystem::path& path, int band = 0)
     if (bytes.size() >= 8 && ((bytes[0] == 'I' && bytes[1] == 'I') ||
                               (bytes[0] == 'M' && bytes[1] == 'M')))
         return read_tiff(bytes, band);
+    static const uint8_t kPng[8] = {0x89, 'P', 'N', 'G', 0x0D, 0x0A, 0x1A, 0x0A};
+    if (bytes.size() >= 8 && std::memcmp(bytes.data(), kPng, 8) == 0) return read_png(bytes, band);
     const std::string text(bytes.begin(), bytes.end());
     if (looks_ascii_grid(text)) {
         if (band != 0) throw ReadError("ascii grid: one band");

@@ -341,3 +341,30 @@ def test_texture_errors_match_reference(tmp_path, ref_project, case):  # noqa: F
         facetcu.Project(path)
     assert str(ours.value) == str(theirs.value)
     assert "reflectance variance texture" in str(ours.value).lower()
+
+
+@pytest.mark.parametrize("kind", ["gray8", "gray16", "rgb8", "rgba8", "graya8", "palette"])
+def test_png_rasters(tmp_path, kind):
+    z = _pattern(19, 27)
+    if kind == "gray16":
+        img = (z * 200).astype(np.uint16)
+    elif kind in ("rgb8", "rgba8", "graya8"):
+        c = {"rgb8": 3, "rgba8": 4, "graya8": 2}[kind]
+        img = np.stack([np.roll(z, k, axis=1) for k in range(c)], axis=2).astype(np.uint8)
+    else:
+        img = z.astype(np.uint8)
+    path = tiff_writer.write_png(str(tmp_path / "t.png"), img, depth=16 if kind == "gray16" else 8,
+                                 palette=kind == "palette")
+    got, _ = facetcu.dem_height_field(path)  # band 1
+    want = (img if img.ndim == 2 else img[:, :, 0]).astype(np.float32)
+    assert np.array_equal(got, want)
+
+
+def test_png_texture_equals_ascii_texture(tmp_path):
+    os.makedirs(tmp_path / "tex")
+    z = _pattern()
+    _write_asc(str(tmp_path / "tex" / "a.asc"), z)
+    tiff_writer.write_png(str(tmp_path / "tex" / "a.png"), z.astype(np.uint8))
+    a = facetcu.Project(_texture_project(tmp_path, "tex/a.asc")).texture_factors
+    b = facetcu.Project(_texture_project(tmp_path, "tex/a.png")).texture_factors
+    assert np.any(a != 1.0) and np.array_equal(a.view(np.uint32), b.view(np.uint32))

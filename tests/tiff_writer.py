@@ -1,11 +1,13 @@
-"""A small GeoTIFF writer for the DEM reader's tests (test infrastructure).
+"""Small GeoTIFF and PNG writers for the raster reader's tests (test
+infrastructure).
 
 Writes one image in any of the layouts facetcu_dem_height_field reads:
 classic or BigTIFF, little or big endian, strips or tiles, chunky or planar
 samples, no compression, LZW (TIFF 6.0 section 13, with the early code-width
 change and a clear code when the table fills), deflate (Python's zlib) or
 PackBits, horizontal (2) or floating-point (3) prediction, and the
-GDAL_NODATA tag.  Independent of the library's decoders."""
+GDAL_NODATA tag; and non-interlaced PNG with every row filter.  Independent
+of the library's decoders."""
 import struct
 import zlib
 
@@ -168,4 +170,53 @@ def write(path, image, *, order="<", tile=None, rows_per_strip=None, compression
             struct.pack(order + "I", 0)
     with open(path, "wb") as f:
         f.write(header + bytes(data) + bytes(extra) + ifd_bytes)
+    return path
+
+
+def write_png(path, image, *, depth=8, palette=False):
+    """A non-interlaced PNG of (H, W) or (H, W, C) samples (C = 1 gray,
+    2 gray + alpha, 3 RGB, 4 RGBA; palette=True: (H, W) indices into a gray
+    palette), every row filtered with one of the five filter types in turn."""
+    img = image if image.ndim == 3 else image[:, :, None]
+    H, W, C = img.shape
+    color = 3 if palette else {1: 0, 2: 4, 3: 2, 4: 6}[C]
+    bps = depth // 8
+    data = img.astype(">u2" if depth == 16 else np.uint8).reshape(H, W * C).view(np.uint8) \
+        if depth == 16 else img.astype(np.uint8).reshape(H, W * C)
+    data = np.asarray(data, np.uint8).reshape(H, W * C * bps)
+    bpp = C * bps
+    rows = []
+    prev = np.zeros(W * C * bps, np.int32)
+    for y in range(H):
+        cur = data[y].astype(np.int32)
+        ft = y % 5
+        left = np.concatenate([np.zeros(bpp, np.int32), cur[:-bpp]])
+        ul = np.concatenate([np.zeros(bpp, np.int32), prev[:-bpp]])
+        if ft == 0:
+            out = cur
+        elif ft == 1:
+            out = cur - left
+        elif ft == 2:
+            out = cur - prev
+        elif ft == 3:
+            out = cur - (left + prev) // 2
+        else:
+            p = left + prev - ul
+            pa, pb, pc = np.abs(p - left), np.abs(p - prev), np.abs(p - ul)
+            pred = np.where((pa <= pb) & (pa <= pc), left, np.where(pb <= pc, prev, ul))
+            out = cur - pred
+        rows.append(bytes([ft]) + (out & 255).astype(np.uint8).tobytes())
+        prev = cur
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xffffffff)
+
+    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", W, H, depth, color, 0, 0, 0))
+    if palette:
+        png += chunk(b"PLTE", bytes(np.repeat(np.arange(256, dtype=np.uint8), 3)))
+    raw = zlib.compress(b"".join(rows))
+    png += chunk(b"IDAT", raw[:len(raw) // 2]) + chunk(b"IDAT", raw[len(raw) // 2:])
+    png += chunk(b"IEND", b"")
+    with open(path, "wb") as f:
+        f.write(png)
     return path

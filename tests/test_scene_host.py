@@ -110,8 +110,14 @@ def test_cli_argument_handling():
     assert os.path.exists(CLI), "build() makes streamsim_gb300/facetcu"
     r = _cli("eUnknown")
     assert r.returncode == 2 and r.stderr.startswith("Usage: facetcu [eVoxelEB|eFacetEB|eFacetRT")
-    r = _cli("eFacetEB", "x.json")
-    assert r.returncode == 3
+    r = _cli("eVoxelEB", "x.json")  # not built on this backend
+    assert r.returncode == 3 and "Failed to create engine resources for eVoxelEB" in r.stderr
+    # eFacetEB runs the FacetEB entry (python -m streamsim_gb300.faceteb)
+    r = _cli("eFacetEB", "/nonexistent/Input.xml")
+    assert r.returncode == 1 and r.stderr.startswith("faceteb: ")
+    r = subprocess.run([CLI, "eFacetEB", "x.xml"], capture_output=True, text=True, timeout=60,
+                       env=dict(os.environ, FACETCU_PYTHON="/nonexistent/python"))
+    assert r.returncode == 3 and "cannot start /nonexistent/python" in r.stderr
     r = _cli("eFacetRT")
     assert r.returncode == 1 and "facetrt: FacetRT requires project.json" in r.stderr
     r = _cli("eFacetRT", "/nonexistent/project.json")  # read through its XML view

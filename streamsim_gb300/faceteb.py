@@ -261,45 +261,47 @@ class Run:
                 run_index.value["products"] += ["photovoltaic_summary.csv",
                                                 ".facet_steps/components.bin"]
         energy_kwh = 0.0
-        for node in range(start_node, end_node):
-            row = meteorology[node]
-            if temperature is None:
-                seed = np.float32(np.clip(np.float32(row["air_temperature"]) +
-                                          np.float32(273.15), 220.0, 340.0))
-                temperature = np.full(S, seed, np.float32)
-            zenith, azimuth = sun_for(row)
-            fields, res, lit = self.node(row, zenith, azimuth, temperature)
-            temperature = fields["temperature"]
-            token = time_token(row["julian_time"])
-            all_converged = all_converged and bool(res["converged"])
-            results.append(dict(res, node=node, token=token))
-            if steps:
-                cols = [fields["temperature"], fields["radiosity"], fields["shortwave_radiosity"],
-                        fields["longwave_radiosity"], fields["net_radiation"],
-                        fields["sensible_heat"], fields["latent_heat"], fields["storage_heat"],
-                        lit]
-                if self.wavelengths:
-                    cols += list(fields["band_output"])
-                rec = np.stack([np.asarray(c, np.float32) for c in cols], 1)
-                rec.astype("<f4").tofile(os.path.join(steps, f"energy_T={token}.bin"))
-            if output_dir and area is not None:
-                energy_kwh, pv_area = self._write_pv(output_dir, node, token, fields, area, pv,
-                                                     summary, energy_kwh)
-                for kind, on in (("radiation", process[0]), ("energy", process[1]),
-                                 ("photovoltaic", pv_area > 0)):
-                    if on:
-                        self._write_process(output_dir, kind, node, row, token, zenith, azimuth,
-                                            fields, res, F, run_index)
-            if run_index is not None:
-                run_index.node(node, token, row["julian_time"], res,
-                               self.params.temperature_tolerance, self.params.coupling_iterations)
-            if progress:
-                progress(f"FACET_CONVERGENCE\t{node}\t{int(res['converged'])}\t"
-                         f"{res['coupling_iterations']}\t{res['max_temperature_delta']}\t"
-                         f"{res['max_energy_residual']}\t{res['max_energy_residual_equivalent']}")
-            last = (fields, res, lit, token)
-        if summary is not None:
-            summary.close()
+        try:
+            for node in range(start_node, end_node):
+                row = meteorology[node]
+                if temperature is None:
+                    seed = np.float32(np.clip(np.float32(row["air_temperature"]) +
+                                              np.float32(273.15), 220.0, 340.0))
+                    temperature = np.full(S, seed, np.float32)
+                zenith, azimuth = sun_for(row)
+                fields, res, lit = self.node(row, zenith, azimuth, temperature)
+                temperature = fields["temperature"]
+                token = time_token(row["julian_time"])
+                all_converged = all_converged and bool(res["converged"])
+                results.append(dict(res, node=node, token=token))
+                if steps:
+                    cols = [fields["temperature"], fields["radiosity"], fields["shortwave_radiosity"],
+                            fields["longwave_radiosity"], fields["net_radiation"],
+                            fields["sensible_heat"], fields["latent_heat"], fields["storage_heat"],
+                            lit]
+                    if self.wavelengths:
+                        cols += list(fields["band_output"])
+                    rec = np.stack([np.asarray(c, np.float32) for c in cols], 1)
+                    rec.astype("<f4").tofile(os.path.join(steps, f"energy_T={token}.bin"))
+                if output_dir and area is not None:
+                    energy_kwh, pv_area = self._write_pv(output_dir, node, token, fields, area, pv,
+                                                         summary, energy_kwh)
+                    for kind, on in (("radiation", process[0]), ("energy", process[1]),
+                                     ("photovoltaic", pv_area > 0)):
+                        if on:
+                            self._write_process(output_dir, kind, node, row, token, zenith, azimuth,
+                                                fields, res, F, run_index)
+                if run_index is not None:
+                    run_index.node(node, token, row["julian_time"], res,
+                                   self.params.temperature_tolerance, self.params.coupling_iterations)
+                if progress:
+                    progress(f"FACET_CONVERGENCE\t{node}\t{int(res['converged'])}\t"
+                             f"{res['coupling_iterations']}\t{res['max_temperature_delta']}\t"
+                             f"{res['max_energy_residual']}\t{res['max_energy_residual_equivalent']}")
+                last = (fields, res, lit, token)
+        finally:
+            if summary is not None:
+                summary.close()
         if output_dir and last is not None:
             self._write_result(os.path.join(output_dir, "faceteb.json"), last, all_converged,
                                vertices, graph)

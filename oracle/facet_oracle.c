@@ -851,7 +851,7 @@ static void side_frame(vec3 N, vec3 *T, vec3 *Bt)
 }
 
 /* Moller-Trumbore; returns t or -1. */
-static float ray_triangle(vec3 o, vec3 d, vec3 a, vec3 e1, vec3 e2)
+static inline __attribute__((always_inline)) float ray_triangle(vec3 o, vec3 d, vec3 a, vec3 e1, vec3 e2)
 {
     const vec3 p = vcross(d, e2);
     const float det = vdot(e1, p);
@@ -929,6 +929,36 @@ static int cmp_u32(const void *a, const void *b)
     return x < y ? -1 : (x > y ? 1 : 0);
 }
 
+/* One side's row from its ray hits (side ids of the sides seen, sky rays
+ * excluded): run counts, the top_k largest counts kept (ties: lower side
+ * first), written sorted by side.  Returns the row length; adds the kept
+ * ray count to *kept and the dropped ones to *dropped. */
+static uint32_t hemi_row(uint32_t *hits, uint32_t nh, hitcount *h, uint32_t top_k,
+                         uint32_t *neighbors, uint32_t *counts, uint32_t *kept,
+                         uint64_t *dropped)
+{
+    qsort(hits, nh, sizeof(uint32_t), cmp_u32);
+    uint32_t nu = 0;
+    for (uint32_t i = 0; i < nh;) {
+        uint32_t j = i;
+        while (j < nh && hits[j] == hits[i]) ++j;
+        h[nu].side = hits[i];
+        h[nu].count = j - i;
+        ++nu;
+        i = j;
+    }
+    qsort(h, nu, sizeof(hitcount), cmp_hit_rank);
+    const uint32_t keep = nu < top_k ? nu : top_k;
+    for (uint32_t i = keep; i < nu; ++i) *dropped += h[i].count;
+    for (uint32_t i = 0; i < keep; ++i) *kept += h[i].count;
+    qsort(h, keep, sizeof(hitcount), cmp_hit_side);
+    for (uint32_t i = 0; i < keep; ++i) {
+        neighbors[i] = h[i].side;
+        counts[i] = h[i].count;
+    }
+    return keep;
+}
+
 int orc_hemisphere_graph(const orc_vertex *V, uint32_t F, const float *uv,
                          const float *dirs, uint32_t rays, uint32_t sets, uint32_t top_k,
                          orc_graph *g, uint64_t *dropped_out)
@@ -975,27 +1005,10 @@ int orc_hemisphere_graph_periodic(const orc_vertex *V, uint32_t F, const float *
             const vec3 ng = v3(V[hit * 3U].normal[0], V[hit * 3U].normal[1], V[hit * 3U].normal[2]);
             hits[nh++] = 2U * (uint32_t)hit + (vdot(ng, d) < 0.0f ? 0U : 1U);
         }
-        qsort(hits, nh, sizeof(uint32_t), cmp_u32);
-        uint32_t nu = 0;
-        for (uint32_t i = 0; i < nh;) {
-            uint32_t j = i;
-            while (j < nh && hits[j] == hits[i]) ++j;
-            h[nu].side = hits[i];
-            h[nu].count = j - i;
-            ++nu;
-            i = j;
-        }
-        qsort(h, nu, sizeof(hitcount), cmp_hit_rank);
-        const uint32_t keep = nu < top_k ? nu : top_k;
         uint32_t kept = 0;
-        for (uint32_t i = keep; i < nu; ++i) dropped += h[i].count;
-        for (uint32_t i = 0; i < keep; ++i) kept += h[i].count;
-        qsort(h, keep, sizeof(hitcount), cmp_hit_side);
-        for (uint32_t i = 0; i < keep; ++i) {
-            g->neighbors[nnz] = h[i].side;
-            g->counts[nnz] = h[i].count;
-            ++nnz;
-        }
+        const uint32_t keep = hemi_row(hits, nh, h, top_k, g->neighbors + nnz, g->counts + nnz,
+                                       &kept, &dropped);
+        nnz += keep;
         g->row_offsets[s + 1] = (uint32_t)nnz;
         g->sky_counts[s] = sky;
         g->denominators[s] = kept + sky;
@@ -1036,4 +1049,536 @@ int orc_hemisphere_sunlit_periodic(const orc_vertex *V, uint32_t F, const float 
         fraction[s] = (float)lit / (float)samples;
     }
     return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The same hemisphere graph and sun visibility with a BVH over the facets   */
+/* and host threads, for scenes too large for the brute force (the          */
+/* 200k-facet forest: 2 x 10^8 rays).  The rays, the intersection test and  */
+/* the tie rules are those above; the BVH only skips facets whose box the   */
+/* ray misses.  Boxes are widened by 1e-4 of the scene extent, far more     */
+/* than the rounding of a hit point, so no facet whose intersection test    */
+/* would report a hit is skipped: the nearest hit (smallest t, then lowest  */
+/* facet) equals the brute force's, and so does every row.                  */
+/* ------------------------------------------------------------------------ */
+#include <pthread.h>
+#include <stdatomic.h>
+#include <unistd.h>
+
+typedef struct {
+    float lo[3], hi[3];
+    int32_t left, right; /* internal: child indices; leaf: left = -1 - first, right = count */
+} bvh_node;
+
+typedef struct {
+    bvh_node *nodes;
+    uint32_t count;
+    uint32_t *facet;  /* facet of each leaf slot */
+    float *tri;       /* per leaf slot: a, b - a, c - a (9 floats) */
+} bvh_tree;
+
+typedef struct {
+    const orc_vertex *V;
+    float *box;      /* per facet lo[3], hi[3] (widened) */
+    float *centroid; /* per facet */
+    uint32_t *idx;
+    bvh_node *nodes;
+    uint32_t count;
+} bvh_build;
+
+static void idx_swap(uint32_t *a, uint32_t i, uint32_t j) { uint32_t t = a[i]; a[i] = a[j]; a[j] = t; }
+
+static float box_area(const float lo[3], const float hi[3])
+{
+    const float x = hi[0] - lo[0], y = hi[1] - lo[1], z = hi[2] - lo[2];
+    return x * y + y * z + z * x;
+}
+
+/* Top-down build with the surface-area heuristic over 16 centroid bins per
+ * axis; ranges of at most 2 facets are leaves.  A range whose centroids
+ * coincide, and every range below depth 64, is halved by index, so the tree
+ * is at most 64 + 32 levels deep (kBvhMaxDepth). */
+enum { kBvhMaxDepth = 96 };
+static int32_t bvh_build_node(bvh_build *b, uint32_t lo, uint32_t hi, uint32_t depth)
+{
+    enum { kBins = 16, kLeaf = 2 };
+    const int32_t me = (int32_t)b->count++;
+    bvh_node *n = &b->nodes[me];
+    float clo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, chi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int a = 0; a < 3; ++a) { n->lo[a] = FLT_MAX; n->hi[a] = -FLT_MAX; }
+    for (uint32_t i = lo; i < hi; ++i) {
+        const uint32_t f = b->idx[i];
+        for (int a = 0; a < 3; ++a) {
+            if (b->box[6 * f + a] < n->lo[a]) n->lo[a] = b->box[6 * f + a];
+            if (b->box[6 * f + 3 + a] > n->hi[a]) n->hi[a] = b->box[6 * f + 3 + a];
+            if (b->centroid[3 * f + a] < clo[a]) clo[a] = b->centroid[3 * f + a];
+            if (b->centroid[3 * f + a] > chi[a]) chi[a] = b->centroid[3 * f + a];
+        }
+    }
+    const uint32_t cnt = hi - lo;
+    if (cnt <= kLeaf) {
+        n->left = -1 - (int32_t)lo;
+        n->right = (int32_t)cnt;
+        return me;
+    }
+    int best_axis = -1;
+    int best_split = 0;
+    float best_cost = FLT_MAX;
+    for (int a = 0; a < 3 && depth < 64U; ++a) {
+        const float ext = chi[a] - clo[a];
+        if (!(ext > 0.0f)) continue;
+        uint32_t bc[kBins] = {0};
+        float blo[kBins][3], bhi[kBins][3];
+        for (int k = 0; k < kBins; ++k)
+            for (int c = 0; c < 3; ++c) { blo[k][c] = FLT_MAX; bhi[k][c] = -FLT_MAX; }
+        const float scale = (float)kBins / ext;
+        for (uint32_t i = lo; i < hi; ++i) {
+            const uint32_t f = b->idx[i];
+            int k = (int)((b->centroid[3 * f + a] - clo[a]) * scale);
+            if (k >= kBins) k = kBins - 1;
+            if (k < 0) k = 0;
+            ++bc[k];
+            for (int c = 0; c < 3; ++c) {
+                if (b->box[6 * f + c] < blo[k][c]) blo[k][c] = b->box[6 * f + c];
+                if (b->box[6 * f + 3 + c] > bhi[k][c]) bhi[k][c] = b->box[6 * f + 3 + c];
+            }
+        }
+        /* sweep: cost of splitting after bin k */
+        float rarea[kBins];
+        uint32_t rcnt[kBins];
+        float rl[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rh[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        uint32_t rc = 0;
+        for (int k = kBins - 1; k > 0; --k) {
+            rc += bc[k];
+            for (int c = 0; c < 3; ++c) {
+                if (blo[k][c] < rl[c]) rl[c] = blo[k][c];
+                if (bhi[k][c] > rh[c]) rh[c] = bhi[k][c];
+            }
+            rcnt[k] = rc;
+            rarea[k] = rc ? box_area(rl, rh) : 0.0f;
+        }
+        float ll[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lh[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        uint32_t lc = 0;
+        for (int k = 0; k < kBins - 1; ++k) {
+            lc += bc[k];
+            for (int c = 0; c < 3; ++c) {
+                if (blo[k][c] < ll[c]) ll[c] = blo[k][c];
+                if (bhi[k][c] > lh[c]) lh[c] = bhi[k][c];
+            }
+            if (lc == 0 || rcnt[k + 1] == 0) continue;
+            const float cost = (float)lc * box_area(ll, lh) + (float)rcnt[k + 1] * rarea[k + 1];
+            if (cost < best_cost) { best_cost = cost; best_axis = a; best_split = k; }
+        }
+    }
+    uint32_t mid;
+    if (best_axis < 0) {
+        mid = lo + cnt / 2U; /* coincident centroids: halve by index */
+    } else {
+        const int a = best_axis;
+        const float scale = (float)kBins / (chi[a] - clo[a]);
+        uint32_t i = lo, j = hi;
+        while (i < j) {
+            const uint32_t f = b->idx[i];
+            int k = (int)((b->centroid[3 * f + a] - clo[a]) * scale);
+            if (k >= kBins) k = kBins - 1;
+            if (k < 0) k = 0;
+            if (k <= best_split) ++i; else idx_swap(b->idx, i, --j);
+        }
+        mid = i;
+        if (mid == lo || mid == hi) mid = lo + cnt / 2U;
+    }
+    const int32_t l = bvh_build_node(b, lo, mid, depth + 1U);
+    const int32_t r = bvh_build_node(b, mid, hi, depth + 1U);
+    b->nodes[me].left = l;
+    b->nodes[me].right = r;
+    return me;
+}
+
+static int bvh_make(const orc_vertex *V, uint32_t F, bvh_tree *t)
+{
+    memset(t, 0, sizeof(*t));
+    if (F == 0U) return 0;
+    float slo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, shi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t k = 0; k < 3U * F; ++k)
+        for (int a = 0; a < 3; ++a) {
+            if (V[k].position[a] < slo[a]) slo[a] = V[k].position[a];
+            if (V[k].position[a] > shi[a]) shi[a] = V[k].position[a];
+        }
+    float extent = 0.0f;
+    for (int a = 0; a < 3; ++a)
+        if (shi[a] - slo[a] > extent) extent = shi[a] - slo[a];
+    const float margin = 1.0e-4f * extent + 1.0e-6f;
+    bvh_build b;
+    b.V = V;
+    b.box = (float *)malloc((size_t)F * 6 * sizeof(float));
+    b.centroid = (float *)malloc((size_t)F * 3 * sizeof(float));
+    b.idx = (uint32_t *)malloc((size_t)F * sizeof(uint32_t));
+    b.nodes = (bvh_node *)malloc((size_t)2 * F * sizeof(bvh_node));
+    b.count = 0;
+    if (!b.box || !b.centroid || !b.idx || !b.nodes) {
+        free(b.box); free(b.centroid); free(b.idx); free(b.nodes);
+        return -1;
+    }
+    for (uint32_t f = 0; f < F; ++f) {
+        for (int a = 0; a < 3; ++a) {
+            const float p0 = V[3 * f].position[a], p1 = V[3 * f + 1].position[a],
+                        p2 = V[3 * f + 2].position[a];
+            const float lo = fminf(p0, fminf(p1, p2)), hi = fmaxf(p0, fmaxf(p1, p2));
+            b.box[6 * f + a] = lo - margin;
+            b.box[6 * f + 3 + a] = hi + margin;
+            b.centroid[3 * f + a] = 0.5f * (lo + hi);
+        }
+        b.idx[f] = f;
+    }
+    bvh_build_node(&b, 0, F, 0U);
+    t->nodes = b.nodes;
+    t->count = b.count;
+    t->facet = b.idx;
+    t->tri = (float *)malloc((size_t)F * 9 * sizeof(float));
+    free(b.box);
+    free(b.centroid);
+    if (!t->tri) return -1;
+    for (uint32_t k = 0; k < F; ++k) {
+        const uint32_t g = t->facet[k];
+        const vec3 a = vpos(&V[g * 3U]);
+        const vec3 e1 = vsub(vpos(&V[g * 3U + 1U]), a);
+        const vec3 e2 = vsub(vpos(&V[g * 3U + 2U]), a);
+        for (int i = 0; i < 3; ++i) {
+            t->tri[9 * k + i] = a.v[i];
+            t->tri[9 * k + 3 + i] = e1.v[i];
+            t->tri[9 * k + 6 + i] = e2.v[i];
+        }
+    }
+    return 0;
+}
+
+static void bvh_free(bvh_tree *t)
+{
+    free(t->nodes);
+    free(t->facet);
+    free(t->tri);
+    memset(t, 0, sizeof(*t));
+}
+
+/* 1/d with |d| raised to at least 1e-30: the slab distances below stay
+ * finite (no infinity, no NaN), so plain comparisons order them. */
+static float safe_inv(float d)
+{
+    return 1.0f / (fabsf(d) < 1.0e-30f ? copysignf(1.0e-30f, d) : d);
+}
+
+static inline __attribute__((always_inline)) void leaf_test(const bvh_tree *t,
+                                                             const bvh_node *n, vec3 o, vec3 d,
+                                                             uint32_t skip, float *bt, int *best)
+{
+    const uint32_t first = (uint32_t)(-1 - n->left);
+    for (uint32_t k = first; k < first + (uint32_t)n->right; ++k) {
+        const uint32_t g = t->facet[k];
+        if (g == skip) continue;
+        const float *p = t->tri + 9 * (size_t)k;
+        const float th = ray_triangle(o, d, v3(p[0], p[1], p[2]), v3(p[3], p[4], p[5]),
+                                      v3(p[6], p[7], p[8]));
+        if (th > 0.0f && (th < *bt || (th == *bt && (int)g < *best))) {
+            *bt = th;
+            *best = (int)g;
+        }
+    }
+}
+
+static inline __attribute__((always_inline)) int slab_near(const bvh_node *n, vec3 o,
+                                                           const float inv[3], float tmax,
+                                                           float *tnear)
+{
+    float tn = 0.0f, tf = FLT_MAX;
+    for (int a = 0; a < 3; ++a) {
+        const float t0 = (n->lo[a] - o.v[a]) * inv[a], t1 = (n->hi[a] - o.v[a]) * inv[a];
+        const float near = t0 < t1 ? t0 : t1, far = t0 < t1 ? t1 : t0;
+        tn = near > tn ? near : tn;
+        tf = far < tf ? far : tf;
+    }
+    *tnear = tn;
+    return tn <= tf && tn <= tmax;
+}
+
+/* Nearest hit (any = 0) or any hit (any = 1) over the tree, improving on
+ * (*bt, *best) with the brute force's update rule.  Both children are
+ * tested at their parent; the nearer one is entered first and the other
+ * stacked, and a stacked node is tested again (against the then nearest
+ * hit) when it is taken off the stack. */
+static void bvh_trace(const bvh_tree *t, vec3 o, vec3 d, uint32_t skip, int any, float *bt,
+                      int *best)
+{
+    if (t->count == 0U) return;
+    const float inv[3] = {safe_inv(d.v[0]), safe_inv(d.v[1]), safe_inv(d.v[2])};
+    float tn;
+    const bvh_node *n = &t->nodes[0];
+    if (!slab_near(n, o, inv, *bt, &tn)) return;
+    int32_t stack[kBvhMaxDepth + 2];
+    int sp = 0;
+    for (;;) {
+        if (n->left < 0) {
+            leaf_test(t, n, o, d, skip, bt, best);
+            if (any && *best >= 0) return;
+        } else {
+            const bvh_node *l = &t->nodes[n->left], *r = &t->nodes[n->right];
+            float tl, tr;
+            const int hl = slab_near(l, o, inv, *bt, &tl);
+            const int hr = slab_near(r, o, inv, *bt, &tr);
+            if (hl && hr) {
+                if (tl <= tr) { stack[sp++] = n->right; n = l; }
+                else { stack[sp++] = n->left; n = r; }
+                continue;
+            }
+            if (hl) { n = l; continue; }
+            if (hr) { n = r; continue; }
+        }
+        /* next stacked node still in reach */
+        for (;;) {
+            if (sp == 0) return;
+            n = &t->nodes[stack[--sp]];
+            if (slab_near(n, o, inv, *bt, &tn)) break;
+        }
+    }
+}
+
+static int bvh_hit_tiles(const bvh_tree *t, uint32_t skip, vec3 o, vec3 d, int any,
+                         uint32_t periodic_count, float size_x, float size_z)
+{
+    int best = -1;
+    float bt = FLT_MAX;
+    const uint32_t tiles = (periodic_count < 20U ? periodic_count : 20U) + 1U;
+    for (uint32_t tile = 0; tile < tiles; ++tile) {
+        int tx, tz;
+        periodic_tile(tile, &tx, &tz);
+        const float ox = (float)tx * size_x, oz = (float)tz * size_z;
+        const vec3 ot = v3(o.v[0] - ox, o.v[1], o.v[2] - oz);
+        bvh_trace(t, ot, d, tile == 0U ? skip : 0xFFFFFFFFu, any, &bt, &best);
+        if (any && best >= 0) break;
+    }
+    return best;
+}
+
+typedef struct {
+    const orc_vertex *V;
+    const bvh_tree *tree;
+    const float *uv, *dirs;
+    uint32_t F, rays, sets, top_k, periodic_count;
+    float size_x, size_z;
+    orc_direction sun;
+    float *fraction;           /* sunlit mode */
+    uint32_t *row_len, *denom, *sky;
+    uint32_t **chunk_nb, **chunk_cnt;
+    uint64_t *chunk_dropped;
+    atomic_uint next;
+    uint32_t chunks;
+    int failed;
+} hemi_job;
+
+enum { kHemiChunk = 64 };
+
+static void *hemi_graph_worker(void *arg)
+{
+    hemi_job *j = (hemi_job *)arg;
+    const uint32_t S = 2U * j->F;
+    const uint32_t cap = j->top_k < j->rays ? j->top_k : j->rays;
+    uint32_t *hits = (uint32_t *)malloc((size_t)j->rays * sizeof(uint32_t) + 4);
+    hitcount *h = (hitcount *)malloc((size_t)j->rays * sizeof(hitcount) + 8);
+    uint32_t *nb = (uint32_t *)malloc((size_t)kHemiChunk * cap * sizeof(uint32_t) + 4);
+    uint32_t *cn = (uint32_t *)malloc((size_t)kHemiChunk * cap * sizeof(uint32_t) + 4);
+    if (!hits || !h || !nb || !cn) { j->failed = 1; goto done; }
+    for (;;) {
+        const uint32_t c = atomic_fetch_add(&j->next, 1U);
+        if (c >= j->chunks) break;
+        const uint32_t s0 = c * kHemiChunk, s1 = s0 + kHemiChunk < S ? s0 + kHemiChunk : S;
+        uint64_t used = 0, dropped = 0;
+        for (uint32_t s = s0; s < s1; ++s) {
+            const uint32_t f = s >> 1U;
+            const uint32_t set = s % j->sets;
+            const orc_vertex *V = j->V;
+            vec3 N = v3(V[f * 3U].normal[0], V[f * 3U].normal[1], V[f * 3U].normal[2]);
+            if (s & 1U) N = v3(-N.v[0], -N.v[1], -N.v[2]);
+            vec3 T, Bt;
+            side_frame(N, &T, &Bt);
+            uint32_t nh = 0, skyc = 0;
+            for (uint32_t r = 0; r < j->rays; ++r) {
+                const size_t k = (size_t)set * j->rays + r;
+                const vec3 o = sample_origin(V, f, j->uv[2 * k], j->uv[2 * k + 1]);
+                const float dx = j->dirs[3 * k], dy = j->dirs[3 * k + 1], dz = j->dirs[3 * k + 2];
+                const vec3 d = v3(T.v[0] * dx + Bt.v[0] * dy + N.v[0] * dz,
+                                  T.v[1] * dx + Bt.v[1] * dy + N.v[1] * dz,
+                                  T.v[2] * dx + Bt.v[2] * dy + N.v[2] * dz);
+                const int hit = bvh_hit_tiles(j->tree, f, o, d, 0, j->periodic_count, j->size_x,
+                                              j->size_z);
+                if (hit < 0) { ++skyc; continue; }
+                const vec3 ng = v3(V[hit * 3U].normal[0], V[hit * 3U].normal[1],
+                                   V[hit * 3U].normal[2]);
+                hits[nh++] = 2U * (uint32_t)hit + (vdot(ng, d) < 0.0f ? 0U : 1U);
+            }
+            uint32_t kept = 0;
+            const uint32_t keep = hemi_row(hits, nh, h, j->top_k, nb + used, cn + used, &kept,
+                                           &dropped);
+            used += keep;
+            j->row_len[s] = keep;
+            j->sky[s] = skyc;
+            j->denom[s] = kept + skyc;
+        }
+        j->chunk_nb[c] = (uint32_t *)malloc(used * sizeof(uint32_t) + 4);
+        j->chunk_cnt[c] = (uint32_t *)malloc(used * sizeof(uint32_t) + 4);
+        if (!j->chunk_nb[c] || !j->chunk_cnt[c]) { j->failed = 1; break; }
+        memcpy(j->chunk_nb[c], nb, used * sizeof(uint32_t));
+        memcpy(j->chunk_cnt[c], cn, used * sizeof(uint32_t));
+        j->chunk_dropped[c] = dropped;
+    }
+done:
+    free(hits);
+    free(h);
+    free(nb);
+    free(cn);
+    return NULL;
+}
+
+static void *hemi_sunlit_worker(void *arg)
+{
+    hemi_job *j = (hemi_job *)arg;
+    const uint32_t S = 2U * j->F;
+    const vec3 d = v3(j->sun.x, j->sun.y, j->sun.z);
+    for (;;) {
+        const uint32_t c = atomic_fetch_add(&j->next, 1U);
+        if (c >= j->chunks) break;
+        const uint32_t s0 = c * kHemiChunk, s1 = s0 + kHemiChunk < S ? s0 + kHemiChunk : S;
+        for (uint32_t s = s0; s < s1; ++s) {
+            const uint32_t f = s >> 1U;
+            const uint32_t set = s % j->sets;
+            const orc_vertex *V = j->V;
+            vec3 N = v3(V[f * 3U].normal[0], V[f * 3U].normal[1], V[f * 3U].normal[2]);
+            if (s & 1U) N = v3(-N.v[0], -N.v[1], -N.v[2]);
+            if (!(vdot(N, d) > 0.0f)) { j->fraction[s] = 0.0f; continue; }
+            uint32_t lit = 0;
+            for (uint32_t r = 0; r < j->rays; ++r) {
+                const size_t k = (size_t)set * j->rays + r;
+                const vec3 o = sample_origin(V, f, j->uv[2 * k], j->uv[2 * k + 1]);
+                if (bvh_hit_tiles(j->tree, f, o, d, 1, j->periodic_count, j->size_x,
+                                  j->size_z) < 0)
+                    ++lit;
+            }
+            j->fraction[s] = (float)lit / (float)j->rays;
+        }
+    }
+    return NULL;
+}
+
+static int run_workers(hemi_job *j, uint32_t threads, void *(*fn)(void *))
+{
+    if (threads == 0U) {
+        const long n = sysconf(_SC_NPROCESSORS_ONLN);
+        threads = n > 0 ? (uint32_t)n : 1U;
+    }
+    if (threads > 256U) threads = 256U;
+    pthread_t tid[256];
+    uint32_t started = 0;
+    for (uint32_t i = 1; i < threads; ++i)
+        if (pthread_create(&tid[started], NULL, fn, j) == 0) ++started;
+    fn(j);
+    for (uint32_t i = 0; i < started; ++i) pthread_join(tid[i], NULL);
+    return j->failed ? -1 : 0;
+}
+
+int orc_hemisphere_graph_bvh(const orc_vertex *V, uint32_t F, const float *uv,
+                             const float *dirs, uint32_t rays, uint32_t sets, uint32_t top_k,
+                             uint32_t periodic_count, float size_x, float size_z,
+                             uint32_t threads, orc_graph *g, uint64_t *dropped_out)
+{
+    memset(g, 0, sizeof(*g));
+    const uint32_t S = 2U * F;
+    bvh_tree tree;
+    if (bvh_make(V, F, &tree) != 0) return -1;
+    hemi_job j;
+    memset(&j, 0, sizeof(j));
+    j.V = V;
+    j.tree = &tree;
+    j.uv = uv;
+    j.dirs = dirs;
+    j.F = F;
+    j.rays = rays;
+    j.sets = sets;
+    j.top_k = top_k;
+    j.periodic_count = periodic_count;
+    j.size_x = size_x;
+    j.size_z = size_z;
+    j.chunks = (S + kHemiChunk - 1U) / kHemiChunk;
+    atomic_init(&j.next, 0U);
+    g->surface_count = S;
+    g->row_offsets = (uint32_t *)calloc((size_t)S + 1, sizeof(uint32_t));
+    g->denominators = (uint32_t *)calloc((size_t)S + 1, sizeof(uint32_t));
+    g->sky_counts = (uint32_t *)calloc((size_t)S + 1, sizeof(uint32_t));
+    j.row_len = (uint32_t *)calloc((size_t)S + 1, sizeof(uint32_t));
+    j.chunk_nb = (uint32_t **)calloc((size_t)j.chunks + 1, sizeof(uint32_t *));
+    j.chunk_cnt = (uint32_t **)calloc((size_t)j.chunks + 1, sizeof(uint32_t *));
+    j.chunk_dropped = (uint64_t *)calloc((size_t)j.chunks + 1, sizeof(uint64_t));
+    j.denom = g->denominators;
+    j.sky = g->sky_counts;
+    int rc = -1;
+    if (g->row_offsets && g->denominators && g->sky_counts && j.row_len && j.chunk_nb &&
+        j.chunk_cnt && j.chunk_dropped)
+        rc = run_workers(&j, threads, hemi_graph_worker);
+    uint64_t nnz = 0, dropped = 0;
+    if (rc == 0) {
+        for (uint32_t s = 0; s < S; ++s) {
+            nnz += j.row_len[s];
+            g->row_offsets[s + 1] = (uint32_t)nnz;
+        }
+        g->neighbors = (uint32_t *)malloc(nnz * sizeof(uint32_t) + 4);
+        g->counts = (uint32_t *)malloc(nnz * sizeof(uint32_t) + 4);
+        if (!g->neighbors || !g->counts) rc = -1;
+    }
+    if (rc == 0) {
+        for (uint32_t c = 0; c < j.chunks; ++c) {
+            const uint32_t s0 = c * kHemiChunk, s1 = s0 + kHemiChunk < S ? s0 + kHemiChunk : S;
+            const uint32_t b = g->row_offsets[s0], n = g->row_offsets[s1] - b;
+            memcpy(g->neighbors + b, j.chunk_nb[c], (size_t)n * sizeof(uint32_t));
+            memcpy(g->counts + b, j.chunk_cnt[c], (size_t)n * sizeof(uint32_t));
+            dropped += j.chunk_dropped[c];
+        }
+        g->nnz = nnz;
+        g->max_closure_error = closure_error(g);
+        if (dropped_out) *dropped_out = dropped;
+    }
+    for (uint32_t c = 0; j.chunk_nb && c < j.chunks; ++c) {
+        free(j.chunk_nb[c]);
+        free(j.chunk_cnt[c]);
+    }
+    free(j.chunk_nb);
+    free(j.chunk_cnt);
+    free(j.chunk_dropped);
+    free(j.row_len);
+    bvh_free(&tree);
+    if (rc != 0) orc_free_graph(g);
+    return rc;
+}
+
+int orc_hemisphere_sunlit_bvh(const orc_vertex *V, uint32_t F, const float *uv,
+                              uint32_t samples, uint32_t sets, orc_direction sun,
+                              uint32_t periodic_count, float size_x, float size_z,
+                              uint32_t threads, float *fraction)
+{
+    bvh_tree tree;
+    if (bvh_make(V, F, &tree) != 0) return -1;
+    hemi_job j;
+    memset(&j, 0, sizeof(j));
+    j.V = V;
+    j.tree = &tree;
+    j.uv = uv;
+    j.F = F;
+    j.rays = samples;
+    j.sets = sets;
+    j.periodic_count = periodic_count;
+    j.size_x = size_x;
+    j.size_z = size_z;
+    j.sun = sun;
+    j.fraction = fraction;
+    j.chunks = (2U * F + kHemiChunk - 1U) / kHemiChunk;
+    atomic_init(&j.next, 0U);
+    const int rc = run_workers(&j, threads, hemi_sunlit_worker);
+    bvh_free(&tree);
+    return rc;
 }

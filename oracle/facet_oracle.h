@@ -131,6 +131,20 @@ int orc_hemisphere_sunlit_periodic(const orc_vertex *vertices, uint32_t facet_co
                                    orc_direction sun, uint32_t periodic_count, float size_x,
                                    float size_z, float *fraction);
 
+/* The same two results with a BVH over the facets and `threads` host
+ * threads (0: every online core), for scenes where the brute force is too
+ * slow.  Identical output: the BVH only skips facets whose widened box the
+ * ray misses.  Return 0, or -1 when memory ran out. */
+int orc_hemisphere_graph_bvh(const orc_vertex *vertices, uint32_t facet_count,
+                             const float *sample_uv, const float *sample_dir,
+                             uint32_t rays_per_side, uint32_t sets, uint32_t top_k,
+                             uint32_t periodic_count, float size_x, float size_z,
+                             uint32_t threads, orc_graph *out, uint64_t *dropped);
+int orc_hemisphere_sunlit_bvh(const orc_vertex *vertices, uint32_t facet_count,
+                              const float *sample_uv, uint32_t samples, uint32_t sets,
+                              orc_direction sun, uint32_t periodic_count, float size_x,
+                              float size_z, uint32_t threads, float *fraction);
+
 void orc_free(void *p);
 
 #ifdef __cplusplus

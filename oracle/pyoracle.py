@@ -27,7 +27,7 @@ def build_oracle(force=False):
             os.path.getmtime(ORACLE_LIB) < max(os.path.getmtime(ORACLE_SRC),
                                                  os.path.getmtime(os.path.join(HERE, "facet_oracle.h"))):
         subprocess.run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared",
-                        ORACLE_SRC, "-o", ORACLE_LIB, "-lm"], check=True)
+                        "-pthread", ORACLE_SRC, "-o", ORACLE_LIB, "-lm"], check=True)
     return ORACLE_LIB
 
 
@@ -164,6 +164,12 @@ class Oracle:
         L.orc_hemisphere_sunlit_periodic.argtypes = [
             C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, OrcDirection, C.c_uint32,
             C.c_float, C.c_float, C.c_void_p]
+        L.orc_hemisphere_graph_bvh.argtypes = [
+            C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+            C.c_uint32, C.c_float, C.c_float, C.c_uint32, C.c_void_p, C.c_void_p]
+        L.orc_hemisphere_sunlit_bvh.argtypes = [
+            C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, OrcDirection, C.c_uint32,
+            C.c_float, C.c_float, C.c_uint32, C.c_void_p]
         L.orc_free.argtypes = [C.c_void_p]
 
     # -- geometry helpers -------------------------------------------------
@@ -302,6 +308,38 @@ class Oracle:
         self.lib.orc_hemisphere_sunlit_periodic(
             vertices.ctypes.data, len(vertices) // 3, sample_uv.ctypes.data, samples, sets, d,
             int(periodic[0]), C.c_float(periodic[1]), C.c_float(periodic[2]), out.ctypes.data)
+        return out
+
+
+    def hemisphere_graph_bvh(self, vertices, sample_uv, sample_dir, rays, sets, top_k,
+                             periodic=(0, 1.0, 1.0), threads=0):
+        """hemisphere_graph with a BVH and host threads (same output)."""
+        vertices = np.ascontiguousarray(vertices, np.float32)
+        sample_uv = np.ascontiguousarray(sample_uv, np.float32)
+        sample_dir = np.ascontiguousarray(sample_dir, np.float32)
+        g = OrcGraph()
+        dropped = C.c_uint64()
+        rc = self.lib.orc_hemisphere_graph_bvh(
+            vertices.ctypes.data, len(vertices) // 3, sample_uv.ctypes.data,
+            sample_dir.ctypes.data, rays, sets, top_k, int(periodic[0]), C.c_float(periodic[1]),
+            C.c_float(periodic[2]), threads, C.byref(g), C.byref(dropped))
+        if rc != 0:
+            raise MemoryError("orc_hemisphere_graph_bvh: out of host memory")
+        return self._take_graph(g), dropped.value
+
+    def hemisphere_sunlit_bvh(self, vertices, sample_uv, samples, sets, sun,
+                              periodic=(0, 1.0, 1.0), threads=0):
+        """hemisphere_sunlit with a BVH and host threads (same output)."""
+        vertices = np.ascontiguousarray(vertices, np.float32)
+        sample_uv = np.ascontiguousarray(sample_uv, np.float32)
+        out = np.zeros(2 * (len(vertices) // 3), np.float32)
+        d = OrcDirection(*[float(x) for x in sun])
+        rc = self.lib.orc_hemisphere_sunlit_bvh(
+            vertices.ctypes.data, len(vertices) // 3, sample_uv.ctypes.data, samples, sets, d,
+            int(periodic[0]), C.c_float(periodic[1]), C.c_float(periodic[2]), threads,
+            out.ctypes.data)
+        if rc != 0:
+            raise MemoryError("orc_hemisphere_sunlit_bvh: out of host memory")
         return out
 
 

@@ -168,3 +168,27 @@ def test_hemisphere_periodic_tiles_bit_exact(oracle, neighbours):
     assert np.array_equal(lit, oracle.hemisphere_sunlit(sc.vertices, suv, 32, 8, sun,
                                                         periodic=(neighbours, 10.0, 10.0)))
     m.close()
+
+
+def test_hemisphere_graph_config2_scale_bit_exact(oracle):
+    """The bench's view factors at full size: the 60-tree forest (203,840
+    facets, 407,680 sides), 512 rays per side, top-K 256, against the
+    oracle's BVH caster on the host cores (the brute force's rules; its
+    equality with the brute force is a CPU test).  Every row, count,
+    denominator and sky count must match, as must the 256-sample sun pass."""
+    sc = scenes.config2(seed=0)
+    uv, dirs = scenes.hemisphere_samples(512, 32, seed=7)
+    m = facetcu.FacetrtCuda()
+    m.initialize(1024, 1024, 1024)
+    m.setGeometry(sc.vertices)
+    diag, dropped = m.buildHemisphereGraph(uv, dirs, 512, 256, 32)
+    suv, _ = scenes.hemisphere_samples(256, 32, seed=8)
+    sun = scenes.sun_direction(30.0, 135.0)
+    lit = m.hemisphereSunlit(sun, suv, 256, 32)
+    gpu_graph = m.graph()
+    m.close()
+    g, dropped_o = oracle.hemisphere_graph_bvh(sc.vertices, uv, dirs, 512, 32, 256)
+    assert g.nnz == diag["directed_edge_count"]
+    assert graphs_equal(gpu_graph, g) is None
+    assert dropped == dropped_o
+    assert np.array_equal(lit, oracle.hemisphere_sunlit_bvh(sc.vertices, suv, 256, 32, sun))

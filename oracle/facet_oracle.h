@@ -145,6 +145,14 @@ int orc_hemisphere_sunlit_bvh(const orc_vertex *vertices, uint32_t facet_count,
                               orc_direction sun, uint32_t periodic_count, float size_x,
                               float size_z, uint32_t threads, float *fraction);
 
+/* Per-ray hits of the listed sides (side seen or 0xFFFFFFFF, distance or
+ * -1), by brute force (use_bvh = 0) or the BVH (use_bvh = 1): the
+ * diagnostic behind a graph difference. */
+int orc_hemisphere_rays(const orc_vertex *vertices, uint32_t facet_count,
+                        const float *sample_uv, const float *sample_dir, uint32_t rays_per_side,
+                        uint32_t sets, const uint32_t *sides, uint32_t side_count, int use_bvh,
+                        uint32_t *hit_side, float *hit_t);
+
 void orc_free(void *p);
 
 #ifdef __cplusplus

@@ -170,6 +170,9 @@ class Oracle:
         L.orc_hemisphere_sunlit_bvh.argtypes = [
             C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, OrcDirection, C.c_uint32,
             C.c_float, C.c_float, C.c_uint32, C.c_void_p]
+        L.orc_hemisphere_rays.argtypes = [
+            C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+            C.c_uint32, C.c_int, C.c_void_p, C.c_void_p]
         L.orc_free.argtypes = [C.c_void_p]
 
     # -- geometry helpers -------------------------------------------------
@@ -341,6 +344,22 @@ class Oracle:
         if rc != 0:
             raise MemoryError("orc_hemisphere_sunlit_bvh: out of host memory")
         return out
+
+
+    def hemisphere_rays(self, vertices, sample_uv, sample_dir, rays, sets, sides, bvh=True):
+        """Per-ray (side seen or 0xFFFFFFFF, distance) of the listed sides."""
+        vertices = np.ascontiguousarray(vertices, np.float32)
+        sides = np.ascontiguousarray(sides, np.uint32)
+        hs = np.zeros((len(sides), rays), np.uint32)
+        ht = np.zeros((len(sides), rays), np.float32)
+        rc = self.lib.orc_hemisphere_rays(
+            vertices.ctypes.data, len(vertices) // 3,
+            np.ascontiguousarray(sample_uv, np.float32).ctypes.data,
+            np.ascontiguousarray(sample_dir, np.float32).ctypes.data, rays, sets,
+            sides.ctypes.data, len(sides), int(bool(bvh)), hs.ctypes.data, ht.ctypes.data)
+        if rc != 0:
+            raise MemoryError("orc_hemisphere_rays: out of host memory")
+        return hs, ht
 
 
 class Reference:

@@ -601,6 +601,9 @@ void ensure_bvh(facetcu_context* ctx)
         ctx->bvh.scene_min[a] = ctx->bmin[a];
         ctx->bvh.scene_max[a] = ctx->bmax[a];
     }
+    const uint32_t periodic = std::min(ctx->config.periodic_neighbor_count, 20u);
+    ctx->bvh.hit_margin = hit_margin(ctx->bmin, ctx->bmax, periodic, ctx->config.periodic_size_x,
+                                     ctx->config.periodic_size_z);
     lbvh_build(ctx->vertices.as<facetcu_vertex>(), ctx->facets, ctx->bvh, ctx->ws, ctx->stream);
     ctx->bvh_ready = true;
 }

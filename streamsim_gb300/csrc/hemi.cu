@@ -3,9 +3,14 @@
 // For every oriented side s (facet f = s / 2, normal N = +/- n_f) a warp
 // casts `rays` rays: ray j of sample set (s mod sets) starts at
 // a + u (b - a) + v (c - a) and leaves along T dx + Bt dy + N dz in the side's
-// frame (T = normalize(helper x N), Bt = N x T).  The nearest hit (smallest
-// t, ties to the lower facet index, the origin facet skipped) gives the side
-// seen: 2g if the ray meets g's normal side, 2g + 1 otherwise.  The warp
+// frame (T = normalize(helper x N), Bt = N x T).  A facet is hit when the
+// Moller-Trumbore test accepts the ray at t > 0 and o + t d lies in the
+// facet's box widened by the hit margin (the test's distance to a long thin
+// facet met at a grazing angle can lie millimetres outside the facet; the
+// BVH's leaf boxes are widened by twice the margin, so the traversal never
+// culls a hit).  The nearest hit (smallest t, ties to the lower facet
+// index, the origin facet skipped) gives the side seen: 2g if the ray
+// meets g's normal side, 2g + 1 otherwise.  The warp
 // sorts the 32 x (rays/32) hit ids in shared memory, counts runs, keeps the
 // top_k most-hit sides (ties: lower side index) and writes the row sorted
 // by neighbour with denominator = kept + sky rays.  With periodic tiles the
@@ -69,9 +74,26 @@ __device__ __forceinline__ bool slab(const float4& lo, const float4& hi, Vec o, 
     return tn <= tf && tn <= tmax;
 }
 
+// 1/d with |d| raised to at least 1e-30: the slab distances stay finite (no
+// infinity, so no 0 * inf), and fminf/fmaxf order them.
 __device__ __forceinline__ float safe_inv(float d)
 {
-    return 1.0f / (d == 0.0f ? copysignf(1.0e-30f, d) : d);
+    return 1.0f / (fabsf(d) < 1.0e-30f ? copysignf(1.0e-30f, d) : d);
+}
+
+// o + t d inside facet g's box widened by m (the hit rule's second half).
+__device__ __forceinline__ bool in_hit_box(const facetcu_vertex* __restrict__ V, uint32_t g,
+                                           Vec o, Vec d, float t, float m)
+{
+    const float p[3] = {o.x + t * d.x, o.y + t * d.y, o.z + t * d.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float v0 = V[3 * g].position[a], v1 = V[3 * g + 1].position[a],
+                    v2 = V[3 * g + 2].position[a];
+        const float lo = fminf(v0, fminf(v1, v2)) - m, hi = fmaxf(v0, fmaxf(v1, v2)) + m;
+        if (!(p[a] >= lo && p[a] <= hi)) return false;
+    }
+    return true;
 }
 
 struct Hit {
@@ -85,7 +107,8 @@ struct Hit {
 // overflowed.
 template <bool kAny>
 __device__ bool trace(const float4* __restrict__ nodes, const float4* __restrict__ tri,
-                      uint32_t leaves, Vec o, Vec d, uint32_t skip, Hit& best)
+                      const facetcu_vertex* __restrict__ V, float m, uint32_t leaves, Vec o,
+                      Vec d, uint32_t skip, Hit& best)
 {
     const Vec inv = {safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
     auto test_leaf = [&](uint32_t k) {
@@ -95,7 +118,8 @@ __device__ bool trace(const float4* __restrict__ nodes, const float4* __restrict
         const float4 E1 = __ldg(tri + 3 * size_t(k) + 1);
         const float4 E2 = __ldg(tri + 3 * size_t(k) + 2);
         const float t = ray_triangle(o, d, {A.x, A.y, A.z}, {E1.x, E1.y, E1.z}, {E2.x, E2.y, E2.z});
-        if (t > 0.0f && (t < best.t || (t == best.t && g < best.facet))) {
+        if (t > 0.0f && (t < best.t || (t == best.t && g < best.facet)) &&
+            in_hit_box(V, g, o, d, t, m)) {
             best.t = t;
             best.facet = g;
         }
@@ -156,16 +180,16 @@ struct Tiles {
 
 template <bool kAny>
 __device__ bool trace_tiles(const float4* __restrict__ nodes, const float4* __restrict__ tri,
-                            uint32_t leaves, const Tiles& tiles, Vec o, Vec d, uint32_t skip,
-                            Hit& best)
+                            const facetcu_vertex* __restrict__ V, float m, uint32_t leaves,
+                            const Tiles& tiles, Vec o, Vec d, uint32_t skip, Hit& best)
 {
     best.t = FLT_MAX;
     best.facet = kSky;
-    if (tiles.n <= 1) return trace<kAny>(nodes, tri, leaves, o, d, skip, best);  // no copies
+    if (tiles.n <= 1) return trace<kAny>(nodes, tri, V, m, leaves, o, d, skip, best);  // no copies
     bool ok = true;
     for (uint32_t t = 0; t < tiles.n; ++t) {
         const Vec ot = {o.x - tiles.x[t], o.y, o.z - tiles.z[t]};
-        ok &= trace<kAny>(nodes, tri, leaves, ot, d, t == 0 ? skip : kSky, best);
+        ok &= trace<kAny>(nodes, tri, V, m, leaves, ot, d, t == 0 ? skip : kSky, best);
         if (kAny && best.facet != kSky) break;
     }
     return ok;
@@ -233,8 +257,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_hemi_rows(
     const facetcu_vertex* __restrict__ V, const float4* __restrict__ nodes,
     const float4* __restrict__ tri, uint32_t leaves, uint32_t surfaces, const float* __restrict__ uv,
     const float* __restrict__ dirs, uint32_t rays, uint32_t sets, uint32_t npow, uint32_t top_k,
-    Tiles tiles, uint32_t* tmp_edges, uint32_t* nnz, uint32_t* denom, uint32_t* skyc,
-    unsigned long long* dropped, uint32_t* error)
+    Tiles tiles, float hit_m, uint32_t* tmp_edges, uint32_t* nnz, uint32_t* denom,
+    uint32_t* skyc, unsigned long long* dropped, uint32_t* error)
 {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -256,7 +280,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_hemi_rows(
                                fr.T.y * dx + fr.B.y * dy + fr.N.y * dz,
                                fr.T.z * dx + fr.B.z * dy + fr.N.z * dz};
                 Hit h;
-                if (!trace_tiles<false>(nodes, tri, leaves, tiles, o, d, f, h))
+                if (!trace_tiles<false>(nodes, tri, V, hit_m, leaves, tiles, o, d, f, h))
                     atomicExch(error, 1u);
                 if (h.facet != kSky) {
                     const Vec ng = {V[3 * h.facet].normal[0], V[3 * h.facet].normal[1],
@@ -372,7 +396,8 @@ __global__ void __launch_bounds__(256) k_hemi_sunlit(const facetcu_vertex* __res
                                                      const float4* __restrict__ tri, uint32_t leaves,
                                                      uint32_t surfaces, const float* __restrict__ uv,
                                                      uint32_t samples, uint32_t sets, Vec sun,
-                                                     Tiles tiles, float* fraction, uint32_t* error)
+                                                     Tiles tiles, float hit_m, float* fraction,
+                                                     uint32_t* error)
 {
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -389,7 +414,8 @@ __global__ void __launch_bounds__(256) k_hemi_sunlit(const facetcu_vertex* __res
         const size_t k = size_t(set) * samples + j;
         const Vec o = sample_origin(V, f, uv[2 * k], uv[2 * k + 1]);
         Hit h;
-        if (!trace_tiles<true>(nodes, tri, leaves, tiles, o, sun, f, h)) atomicExch(error, 1u);
+        if (!trace_tiles<true>(nodes, tri, V, hit_m, leaves, tiles, o, sun, f, h))
+            atomicExch(error, 1u);
         if (h.facet == kSky) ++lit;
     }
     for (int o = 16; o > 0; o >>= 1) lit += __shfl_xor_sync(0xffffffffu, lit, o);
@@ -440,7 +466,8 @@ void hemisphere_graph(const facetcu_vertex* d_vertices, uint32_t facets, const L
     const unsigned grid_blocks = unsigned(std::max(1, sms * std::max(per_sm, 1)));
     k_hemi_rows<<<grid_blocks, kWarps * 32, smem, s>>>(
         d_vertices, bvh.nodes.as<float4>(), bvh.tri.as<float4>(), bvh.leaves, S, d_uv, d_dir, rays,
-        sets, npow, top_k, make_tiles(periodic), tmp_edges, rows, den, sky, d_dropped, d_error);
+        sets, npow, top_k, make_tiles(periodic), bvh.hit_margin, tmp_edges, rows, den, sky,
+        d_dropped, d_error);
     FCU_LAUNCH("k_hemi_rows");
     // rows currently holds per-side nnz; scan in place into offsets
     exclusive_scan_u32(rows, rows, S, d_total, ws, s);
@@ -471,7 +498,8 @@ void hemisphere_sunlit(const facetcu_vertex* d_vertices, uint32_t facets, const 
     k_hemi_sunlit<<<(S * 32 + 255) / 256, 256, 0, s>>>(d_vertices, bvh.nodes.as<float4>(),
                                                        bvh.tri.as<float4>(), bvh.leaves, S, d_uv,
                                                        samples, sets, {sun.x, sun.y, sun.z},
-                                                       make_tiles(periodic), d_fraction, d_error);
+                                                       make_tiles(periodic), bvh.hit_margin,
+                                                       d_fraction, d_error);
     FCU_LAUNCH("k_hemi_sunlit");
     uint32_t e = 0;
     FCU_CHECK(cudaMemcpyAsync(&e, d_error, 4, cudaMemcpyDeviceToHost, s));

@@ -221,7 +221,16 @@ struct Lbvh {
     DeviceBuffer parent;     // build scratch
     DeviceBuffer flags;      // build scratch
     float scene_min[3], scene_max[3];
+    // A hit counts only when o + t d lies in the facet's box widened by
+    // hit_margin (set before lbvh_build); leaf boxes are widened by twice it.
+    float hit_margin = 0.0f;
 };
+// The hemisphere caster's hit margin from the vertex bounds and the periodic
+// copies traced: 1e-5 of (reach + extent) + 1e-7, where reach is the largest
+// coordinate magnitude (plus two periods with copies) and extent the largest
+// side of the bounds.
+float hit_margin(const float lo[3], const float hi[3], uint32_t periodic_count, float size_x,
+                 float size_z);
 void lbvh_build(const facetcu_vertex* d_vertices, uint32_t facets, Lbvh& bvh, Workspace& ws,
                 cudaStream_t s);
 // Facet ids sorted by the 30-bit Morton code of their centroids in [lo, hi].

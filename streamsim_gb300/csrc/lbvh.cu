@@ -6,10 +6,12 @@
 // Each internal node stores both children's boxes (64 bytes), so a traversal
 // step is one node fetch and two slab tests; each leaf stores the triangle
 // as (a, e1 = b - a, e2 = c - a) and the facet index (48 bytes), the exact
-// operands of the intersection test.  Leaf boxes are widened by a margin of
-// 1e-5 of the scene extent so that no float slab test rejects a triangle the
-// intersection test would accept: nearest hits are the same as a brute-force
-// search over all facets.
+// operands of the intersection test.  A hit counts only when its point lies
+// in the facet's box widened by the hit margin (hemi.cu), and leaf boxes are
+// widened by twice that margin, so no float slab test rejects a hit: nearest
+// hits are the same as a brute-force search over all facets.
+#include <cmath>
+
 #include "internal.h"
 
 namespace facetcu {
@@ -108,6 +110,20 @@ __device__ __forceinline__ void child_box(int c, const float* leaf_box_sorted, c
     }
 }
 
+// A child's box as the refit must read it: an internal child's box was
+// written by another thread, possibly on another SM, so it is read from L2
+// (ld.global.cg); a plain load may return a line this SM's L1 cached before
+// the write.
+__device__ __forceinline__ void child_box_l2(int c, const float* leaf_box_sorted,
+                                             const float* int_box, float lo[3], float hi[3])
+{
+    const float* b = c < 0 ? leaf_box_sorted + 6 * size_t(~c) : int_box + 6 * size_t(c);
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = __ldcg(b + a);
+        hi[a] = __ldcg(b + 3 + a);
+    }
+}
+
 __global__ void k_refit(int n, const int* child, const int* parent_int, const int* parent_leaf,
                         const float* leaf_box_sorted, float* int_box, unsigned* flags)
 {
@@ -119,11 +135,11 @@ __global__ void k_refit(int n, const int* child, const int* parent_int, const in
         if (atomicAdd(&flags[node], 1u) == 0u) return;  // the sibling finishes this node
         __threadfence();
         float l0[3], h0[3], l1[3], h1[3];
-        child_box(child[2 * node], leaf_box_sorted, int_box, l0, h0);
-        child_box(child[2 * node + 1], leaf_box_sorted, int_box, l1, h1);
+        child_box_l2(child[2 * node], leaf_box_sorted, int_box, l0, h0);
+        child_box_l2(child[2 * node + 1], leaf_box_sorted, int_box, l1, h1);
         for (int a = 0; a < 3; ++a) {
-            int_box[6 * size_t(node) + a] = fminf(l0[a], l1[a]);
-            int_box[6 * size_t(node) + 3 + a] = fmaxf(h0[a], h1[a]);
+            __stcg(int_box + 6 * size_t(node) + a, fminf(l0[a], l1[a]));
+            __stcg(int_box + 6 * size_t(node) + 3 + a, fmaxf(h0[a], h1[a]));
         }
         node = parent_int[node];
     }
@@ -166,19 +182,29 @@ inline unsigned grid(size_t n, unsigned b) { return unsigned((n + b - 1) / b); }
 
 }  // namespace
 
+float hit_margin(const float lo[3], const float hi[3], uint32_t periodic_count, float size_x,
+                 float size_z)
+{
+    float extent = 0.0f, reach = 0.0f;
+    for (int a = 0; a < 3; ++a) {
+        extent = std::max(extent, hi[a] - lo[a]);
+        reach = std::max(reach, std::max(std::fabs(lo[a]), std::fabs(hi[a])));
+    }
+    if (periodic_count > 0u) reach = reach + 2.0f * std::max(std::fabs(size_x), std::fabs(size_z));
+    return 1.0e-5f * (reach + extent) + 1.0e-7f;
+}
+
 void lbvh_build(const facetcu_vertex* d_vertices, uint32_t n, Lbvh& bvh, Workspace& ws,
                 cudaStream_t s)
 {
     if (n == 0) throw Error(FACETCU_LOGIC_ERROR, "setGeometry() must be called before building the BVH");
     bvh.leaves = n;
     Bounds sb;
-    float extent = 0.0f;
     for (int a = 0; a < 3; ++a) {
         sb.lo[a] = bvh.scene_min[a];
         sb.hi[a] = bvh.scene_max[a];
-        extent = std::max(extent, sb.hi[a] - sb.lo[a]);
     }
-    const float margin = 1.0e-5f * extent + 1.0e-7f;
+    const float margin = 2.0f * bvh.hit_margin;
     DeviceBuffer keys_a, keys_b, ids_a, ids_b, leaf_box, int_box, child, parent_int, parent_leaf;
     uint64_t* ka = static_cast<uint64_t*>(keys_a.reserve(size_t(n) * 8));
     uint64_t* kb = static_cast<uint64_t*>(keys_b.reserve(size_t(n) * 8));

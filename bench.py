@@ -496,7 +496,8 @@ def run_gpu(args, rank, world, local):
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     achieved = rt["sweep_bytes"] / max(rt["sweep_seconds"], 1e-12) / 1e9
     panel = min(128, 1 << (B - 1).bit_length())
-    kname = (f"k_step_i8<{panel}>" if prec == fc.PRECISION_MIXED else f"k_sweep_wide<{panel}>")
+    kname = (f"k_sweep_wide<{panel}>" if prec != fc.PRECISION_MIXED else
+             "k_step_i8_async<64>" if panel == 64 else f"k_step_i8<{panel}>")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": None, "kernel": kname,
                 "launches_timed": rt["timed_sweeps"],

@@ -221,9 +221,14 @@ typedef struct {
                                    |dB_s| / max(|B_s|, 1e-6 max|B|) <= tolerance */
     uint32_t panel_width;       /* RHS columns per resident panel (power of two, <= 128;
                                    <= 32 in FP64); 0 = the widest that fits */
-    uint32_t flags;             /* FACETCU_BATCH_TIME_SWEEPS: time every sweep kernel */
+    uint32_t flags;             /* FACETCU_BATCH_TIME_SWEEPS: time every sweep kernel;
+                                   FACETCU_BATCH_LEGACY_STEP: run the 64-column int8
+                                   steps on the register-gather kernel instead of the
+                                   asynchronous-copy pipeline (same results; for
+                                   comparisons) */
 } facetcu_batch_config;
 #define FACETCU_BATCH_TIME_SWEEPS 1u
+#define FACETCU_BATCH_LEGACY_STEP 2u
 typedef struct {
     uint32_t iterations;        /* sweeps of the slowest panel */
     uint32_t residual_corrections;

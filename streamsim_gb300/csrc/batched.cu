@@ -87,6 +87,7 @@ struct GraphView {
     float* scene_sig;                  // two slots of [scenes][kMaxP] int8 step scales
     float* scene_cheb;                 // [scenes][4 kMaxP] Chebyshev state (weights at 2 kMaxP)
     uint32_t* scene_done;              // [scenes]
+    uint32_t legacy_step;              // 1: 64-column int8 steps on the register-gather kernel
 };
 
 __device__ __forceinline__ void edge_at(const GraphView& g, uint32_t e, uint32_t& nb, float& c)
@@ -956,6 +957,435 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
     publish_cols<NC>(md, mb, mr, col0, true, P, stats);
 }
 
+// ---- the 64-column int8 step as an asynchronous-copy pipeline --------------
+// The same step as k_step_i8<64, false> (bit-identical X, R, Q and
+// statistics: the gathered sums are exact int32), restructured so that each
+// warp keeps neighbour rows in flight while it computes.  A warp walks the
+// rows of its facets as a sequence of 64-edge stages (a side's last stage
+// may be partial; an empty side is one empty stage) with three cursors:
+//   request — kLookahead stages ahead of issue: writes the stage's
+//             descriptor (side, last-stage flag, denominator, edges) to
+//             shared memory and loads its 32 packed edge words into a
+//             register queue;
+//   issue   — kAsyncStages - 1 stages ahead of consume: 16-byte cp.async
+//             copies (LDGSTS, L2 only) of the stage's neighbour rows into a
+//             ring of kAsyncStages stages in shared memory, and its counts
+//             (low bytes packed per dp4a word);
+//   consume — 4 x 4 byte transposes and dp4a from shared memory; at a
+//             side's last stage the reduction and (odd side) the facet's
+//             epilogue.
+// In-flight rows cost shared memory instead of registers, and the edge
+// words are requested before their rows are, so neither the dp4a work nor
+// the epilogue's loads stop the gather.  Facets come in chunks of kChunk
+// from the step's counter; the request cursor takes its next chunk (and
+// that chunk's row offsets and denominators) one chunk ahead, and asks L2
+// for the next chunk's edge words and each chunk's per-cell planes
+// (cp.async.bulk.prefetch) as it enters a chunk.  Measured on GB300 with a
+// 64-byte row gather of the bench's size: tile::gather4 TMA loads peak at
+// 0.52 ms (the TMA unit's rate for 256-byte requests), cp.async.bulk per
+// row at 1.1 ms, LDGSTS rings at 0.30 ms, plain register loads at 0.31 ms.
+#ifndef FCU_STEP_ASYNC
+#define FCU_STEP_ASYNC 1
+#endif
+// Measured on the config-2 forest (C2 graph, 64 columns; the register-gather
+// kernel 0.619 ms): 64-edge stages, 2 ring stages, 1 stage of lookahead
+// 0.527 ms; 2 of lookahead 0.608; 3 ring stages on 2 CTAs per SM 0.636;
+// 32-edge stages with 4 ring stages 0.622 (their per-stage bookkeeping
+// doubled the instructions per edge).
+#ifndef FCU_ASYNC_STAGES
+#define FCU_ASYNC_STAGES 2
+#endif
+#ifndef FCU_ASYNC_LOOKAHEAD
+#define FCU_ASYNC_LOOKAHEAD 1
+#endif
+#ifndef FCU_ASYNC_BLOCKS
+#define FCU_ASYNC_BLOCKS 3
+#endif
+#ifndef FCU_ASYNC_EDGES
+#define FCU_ASYNC_EDGES 64
+#endif
+constexpr int kAsyncStages = FCU_ASYNC_STAGES;
+constexpr int kLookahead = FCU_ASYNC_LOOKAHEAD;
+constexpr int kStageEdges = FCU_ASYNC_EDGES;  // 32 or 64 edges per stage
+
+constexpr int pow2_at_least(int n) { return n <= 1 ? 1 : 2 * pow2_at_least((n + 1) / 2); }
+
+template <int P>
+struct AsyncLayout {
+    static constexpr int kStageBytes = kStageEdges * P;  // int8 rows of one stage
+    // a stage's counts: the low bytes packed for the dp4a (one byte per
+    // edge), a flag word (any count above 255) and the full counts for that
+    // case
+    static constexpr int kCountBytes = kStageEdges + 16 + kStageEdges * 4;
+    // descriptor slots (a power of two, at least stages + lookahead)
+    static constexpr int kDesc = pow2_at_least(kAsyncStages + kLookahead);
+    // per warp: the row ring, the counts of each ring stage, the descriptors
+    static constexpr int kWarpBytes = kAsyncStages * (kStageBytes + kCountBytes) + kDesc * 16;
+    static constexpr int kBlockBytes = kWarps * kWarpBytes;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return uint32_t(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit()
+{
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N> __device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// Asynchronous prefetch of `bytes` (a multiple of 16, 16-byte aligned) into L2.
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+template <int P>
+__global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async(
+    GraphView g, PanelParams pp, const int8_t* __restrict__ Qin, int8_t* __restrict__ Qout,
+    float* __restrict__ X, float* __restrict__ R, const float* __restrict__ sig_in,
+    const float* __restrict__ sig_out, uint32_t* stats, uint32_t* counter, const uint32_t* done)
+{
+    static_assert(P == 64, "the pipelined step covers 64-column panels");
+    using Lay = AsyncLayout<P>;
+    constexpr int L = P / 16, G = 32 / L, NC = P / 32;
+    constexpr int SE = kStageEdges;
+    constexpr int WPL = SE / 32;       // packed edge words per lane per stage
+    constexpr int EPL = SE / G;        // edges per lane per stage
+    constexpr int CPL = SE * L / 32;   // 16-byte copies per lane per stage
+    constexpr int NST = kAsyncStages, D = kLookahead, NQ = Lay::kDesc;
+    constexpr uint32_t C = kChunk;
+    constexpr unsigned kAll = 0xffffffffu;
+    static_assert(SE == 32 || SE == 64, "32 or 64 edges per stage");
+    static_assert(EPL % 4 == 0 && G == 8, "4 x 4 transpose blocks, 8 edge groups");
+    static_assert(NST >= 2 && D >= 1, "pipeline depths");
+    extern __shared__ __align__(16) unsigned char dyn[];
+    if (*done) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int grp = lane / L, sub = lane % L;
+    unsigned char* ring = dyn + size_t(warp) * Lay::kWarpBytes;
+    unsigned char* cnt_s = ring + NST * Lay::kStageBytes;  // [NST][kCountBytes]
+    uint4* meta = reinterpret_cast<uint4*>(cnt_s + NST * Lay::kCountBytes);
+
+    const int col0 = sub * 16 + i8_offset<G>(grp);
+    float si[NC], inv_so[NC], md[NC], mb[NC], mr[NC], om[NC], fl[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        si[k] = sig_in[col0 + k];
+        const float so = sig_out[col0 + k];
+        inv_so[k] = so > 0.0f ? 1.0f / so : 0.0f;
+        om[k] = pp.omega ? pp.omega[col0 + k] : 1.0f;
+        fl[k] = kSideFloor * pp.colmax[col0 + k];
+        md[k] = 0.0f;
+        mb[k] = 0.0f;
+        mr[k] = 0.0f;
+    }
+
+    // ---- request cursor: chunks, sides, stages ---------------------------
+    const uint32_t F = g.facets;
+    const uint32_t chunks = (F + C - 1) / C;
+    const uint32_t nb_mask = (1u << g.nb_bits) - 1u;
+    const size_t word_bytes = (size_t(__ldg(g.rows + 2u * F)) * 4u) & ~size_t(15);  // prefetch bound
+    // a chunk: its id, and in lane i its side i's row start (lanes 0..sides)
+    // and denominator (lanes 0..sides-1)
+    auto grab = [&](uint32_t& id, uint32_t& rw, uint32_t& dn) {
+        id = next_chunk(counter, lane);
+        rw = 0u;
+        dn = 0u;
+        if (id < chunks) {
+            const uint32_t s0 = 2u * id * C, ns = 2u * (min(F, (id + 1u) * C) - id * C);
+            if (uint32_t(lane) <= ns) rw = __ldg(g.rows + s0 + lane);
+            if (uint32_t(lane) < ns) dn = __ldg(g.denom + s0 + lane);
+        }
+    };
+    uint32_t r_id, r_rw, r_dn, n_id, n_rw, n_dn;
+    grab(r_id, r_rw, r_dn);
+    grab(n_id, n_rw, n_dn);
+    bool rdone = r_id >= chunks;
+    uint32_t r_side = 0, r_ns = 0, r_e = 0, r_end = 0;
+    // Entering chunk r_id (its row offsets were loaded a chunk ago): its
+    // first side, and L2 prefetches of its per-cell planes for its epilogues.
+    auto start_chunk = [&]() {
+        const uint32_t f0 = r_id * C;
+        r_ns = 2u * (min(F, f0 + C) - f0);
+        r_side = 0;
+        r_e = __shfl_sync(kAll, r_rw, 0);
+        r_end = __shfl_sync(kAll, r_rw, 1);
+        if (lane == 0) {
+            const size_t c0 = size_t(2u * f0) * P;
+            const uint32_t bytes = r_ns * P * 4u;
+            prefetch_l2(pp.rho + c0, bytes);
+            prefetch_l2(pp.tau + c0, bytes);
+            prefetch_l2(X + c0, bytes);
+            prefetch_l2(R + c0, bytes);
+            prefetch_l2(Qin + c0, r_ns * P);
+        }
+    };
+    // L2 prefetch of the next chunk's edge words, once its row offsets have
+    // arrived (at the current chunk's second side).
+    bool words_pending = true;
+    auto prefetch_words = [&]() {
+        words_pending = false;
+        if (n_id >= chunks) return;
+        const uint32_t nns = 2u * (min(F, (n_id + 1u) * C) - n_id * C);
+        const uint32_t nb0 = __shfl_sync(kAll, n_rw, 0);
+        const uint32_t nb1 = __shfl_sync(kAll, n_rw, int(nns));
+        const size_t b0 = (size_t(nb0) * 4u) & ~size_t(15);
+        const size_t b1 = min(word_bytes, (size_t(nb1) * 4u + 15u) & ~size_t(15));
+        if (lane == 0 && b1 > b0)
+            prefetch_l2(reinterpret_cast<const unsigned char*>(g.packed) + b0, uint32_t(b1 - b0));
+    };
+    if (!rdone) start_chunk();
+
+    uint32_t wf[D][WPL];  // packed edge words of the requested, not yet issued stages
+    uint32_t nf[D];       // their edge counts
+    uint32_t requested = 0, issued = 0, consumed = 0;
+    // Request the next stage: its descriptor goes to meta[stage % NQ], its
+    // words (0 past the stage's edges) to the back of the queue.
+    auto request = [&]() {
+        uint32_t w[WPL], n = 0u;
+#pragma unroll
+        for (int j = 0; j < WPL; ++j) w[j] = 0u;
+        if (!rdone) {
+            n = min(uint32_t(kStageEdges), r_end - r_e);
+            const bool last = r_e + n == r_end;
+            const uint32_t dn = __shfl_sync(kAll, r_dn, int(r_side));
+            if (lane == 0)
+                meta[requested & (NQ - 1)] = make_uint4(2u * r_id * C + r_side, last ? 1u : 0u, dn, n);
+#pragma unroll
+            for (int j = 0; j < WPL; ++j)
+                if (uint32_t(j * 32 + lane) < n) w[j] = __ldcs(g.packed + r_e + j * 32 + lane);
+            ++requested;
+            r_e += n;
+            if (last) {
+                ++r_side;
+                if (r_side == r_ns) {
+                    r_id = n_id;
+                    r_rw = n_rw;
+                    r_dn = n_dn;
+                    if (r_id >= chunks) {
+                        rdone = true;
+                    } else {
+                        start_chunk();
+                        grab(n_id, n_rw, n_dn);
+                        words_pending = true;
+                    }
+                } else {
+                    r_e = __shfl_sync(kAll, r_rw, int(r_side));
+                    r_end = __shfl_sync(kAll, r_rw, int(r_side) + 1);
+                    if (words_pending) prefetch_words();
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < D - 1; ++k) {
+#pragma unroll
+            for (int j = 0; j < WPL; ++j) wf[k][j] = wf[k + 1][j];
+            nf[k] = nf[k + 1];
+        }
+#pragma unroll
+        for (int j = 0; j < WPL; ++j) wf[D - 1][j] = w[j];
+        nf[D - 1] = n;
+    };
+    // Issue the oldest requested stage (front of the queue): its counts and
+    // row copies into ring slot issued % NST, as one copy group.
+    // Edge e = k * G + grp of a stage is the k-th edge of lane group grp:
+    // its count's low byte goes to byte k % 4 of word (k / 4) * G + grp, the
+    // word one dp4a of that group uses.  Lane l holds edges j * 32 + l, so
+    // k = 4 j + l / G.
+    const int cnt_byte = (lane % G) * 4 + lane / G;
+    const unsigned char* qsrc = reinterpret_cast<const unsigned char*>(Qin) + sub * 16;
+    auto issue = [&]() {
+        if (issued < requested) {
+            const int slot = int(issued % NST);
+            const uint32_t n = nf[0];
+            uint32_t nb[WPL], c[WPL];
+            uint32_t cmax = 0u;
+#pragma unroll
+            for (int j = 0; j < WPL; ++j) {
+                nb[j] = wf[0][j] & nb_mask;
+                c[j] = wf[0][j] >> g.nb_bits;
+                cmax |= c[j];
+            }
+            unsigned char* cs = cnt_s + slot * Lay::kCountBytes;
+#pragma unroll
+            for (int j = 0; j < WPL; ++j) cs[j * 32 + cnt_byte] = static_cast<unsigned char>(c[j] & 255u);
+            const bool high = __any_sync(kAll, cmax > 255u);
+            if (high) {
+#pragma unroll
+                for (int j = 0; j < WPL; ++j)
+                    reinterpret_cast<uint32_t*>(cs + SE + 16)[j * 32 + lane] = c[j];
+            }
+            if (lane == 0) reinterpret_cast<uint32_t*>(cs + SE)[0] = high ? 1u : 0u;
+            unsigned char* dst = ring + slot * Lay::kStageBytes + sub * 16;
+#pragma unroll
+            for (int k = 0; k < CPL; ++k) {
+                const int row = k * G + grp;  // row / 32 == k / 4
+                const uint32_t rn = __shfl_sync(kAll, nb[k / 4], row & 31);
+                if (uint32_t(row) < n) cp_async16(dst + row * P, qsrc + size_t(rn) * P);
+            }
+            ++issued;
+        }
+        cp_async_commit();
+    };
+
+    // ---- consumer ----------------------------------------------------------
+    int acc[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc[k] = 0;
+    float h0[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) h0[k] = 0.0f;
+
+    auto consume = [&]() {
+        const int slot = int(consumed % NST);
+        const uint4 mt = meta[consumed & (NQ - 1)];
+        const unsigned char* cs = cnt_s + slot * Lay::kCountBytes;
+        const uint4* rows = reinterpret_cast<const uint4*>(ring + slot * Lay::kStageBytes);
+        const bool high = reinterpret_cast<const uint32_t*>(cs + SE)[0] != 0u;
+#pragma unroll
+        for (int blk = 0; blk < EPL / 4; ++blk) {
+            uint4 q[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) q[k] = rows[((blk * 4 + k) * G + grp) * L + sub];
+            const uint32_t lo = reinterpret_cast<const uint32_t*>(cs)[blk * G + grp];
+            const uint32_t e0[4] = {q[0].x, q[0].y, q[0].z, q[0].w};
+            const uint32_t e1[4] = {q[1].x, q[1].y, q[1].z, q[1].w};
+            const uint32_t e2[4] = {q[2].x, q[2].y, q[2].z, q[2].w};
+            const uint32_t e3[4] = {q[3].x, q[3].y, q[3].z, q[3].w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                uint32_t t[4];
+                transpose4(e0[i], e1[i], e2[i], e3[i], t);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) acc[4 * i + k] = dp4a_su(t[k], lo, acc[4 * i + k]);
+                if (high) {  // rare: counts above 255 add their higher bytes
+                    const uint32_t* cf = reinterpret_cast<const uint32_t*>(cs + SE + 16);
+                    const int c0 = int(cf[(blk * 4) * G + grp]), c1 = int(cf[(blk * 4 + 1) * G + grp]),
+                              c2 = int(cf[(blk * 4 + 2) * G + grp]),
+                              c3 = int(cf[(blk * 4 + 3) * G + grp]);
+                    for (int sh = 8; sh < 32; sh += 8) {
+                        const uint32_t cb = pack_bytes(c0, c1, c2, c3, sh);
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            acc[4 * i + k] += int(uint32_t(dp4a_su(t[k], cb, 0)) << sh);
+                    }
+                }
+            }
+        }
+        ++consumed;
+        if (!mt.y) return;
+        // the side's last stage: sums, then (odd side) the facet's update
+        reduce_scatter_i8<G, L>(acc, lane);
+        const float inv = mt.z ? 1.0f / float(mt.z) : 0.0f;
+        float h[NC];
+#pragma unroll
+        for (int k = 0; k < NC; ++k) h[k] = float(acc[k]) * si[k] * inv;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) acc[k] = 0;
+        if ((mt.x & 1u) == 0u) {
+#pragma unroll
+            for (int k = 0; k < NC; ++k) h0[k] = h[k];
+            return;
+        }
+        const uint32_t f = mt.x >> 1;
+        const size_t i0 = size_t(2u * f) * P + col0, i1 = i0 + P;
+        float r0[NC], r1[NC], t0[NC], t1[NC], x0[NC], x1[NC], s0[NC], s1[NC];
+        int q0[NC], q1[NC];
+        VecN<NC>::ld(pp.rho + i0, r0);
+        VecN<NC>::ld(pp.rho + i1, r1);
+        VecN<NC>::ld(pp.tau + i0, t0);
+        VecN<NC>::ld(pp.tau + i1, t1);
+        VecN<NC>::ld(X + i0, x0);
+        VecN<NC>::ld(X + i1, x1);
+        VecN<NC>::ld(R + i0, s0);
+        VecN<NC>::ld(R + i1, s1);
+        VecN<NC>::ldq(Qin + i0, q0);
+        VecN<NC>::ldq(Qin + i1, q1);
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const float kd0 = r0[k] * h0[k] + t0[k] * h[k];
+            const float kd1 = r1[k] * h[k] + t1[k] * h0[k];
+            const float dl0 = si[k] * float(q0[k]), dl1 = si[k] * float(q1[k]);
+            x0[k] += dl0;
+            x1[k] += dl1;
+            s0[k] = s0[k] - dl0 + kd0;
+            s1[k] = s1[k] - dl1 + kd1;
+            const float n0 = om[k] * s0[k] + (om[k] - 1.0f) * dl0;
+            const float n1 = om[k] * s1[k] + (om[k] - 1.0f) * dl1;
+            q0[k] = max(-127, min(127, __float2int_rn(n0 * inv_so[k])));
+            q1[k] = max(-127, min(127, __float2int_rn(n1 * inv_so[k])));
+            md[k] = fmaxf(md[k], fmaxf(fabsf(s0[k]), fabsf(s1[k])));
+            mb[k] = fmaxf(mb[k], fmaxf(fabsf(x0[k]), fabsf(x1[k])));
+            mr[k] = fmaxf(mr[k], fmaxf(__fdividef(fabsf(s0[k]), fmaxf(fabsf(x0[k]), fl[k])),
+                                       __fdividef(fabsf(s1[k]), fmaxf(fabsf(x1[k]), fl[k]))));
+        }
+        VecN<NC>::st(X + i0, x0);
+        VecN<NC>::st(X + i1, x1);
+        VecN<NC>::st(R + i0, s0);
+        VecN<NC>::st(R + i1, s1);
+        VecN<NC>::stq(Qout + i0, q0);
+        VecN<NC>::stq(Qout + i1, q1);
+    };
+
+    // ---- the pipeline --------------------------------------------------------
+    // Issue step j commits copy group j (empty once the facets run out), so
+    // waiting until at most NST - 1 newer groups are pending completes the
+    // stage about to be consumed.  Stage k's descriptor was written D issue
+    // steps before it is issued and NST - 1 + D before it is consumed; its
+    // slot (k % NQ) is rewritten only after stage k was consumed.
+#pragma unroll
+    for (int k = 0; k < D; ++k) request();
+    __syncwarp();
+#pragma unroll 1
+    for (int k = 0; k < NST - 1; ++k) {
+        issue();
+        request();
+        __syncwarp();
+    }
+#pragma unroll 1
+    while (consumed < issued) {
+        issue();
+        request();
+        cp_async_wait<NST - 1>();
+        __syncwarp();
+        consume();
+        __syncwarp();
+    }
+    cp_async_wait<0>();
+
+    // ---- statistics: CTA max per column, one atomic per column -------------
+    __syncthreads();  // every warp is done with its ring
+    float* s_md = reinterpret_cast<float*>(dyn);
+    float* s_mb = s_md + kWarps * P;
+    float* s_mr = s_mb + kWarps * P;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        s_md[warp * P + col0 + k] = md[k];
+        s_mb[warp * P + col0 + k] = mb[k];
+        s_mr[warp * P + col0 + k] = mr[k];
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < P; c += blockDim.x) {
+        float a = 0.0f, b = 0.0f, r = 0.0f;
+        for (int w = 0; w < kWarps; ++w) {
+            a = fmaxf(a, s_md[w * P + c]);
+            b = fmaxf(b, s_mb[w * P + c]);
+            r = fmaxf(r, s_mr[w * P + c]);
+        }
+        atomicMax(stats + c, __float_as_uint(a));
+        atomicMax(stats + kMaxP + c, __float_as_uint(b));
+        atomicMax(stats + 2 * kMaxP + c, __float_as_uint(r));
+    }
+}
+
 __device__ __forceinline__ float cheb_advance(float* cheb, int c, int mode, float md);
 
 // After an int8 step of a scene batch: a scene whose worst per-side ratio is
@@ -1449,6 +1879,30 @@ int step_grid()
     return grid;
 }
 
+// The pipelined 64-column step: its dynamic shared memory is opted in once
+// (before any graph capture) and the grid sized for it.
+int async_step_grid()
+{
+    static const int grid = [] {
+        constexpr int bytes = AsyncLayout<64>::kBlockBytes;
+        FCU_CHECK(cudaFuncSetAttribute(k_step_i8_async<64>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        FCU_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_i8_async<64>,
+                                                                kWarps * 32, bytes));
+        return std::max(1, sms) * std::max(1, per_sm);
+    }();
+    return grid;
+}
+
+bool use_async_step(int P, const GraphView& g)
+{
+    return FCU_STEP_ASYNC && P == 64 && g.scene == nullptr && g.packed != nullptr &&
+           g.legacy_step == 0u;
+}
+
 // parity: the step's index modulo 2 (its input scales are slot `parity`,
 // its output scales slot `parity ^ 1`)
 void launch_step_i8(int P, const GraphView& g, const PanelParams& pp, const int8_t* qin,
@@ -1473,6 +1927,9 @@ void launch_step_i8(int P, const GraphView& g, const PanelParams& pp, const int8
         if (sc)
             k_step_i8<64, true><<<step_grid<64, true>(), kWarps * 32, 0, s>>>(
                 g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
+        else if (use_async_step(P, g))
+            k_step_i8_async<64><<<async_step_grid(), kWarps * 32, AsyncLayout<64>::kBlockBytes,
+                                  s>>>(g, pp, qin, qout, X, R, sin, sout, stats, counter, done);
         else
             k_step_i8<64, false><<<step_grid<64, false>(), kWarps * 32, 0, s>>>(
                 g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
@@ -1549,7 +2006,7 @@ cudaGraphExec_t step_graph(BatchState& st, const StepGraphKey& key)
     release_graphs(st);
     switch (key.P) {  // size the grids before capture starts
     case 32: step_grid<32, false>(); step_grid<32, true>(); break;
-    case 64: step_grid<64, false>(); step_grid<64, true>(); break;
+    case 64: step_grid<64, false>(); step_grid<64, true>(); async_step_grid(); break;
     default: step_grid<128, false>(); step_grid<128, true>(); break;
     }
     cudaGraph_t graph = nullptr;
@@ -1717,6 +2174,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
     g.scene_sig = nullptr;
     g.scene_cheb = nullptr;
     g.scene_done = nullptr;
+    g.legacy_step = (cfg.flags & FACETCU_BATCH_LEGACY_STEP) != 0u ? 1u : 0u;
     if (FCU_SCENE_SKIP && perm && mixed && gr.p_scene.ptr && gr.p_scene.bytes >= size_t(S / 2u) * 2 &&
         gr.scene_facets.size() >= 3) {
         // scene batch: converged scenes leave the int8 steps

@@ -34,6 +34,7 @@ WARM_NONE = 0
 WARM_GIVEN = 1
 WARM_MLP = 2
 BATCH_TIME_SWEEPS = 1
+BATCH_LEGACY_STEP = 2
 
 
 class FacetcuError(RuntimeError):

@@ -298,3 +298,42 @@ def test_autotune_panel_width_and_cache(c1, tmp_path):
     assert fresh.autotuneBatched(cfg, *ptrs, out.data_ptr(), str(cache)) == best  # from the cache
     assert np.array_equal(solve(fresh, 0), tuned)
     fresh.close()
+
+
+@pytest.mark.parametrize("kind", ["forest", "coarse_soil"])
+def test_pipelined_int8_step_bit_identical(kind):
+    """The 64-column int8 step runs as an asynchronous-copy pipeline (rows
+    staged in shared memory by cp.async); FACETCU_BATCH_LEGACY_STEP runs the
+    register-gather kernel instead.  Both sum exactly in int32, so the
+    radiosity must be the same bits and the sweep counts the same; the
+    result meets the 1e-4 bar against FP64.  Both graphs have empty rows
+    (downward soil sides); the coarse soil (2.5 m quads under low leaves)
+    has counts above 255, the high-byte path of the dp4a sums."""
+    if kind == "forest":
+        sc = scenes.forest(6, 20.0, 2000, 3, name="step")
+    else:
+        sc = scenes.config1(seed=3, leaves=2048, grid=4)
+    m = facetcu.FacetrtCuda()
+    m.initialize(512, 512, 1024)
+    m.setGeometry(sc.vertices)
+    sun = scenes.sun_direction(30.0, 135.0)
+    uv, dirs = scenes.hemisphere_samples(512, 32, seed=7)
+    m.buildHemisphereGraph(uv, dirs, 512, 256, 32)
+    suv, _ = scenes.hemisphere_samples(256, 32, seed=8)
+    lit = m.hemisphereSunlit(sun, suv, 256, 32)
+    rows, _, counts, _, _ = m.graph()
+    assert np.any(np.diff(rows) == 0)  # empty rows
+    if kind == "coarse_soil":
+        assert 255 < counts.max() < 1024  # packed graph, counts above one byte
+    rho, tau, dgeo, sky, beam = _bands(sc, lit, sun, 64)
+    a, ra = m.solveBatched(rho, tau, sky, beam, dgeo, precision=facetcu.PRECISION_MIXED,
+                           tolerance=1e-6)
+    b, rb = m.solveBatched(rho, tau, sky, beam, dgeo, precision=facetcu.PRECISION_MIXED,
+                           tolerance=1e-6, flags=facetcu.BATCH_LEGACY_STEP)
+    assert ra["iterations"] == rb["iterations"]
+    assert ra["kernel_launches"] == rb["kernel_launches"]
+    assert np.array_equal(a, b)
+    truth, _ = m.solveBatched(rho, tau, sky, beam, dgeo, precision=facetcu.PRECISION_FP64,
+                              tolerance=1e-12, maximum_iterations=4000)
+    assert rel_err(a, truth) < 1e-4
+    m.close()

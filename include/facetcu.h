@@ -336,12 +336,14 @@ int facetcu_mlp_samples_device(facetcu_context *ctx, const facetcu_batch_config 
  * sweeps); the result is written to `radiosity`.  Work is queued on
  * `stream` (a cudaStream_t; NULL = the default stream) of the current
  * device; when max_delta is non-NULL the call waits for the stream and
- * stores the last sweep's max|dB|, otherwise it returns once the work is
- * queued.  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  All calls share the one array: calls whose
- * work overlaps on a GPU (other threads or streams) race and must be
- * serialised by the caller.  Inputs are not read back for validation. */
+ * stores the last sweep's max|dB| (max_delta must then be NULL while
+ * `stream` is being captured into a graph: FACETCU_INVALID_ARGUMENT),
+ * otherwise it returns once the work is queued.  Every call looks up the
+ * array's device address (cudaGetSymbolAddress) in the current device's
+ * context, so a context reset between calls is harmless.  All calls share
+ * the one array: calls whose work overlaps on a GPU (other threads or
+ * streams) race and must be serialised by the caller.  Inputs are not read
+ * back for validation. */
 #define FACETCU_NOALLOC_MAX_SURFACES 1048576u
 #define FACETCU_NOALLOC_MAX_ITERATIONS 4096u
 int facetcu_solve_noalloc(const uint32_t *row_offsets, const facetcu_csr_edge *edges,

@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cctype>
 #include <cmath>
+#include <climits>
 #include <cstdint>
 #include <cstring>
 #include <filesystem>
@@ -735,6 +736,7 @@ Raster read_png(const std::vector<uint8_t>& b, int band)
     const int channels = color == 0 ? 1 : color == 2 ? 3 : color == 3 ? 1 : color == 4 ? 2
                          : color == 6 ? 4 : 0;
     if (!channels || (depth != 8 && depth != 16) || interlace != 0 || width == 0 || height == 0 ||
+        width > uint32_t(INT_MAX) || height > uint32_t(INT_MAX) ||
         uint64_t(width) * height > (uint64_t(1) << 31) || (color == 3 && depth != 8))
         throw OpenError("png: unsupported");
     if (band < 0 || band >= channels) throw ReadError("png: band");

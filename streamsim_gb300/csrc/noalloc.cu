@@ -4,11 +4,12 @@
 // Its working memory is one file-scope device array: the second radiosity
 // buffer of the ping-pong pair (the caller's output is the first) followed
 // by one max|dB| slot per sweep.  Host code must not use the array's name as
-// a device address; the address is looked up once per device with
-// cudaGetSymbolAddress while that device is current, and passed to the
-// kernels.  Every call clears the parts that must start at zero.
+// a device address; every call looks the address up with
+// cudaGetSymbolAddress on the current device (the context of that device may
+// have been reset and the module reloaded since an earlier call, so a cached
+// address could be stale) and passes it to the kernels.  Every call clears
+// the parts that must start at zero.
 #include <cmath>
-#include <mutex>
 
 #include "internal.h"
 
@@ -16,17 +17,13 @@ namespace {
 
 constexpr uint32_t kMaxSurfaces = FACETCU_NOALLOC_MAX_SURFACES;
 constexpr uint32_t kMaxIterations = FACETCU_NOALLOC_MAX_ITERATIONS;
-constexpr int kMaxDevices = 64;
 
 // [0, kMaxSurfaces): radiosity buffer (float bits); then kMaxIterations
 // max|dB| slots.  (1,048,576 + 4,096) x 4 B = 4.2 MB per device.
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kMaxSurfaces + kMaxIterations];
 
-std::mutex g_setup_mutex;
-uint32_t* g_scratch_address[kMaxDevices] = {};
-
-// Device address of g_noalloc_scratch on the current device (set-up once
-// per device, with that device current).
+// Device address of g_noalloc_scratch in the current device's context,
+// looked up on every call (a host-side lookup, no device work).
 int scratch_for_current_device(uint32_t** out)
 {
     int device = 0;
@@ -34,18 +31,13 @@ int scratch_for_current_device(uint32_t** out)
         cudaGetLastError();
         return FACETCU_NO_DEVICE;
     }
-    if (device < 0 || device >= kMaxDevices) return FACETCU_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_address[device]) {
-        void* ptr = nullptr;
-        const cudaError_t rc = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (rc != cudaSuccess || !ptr) {
-            cudaGetLastError();
-            return FACETCU_CUDA_ERROR;
-        }
-        g_scratch_address[device] = static_cast<uint32_t*>(ptr);
+    void* ptr = nullptr;
+    const cudaError_t rc = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (rc != cudaSuccess || !ptr) {
+        cudaGetLastError();
+        return FACETCU_CUDA_ERROR;
     }
-    *out = g_scratch_address[device];
+    *out = static_cast<uint32_t*>(ptr);
     return FACETCU_OK;
 }
 
@@ -64,12 +56,22 @@ extern "C" int facetcu_solve_noalloc(const uint32_t* row_offsets, const facetcu_
     if (iterations == 0 || iterations > kMaxIterations) return FACETCU_INVALID_ARGUMENT;
     if (!(relaxation > 0.0f && relaxation <= 1.0f)) return FACETCU_INVALID_ARGUMENT;
     if (!std::isfinite(sky_radiosity) || sky_radiosity < 0.0f) return FACETCU_INVALID_ARGUMENT;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (max_delta) {
+        // reading max|dB| back waits for the stream, which a stream being
+        // captured into a graph cannot do
+        cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &capture) != cudaSuccess) {
+            cudaGetLastError();
+            return FACETCU_CUDA_ERROR;
+        }
+        if (capture != cudaStreamCaptureStatusNone) return FACETCU_INVALID_ARGUMENT;
+    }
     uint32_t* scratch = nullptr;
     const int rc = scratch_for_current_device(&scratch);
     if (rc != FACETCU_OK) return rc;
     float* work = reinterpret_cast<float*>(scratch);
     uint32_t* residual = scratch + kMaxSurfaces;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     try {
         // Sweep i reads buffer i % 2 and writes (i + 1) % 2; the caller's
         // output is the buffer holding the final sweep, so no copy is needed.

@@ -77,4 +77,45 @@ def test_report_compares_with_the_fp64_solution():
     rep = bench.energy_report(model, verts, rho, tau, L, beam, dgeo[None, :], exact.copy(),
                               exact, torch.device("cpu"), emission=emis)
     assert rep["absorbed_rel_err_vs_fp64"] == 0.0 and rep["rel_err_per_side"]["max"] == 0.0
-    assert rep["closure_residual"] < 1e-14
+    assert rep["fixed_point_defect"] < 1e-14
+
+
+def _equal_area_graph(rng, facets=6, denom=100):
+    """Right triangles of area 0.5 and a symmetric count matrix with equal
+    denominators: A_s F_sn = 0.5 c_sn / denom is symmetric (exact
+    reciprocity)."""
+    verts = np.zeros((facets * 3, 6), np.float32)
+    for f in range(facets):
+        verts[3 * f] = [f * 2.0, 0, 0, 0, 1, 0]
+        verts[3 * f + 1] = [f * 2.0 + 1.0, 0, 0, 0, 1, 0]
+        verts[3 * f + 2] = [f * 2.0, 0, 1.0, 0, 1, 0]
+    S = 2 * facets
+    c = rng.integers(0, 9, (S, S))
+    c = np.triu(c, 1)
+    c = c + c.T
+    rows, nbrs, counts = [0], [], []
+    for s in range(S):
+        for n in range(S):
+            if c[s, n]:
+                nbrs.append(n)
+                counts.append(c[s, n])
+        rows.append(len(nbrs))
+    den = np.full(S, denom, np.uint32)
+    return verts, [np.array(rows, np.uint32), np.array(nbrs, np.uint32),
+                   np.array(counts, np.uint32), den, den - np.array([c[s].sum() for s in range(S)],
+                                                                    np.uint32)]
+
+
+def test_exchange_metrics_reciprocity_and_conservation():
+    """Exact reciprocity gives zero reciprocity error and a zero conservation
+    residual for any radiosity; breaking one count's symmetry shows in both."""
+    rng = np.random.default_rng(3)
+    verts, g = _equal_area_graph(rng)
+    B = [rng.uniform(1, 5, len(g[3])) for _ in range(3)]
+    rec, cons = bench.exchange_metrics(g, verts, B, torch.device("cpu"))
+    assert rec["weighted"] < 1e-15 and rec["reverse_edge_share"] == 1.0
+    assert cons["max_over_bands"] < 1e-14
+    g[2] = g[2].copy()
+    g[2][0] += 3  # one directed count without its reverse change
+    rec, cons = bench.exchange_metrics(g, verts, B, torch.device("cpu"))
+    assert rec["weighted"] > 1e-3 and cons["max_over_bands"] > 1e-4

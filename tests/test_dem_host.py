@@ -21,7 +21,7 @@ from streamsim_gb300 import facetcu
 from tests import tiff_writer
 from tests.test_project_host import _compare, _write_project, ref_project  # noqa: F401
 
-REFERENCE = os.environ.get("FACETRT_REFERENCE_ROOT", "/root/reference")
+from oracle.build_ref import REFERENCE  # the reference tree the oracle recipe reads
 
 
 def _reference_file(*parts):

@@ -12,10 +12,10 @@ import shutil
 import numpy as np
 import pytest
 
+from oracle.build_ref import REFERENCE  # the reference tree the oracle recipe reads
 from streamsim_gb300 import facetcu
 
-OPTIPAR = os.path.join(os.environ.get("FACETRT_REFERENCE_ROOT", "/root/reference"),
-                       "models", "bin_x64", "Release", "defined", "optipar.txt")
+OPTIPAR = os.path.join(REFERENCE, "models", "bin_x64", "Release", "defined", "optipar.txt")
 
 HOUSE_OBJ = """# a house: walls and a roof in their own groups
 o body

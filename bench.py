@@ -72,6 +72,9 @@ def parse():
                         "(16,384 right-hand sides, outputs kept on the device); c5: 32 scenes "
                         "of uneven size, 64 bands + a thermal band, as one batch; eb: one "
                         "FacetEB time node (shortwave windows, longwave coupling, sensor bands)")
+    p.add_argument("--step-kernel", default="pipelined", choices=["pipelined", "register"],
+                   help="64-column int8 steps: the asynchronous-copy pipeline (default) or the "
+                        "register-gather kernel (FACETCU_BATCH_LEGACY_STEP; same results)")
     p.add_argument("--warm-start", default="none", choices=["auto", "mlp", "none"],
                    help="mlp: the shipped MLP weights; auto: those when present and bands == 64")
     return p.parse_args()
@@ -507,6 +510,7 @@ def run_gpu(args, rank, world, local):
     if use_mlp:
         m.mlpLoad()
     warm = fc.WARM_MLP if use_mlp else fc.WARM_NONE
+    step_flags = fc.BATCH_LEGACY_STEP if args.step_kernel == "register" else 0
 
     # FP64 truth of the same graph (not timed)
     truth, tres = m.solveBatched(w["rho"], w["tau"], w["sky"], w["beam"], w["dgeo"],
@@ -519,7 +523,7 @@ def run_gpu(args, rank, world, local):
     out = torch.empty((B, S), dtype=torch.float32, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.ExternalStream(m.stream(), device=dev)
-    cfg = fc.BatchConfig(B, 1, prec, warm, 2000, args.tolerance, 0, 0)
+    cfg = fc.BatchConfig(B, 1, prec, warm, 2000, args.tolerance, 0, step_flags)
 
     def step(c=cfg):
         return m.solveBatchedDevice(c, t["rho"].data_ptr(), t["tau"].data_ptr(), None,
@@ -586,7 +590,8 @@ def run_gpu(args, rank, world, local):
     value = units * world / step_s
 
     # sweep-kernel roofline: one extra solve with per-sweep CUDA events
-    cfg_t = fc.BatchConfig(B, 1, prec, warm, 2000, args.tolerance, 0, fc.BATCH_TIME_SWEEPS)
+    cfg_t = fc.BatchConfig(B, 1, prec, warm, 2000, args.tolerance, 0,
+                           fc.BATCH_TIME_SWEEPS | step_flags)
     rt = step(cfg_t)
     peaks = {}
     try:
@@ -597,7 +602,7 @@ def run_gpu(args, rank, world, local):
     achieved = rt["sweep_bytes"] / max(rt["sweep_seconds"], 1e-12) / 1e9
     panel = min(128, 1 << (B - 1).bit_length())
     kname = (f"k_sweep_wide<{panel}>" if prec != fc.PRECISION_MIXED else
-             "k_step_i8_async<64>" if panel == 64 else f"k_step_i8<{panel}>")
+             "k_step_i8_async<64>" if panel == 64 and not step_flags else f"k_step_i8<{panel}>")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": None, "kernel": kname,
                 "launches_timed": rt["timed_sweeps"],

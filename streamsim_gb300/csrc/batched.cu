@@ -1047,11 +1047,12 @@ __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes)
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-template <int P>
+template <int P, bool Scenes>
 __global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async(
     GraphView g, PanelParams pp, const int8_t* __restrict__ Qin, int8_t* __restrict__ Qout,
     float* __restrict__ X, float* __restrict__ R, const float* __restrict__ sig_in,
-    const float* __restrict__ sig_out, uint32_t* stats, uint32_t* counter, const uint32_t* done)
+    const float* __restrict__ sig_out, uint32_t* stats, uint32_t* counter, const uint32_t* done,
+    const float* __restrict__ scene_sig_in, const float* __restrict__ scene_sig_out)
 {
     static_assert(P == 64, "the pipelined step covers 64-column panels");
     using Lay = AsyncLayout<P>;
@@ -1061,7 +1062,8 @@ __global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async
     constexpr int EPL = SE / G;        // edges per lane per stage
     constexpr int CPL = SE * L / 32;   // 16-byte copies per lane per stage
     constexpr int NST = kAsyncStages, D = kLookahead, NQ = Lay::kDesc;
-    constexpr uint32_t C = kChunk;
+    constexpr uint32_t C = Scenes ? kSceneChunk : kChunk;
+    static_assert(2 * C + 1 <= 32, "a chunk's row offsets fit one warp");
     constexpr unsigned kAll = 0xffffffffu;
     static_assert(SE == 32 || SE == 64, "32 or 64 edges per stage");
     static_assert(EPL % 4 == 0 && G == 8, "4 x 4 transpose blocks, 8 edge groups");
@@ -1088,26 +1090,55 @@ __global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async
         mr[k] = 0.0f;
     }
 
+    // Scene batches: each scene steps with its own int8 scales and Chebyshev
+    // weight, the facets of a converged scene get no stages, and the
+    // scene's worst per-side ratio and max |R| are gathered while the warp
+    // stays in that scene (flushed with atomics when it moves on), as in
+    // k_step_i8<P, true>.
+    uint32_t cur = 0xffffffffu;
+    float ms[NC], mq[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        ms[k] = 0.0f;
+        mq[k] = 0.0f;
+    }
+    auto flush = [&]() {
+        if (Scenes && cur != 0xffffffffu) {
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                atomicMax(g.scene_stats + size_t(cur) * kMaxP + col0 + k, __float_as_uint(ms[k]));
+                atomicMax(g.scene_md + size_t(cur) * kMaxP + col0 + k, __float_as_uint(mq[k]));
+            }
+        }
+    };
+
     // ---- request cursor: chunks, sides, stages ---------------------------
     const uint32_t F = g.facets;
     const uint32_t chunks = (F + C - 1) / C;
     const uint32_t nb_mask = (1u << g.nb_bits) - 1u;
     const size_t word_bytes = (size_t(__ldg(g.rows + 2u * F)) * 4u) & ~size_t(15);  // prefetch bound
     // a chunk: its id, and in lane i its side i's row start (lanes 0..sides)
-    // and denominator (lanes 0..sides-1)
-    auto grab = [&](uint32_t& id, uint32_t& rw, uint32_t& dn) {
+    // and denominator (lanes 0..sides-1); with scenes, in lane i facet i's
+    // scene and whether that scene is done
+    auto grab = [&](uint32_t& id, uint32_t& rw, uint32_t& dn, uint32_t& sc, uint32_t& fd) {
         id = next_chunk(counter, lane);
         rw = 0u;
         dn = 0u;
+        sc = 0u;
+        fd = 0u;
         if (id < chunks) {
             const uint32_t s0 = 2u * id * C, ns = 2u * (min(F, (id + 1u) * C) - id * C);
             if (uint32_t(lane) <= ns) rw = __ldg(g.rows + s0 + lane);
             if (uint32_t(lane) < ns) dn = __ldg(g.denom + s0 + lane);
+            if (Scenes && uint32_t(lane) < ns / 2u) {
+                sc = __ldg(g.scene + id * C + lane);
+                fd = g.scene_done[sc];
+            }
         }
     };
-    uint32_t r_id, r_rw, r_dn, n_id, n_rw, n_dn;
-    grab(r_id, r_rw, r_dn);
-    grab(n_id, n_rw, n_dn);
+    uint32_t r_id, r_rw, r_dn, r_sc, r_fd, n_id, n_rw, n_dn, n_sc, n_fd;
+    grab(r_id, r_rw, r_dn, r_sc, r_fd);
+    grab(n_id, n_rw, n_dn, n_sc, n_fd);
     bool rdone = r_id >= chunks;
     uint32_t r_side = 0, r_ns = 0, r_e = 0, r_end = 0;
     // Entering chunk r_id (its row offsets were loaded a chunk ago): its
@@ -1149,40 +1180,53 @@ __global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async
     uint32_t requested = 0, issued = 0, consumed = 0;
     // Request the next stage: its descriptor goes to meta[stage % NQ], its
     // words (0 past the stage's edges) to the back of the queue.
+    // The cursor's next side (side r_side + 1, or the next chunk's first).
+    auto next_side = [&]() {
+        ++r_side;
+        if (r_side == r_ns) {
+            r_id = n_id;
+            r_rw = n_rw;
+            r_dn = n_dn;
+            r_sc = n_sc;
+            r_fd = n_fd;
+            if (r_id >= chunks) {
+                rdone = true;
+            } else {
+                start_chunk();
+                grab(n_id, n_rw, n_dn, n_sc, n_fd);
+                words_pending = true;
+            }
+        } else {
+            r_e = __shfl_sync(kAll, r_rw, int(r_side));
+            r_end = __shfl_sync(kAll, r_rw, int(r_side) + 1);
+            if (words_pending) prefetch_words();
+        }
+    };
     auto request = [&]() {
         uint32_t w[WPL], n = 0u;
 #pragma unroll
         for (int j = 0; j < WPL; ++j) w[j] = 0u;
+        if constexpr (Scenes) {
+            // a converged scene's facets get no stages
+            while (!rdone && (r_side & 1u) == 0u &&
+                   __shfl_sync(kAll, r_fd, int(r_side >> 1)) != 0u) {
+                next_side();
+                if (!rdone) next_side();
+            }
+        }
         if (!rdone) {
             n = min(uint32_t(kStageEdges), r_end - r_e);
             const bool last = r_e + n == r_end;
             const uint32_t dn = __shfl_sync(kAll, r_dn, int(r_side));
+            const uint32_t sc = Scenes ? __shfl_sync(kAll, r_sc, int(r_side >> 1)) : 0u;
             if (lane == 0)
-                meta[requested & (NQ - 1)] = make_uint4(2u * r_id * C + r_side, last ? 1u : 0u, dn, n);
+                meta[requested & (NQ - 1)] = make_uint4(2u * r_id * C + r_side, last ? 1u : 0u, dn, sc);
 #pragma unroll
             for (int j = 0; j < WPL; ++j)
                 if (uint32_t(j * 32 + lane) < n) w[j] = __ldcs(g.packed + r_e + j * 32 + lane);
             ++requested;
             r_e += n;
-            if (last) {
-                ++r_side;
-                if (r_side == r_ns) {
-                    r_id = n_id;
-                    r_rw = n_rw;
-                    r_dn = n_dn;
-                    if (r_id >= chunks) {
-                        rdone = true;
-                    } else {
-                        start_chunk();
-                        grab(n_id, n_rw, n_dn);
-                        words_pending = true;
-                    }
-                } else {
-                    r_e = __shfl_sync(kAll, r_rw, int(r_side));
-                    r_end = __shfl_sync(kAll, r_rw, int(r_side) + 1);
-                    if (words_pending) prefetch_words();
-                }
-            }
+            if (last) next_side();
         }
 #pragma unroll
         for (int k = 0; k < D - 1; ++k) {
@@ -1283,6 +1327,21 @@ __global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async
         ++consumed;
         if (!mt.y) return;
         // the side's last stage: sums, then (odd side) the facet's update
+        if constexpr (Scenes) {
+            if (mt.w != cur) {
+                flush();
+                cur = mt.w;
+#pragma unroll
+                for (int k = 0; k < NC; ++k) {
+                    ms[k] = 0.0f;
+                    mq[k] = 0.0f;
+                    si[k] = scene_sig_in[size_t(cur) * kMaxP + col0 + k];
+                    const float so = scene_sig_out[size_t(cur) * kMaxP + col0 + k];
+                    inv_so[k] = so > 0.0f ? 1.0f / so : 0.0f;
+                    om[k] = g.scene_cheb[size_t(cur) * 4 * kMaxP + 2 * kMaxP + col0 + k];
+                }
+            }
+        }
         reduce_scatter_i8<G, L>(acc, lane);
         const float inv = mt.z ? 1.0f / float(mt.z) : 0.0f;
         float h[NC];
@@ -1326,6 +1385,17 @@ __global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async
             mb[k] = fmaxf(mb[k], fmaxf(fabsf(x0[k]), fabsf(x1[k])));
             mr[k] = fmaxf(mr[k], fmaxf(__fdividef(fabsf(s0[k]), fmaxf(fabsf(x0[k]), fl[k])),
                                        __fdividef(fabsf(s1[k]), fmaxf(fabsf(x1[k]), fl[k]))));
+            if (Scenes) {
+                // a zero residual passes (the column test's md == 0 case)
+                const float a0 = fabsf(s0[k]) > 0.0f
+                                     ? __fdividef(fabsf(s0[k]), fmaxf(fabsf(x0[k]), fl[k]))
+                                     : 0.0f;
+                const float a1 = fabsf(s1[k]) > 0.0f
+                                     ? __fdividef(fabsf(s1[k]), fmaxf(fabsf(x1[k]), fl[k]))
+                                     : 0.0f;
+                ms[k] = fmaxf(ms[k], fmaxf(a0, a1));
+                mq[k] = fmaxf(mq[k], fmaxf(fabsf(s0[k]), fabsf(s1[k])));
+            }
         }
         VecN<NC>::st(X + i0, x0);
         VecN<NC>::st(X + i1, x1);
@@ -1360,6 +1430,7 @@ __global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async
         __syncwarp();
     }
     cp_async_wait<0>();
+    flush();
 
     // ---- statistics: CTA max per column, one atomic per column -------------
     __syncthreads();  // every warp is done with its ring
@@ -1881,17 +1952,18 @@ int step_grid()
 
 // The pipelined 64-column step: its dynamic shared memory is opted in once
 // (before any graph capture) and the grid sized for it.
+template <bool Scenes>
 int async_step_grid()
 {
     static const int grid = [] {
         constexpr int bytes = AsyncLayout<64>::kBlockBytes;
-        FCU_CHECK(cudaFuncSetAttribute(k_step_i8_async<64>,
+        FCU_CHECK(cudaFuncSetAttribute(k_step_i8_async<64, Scenes>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        FCU_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_i8_async<64>,
-                                                                kWarps * 32, bytes));
+        FCU_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_step_i8_async<64, Scenes>, kWarps * 32, bytes));
         return std::max(1, sms) * std::max(1, per_sm);
     }();
     return grid;
@@ -1899,8 +1971,7 @@ int async_step_grid()
 
 bool use_async_step(int P, const GraphView& g)
 {
-    return FCU_STEP_ASYNC && P == 64 && g.scene == nullptr && g.packed != nullptr &&
-           g.legacy_step == 0u;
+    return FCU_STEP_ASYNC && P == 64 && g.packed != nullptr && g.legacy_step == 0u;
 }
 
 // parity: the step's index modulo 2 (its input scales are slot `parity`,
@@ -1924,12 +1995,17 @@ void launch_step_i8(int P, const GraphView& g, const PanelParams& pp, const int8
                 g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
         break;
     case 64:
-        if (sc)
-            k_step_i8<64, true><<<step_grid<64, true>(), kWarps * 32, 0, s>>>(
+        if (use_async_step(P, g) && sc)
+            k_step_i8_async<64, true><<<async_step_grid<true>(), kWarps * 32,
+                                        AsyncLayout<64>::kBlockBytes, s>>>(
                 g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
         else if (use_async_step(P, g))
-            k_step_i8_async<64><<<async_step_grid(), kWarps * 32, AsyncLayout<64>::kBlockBytes,
-                                  s>>>(g, pp, qin, qout, X, R, sin, sout, stats, counter, done);
+            k_step_i8_async<64, false><<<async_step_grid<false>(), kWarps * 32,
+                                         AsyncLayout<64>::kBlockBytes, s>>>(
+                g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
+        else if (sc)
+            k_step_i8<64, true><<<step_grid<64, true>(), kWarps * 32, 0, s>>>(
+                g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
         else
             k_step_i8<64, false><<<step_grid<64, false>(), kWarps * 32, 0, s>>>(
                 g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
@@ -2006,7 +2082,12 @@ cudaGraphExec_t step_graph(BatchState& st, const StepGraphKey& key)
     release_graphs(st);
     switch (key.P) {  // size the grids before capture starts
     case 32: step_grid<32, false>(); step_grid<32, true>(); break;
-    case 64: step_grid<64, false>(); step_grid<64, true>(); async_step_grid(); break;
+    case 64:
+        step_grid<64, false>();
+        step_grid<64, true>();
+        async_step_grid<false>();
+        async_step_grid<true>();
+        break;
     default: step_grid<128, false>(); step_grid<128, true>(); break;
     }
     cudaGraph_t graph = nullptr;

@@ -220,6 +220,10 @@ def test_scene_batch_matches_scenes_solved_alone():
     out, res = batch.solveBatched(*args, emission=cat(emis), precision=facetcu.PRECISION_MIXED,
                                   tolerance=1e-6)
     assert res["converged"] and rel_err(out, truth) < 1e-4
+    # the pipelined scene step equals the register-gather one bit for bit
+    reg, rres = batch.solveBatched(*args, emission=cat(emis), precision=facetcu.PRECISION_MIXED,
+                                   tolerance=1e-6, flags=facetcu.BATCH_LEGACY_STEP)
+    assert np.array_equal(out, reg) and res["iterations"] == rres["iterations"]
     for m in models + [batch]:
         m.close()
 

@@ -37,7 +37,9 @@ enum {
     FACETCU_NO_DEVICE = 6,        /* no usable GPU */
     FACETCU_OUT_OF_MEMORY = 7,    /* device allocation failed */
     FACETCU_DEVICE_CAPACITY = 8,  /* a device-side capacity flag was raised */
-    FACETCU_NOT_CONVERGED = 9     /* iteration budget spent; result still written */
+    FACETCU_NOT_CONVERGED = 9,    /* iteration budget spent; result still written */
+    FACETCU_DEVICE_TIMEOUT = 10   /* a bounded wait inside a kernel ran out (the context
+                                     stays usable; the result is not written) */
 };
 
 typedef struct facetcu_context facetcu_context;
@@ -297,6 +299,14 @@ int facetcu_mlp_get_parameters(facetcu_context *ctx, float *parameters);
 int facetcu_mlp_set_parameters(facetcu_context *ctx, const float *parameters);
 /* Forward pass of n samples (host arrays): x[n * 12] -> y[n * 64]. */
 int facetcu_mlp_forward(facetcu_context *ctx, const float *x, uint32_t n, float *y);
+/* The same forward pass on the tensor cores (no reference counterpart; the
+ * inference the learned warm start runs): each layer is 128-row tiles of
+ * tcgen05.mma (BF16 operands staged by TMA, FP32 accumulation in tensor
+ * memory) with the bias and GELU applied when the accumulator is read back;
+ * hidden activations are BF16, so outputs differ from facetcu_mlp_forward by
+ * a BF16 rounding per layer (about 1e-2 of the output scale).
+ * FACETCU_DEVICE_TIMEOUT if a kernel's bounded wait ran out. */
+int facetcu_mlp_forward_tensor(facetcu_context *ctx, const float *x, uint32_t n, float *y);
 /* Mean-squared loss over n x 64 outputs and its FP32 gradient with respect
  * to the parameters (same order), for x[n * 12] and target[n * 64];
  * n <= 2^21 (FACETCU_OVERFLOW_ERROR above). */

@@ -93,3 +93,15 @@ def loss_only(eff, x, t):
     a2 = gelu(z2)
     y = a2 @ eff["W3"].T + eff["b3"]
     return float(((y - t) ** 2).sum() / y.size)
+
+
+def forward_bf16_activations(params, x):
+    """The forward pass as the tensor-core inference rounds it: inputs and
+    hidden activations (after GELU) rounded to BF16, everything else
+    float64.  Returns the (n, 64) outputs."""
+    p = unpack(params)
+    w = {k: bf16_round(p[k]) if k.startswith("W") else p[k] for k in p}
+    a = bf16_round(np.asarray(x, np.float32))
+    a = bf16_round(gelu(a @ w["W1"].T + w["b1"]).astype(np.float32))
+    a = bf16_round(gelu(a @ w["W2"].T + w["b2"]).astype(np.float32))
+    return a @ w["W3"].T + w["b3"]

@@ -54,6 +54,7 @@ struct facetcu_context {
     bool bvh_ready = false;
     mlp::Net net;
     mlp::Scratch mlp_scratch;
+    mlp::TensorScratch mlp_tensor;
     DeviceBuffer mlp_io, warm_b1, warm_x, warm_y, warm_x0;
     DeviceBuffer samples_uv, samples_dir, fraction;
     spectral::Tables spec;
@@ -384,7 +385,8 @@ int facetcu_destroy(facetcu_context* ctx)
                             &ctx->mlp_scratch.a2, &ctx->mlp_scratch.y, &ctx->mlp_scratch.dy,
                             &ctx->mlp_scratch.da, &ctx->mlp_scratch.dz, &ctx->mlp_scratch.part,
                             &ctx->mlp_scratch.lossp, &ctx->mlp_scratch.idx, &ctx->mlp_scratch.xb,
-                            &ctx->mlp_scratch.tb})
+                            &ctx->mlp_scratch.tb, &ctx->mlp_tensor.xb, &ctx->mlp_tensor.a1,
+                            &ctx->mlp_tensor.a2, &ctx->mlp_tensor.w1p, &ctx->mlp_tensor.error})
         b->release();
     ctx->net.ready = false;
     ctx->bvh_ready = false;
@@ -1020,7 +1022,9 @@ int run_batched(facetcu_context* ctx, const facetcu_batch_config* cfg_in, const 
         mlp::features(b1, S, p.bands, p.suns, p.rho, p.tau, p.sky, p.beam,
                       ctx->graph.denominators.as<uint32_t>(), ctx->graph.sky.as<uint32_t>(),
                       ctx->vertices.as<facetcu_vertex>(), x, ctx->stream);
-        mlp::infer(ctx->net, x, size_t(p.suns) * S, ctx->mlp_scratch, y, ctx->stream);
+        mlp::infer_tensor(ctx->net, x, size_t(p.suns) * S, ctx->mlp_tensor, y, ctx->stream);
+        if (mlp::tensor_error(ctx->mlp_tensor, ctx->stream))
+            throw Error(FACETCU_DEVICE_TIMEOUT, "tensor-core MLP kernel timed out");
         mlp::warm_combine(b1, y, S, p.bands, p.suns, p.sky, p.beam, x0, ctx->stream);
         facetcu_batch_config rest = *cfg;
         rest.warm_start = FACETCU_WARM_GIVEN;
@@ -1184,6 +1188,26 @@ int facetcu_mlp_forward(facetcu_context* ctx, const float* x, uint32_t n, float*
         float* dy = dx + size_t(n) * mlp::kInputs;
         FCU_CHECK(cudaMemcpyAsync(dx, x, size_t(n) * mlp::kInputs * 4, cudaMemcpyHostToDevice, s));
         mlp::infer(ctx->net, dx, n, ctx->mlp_scratch, dy, s);
+        FCU_CHECK(cudaMemcpyAsync(y, dy, size_t(n) * mlp::kOutputs * 4, cudaMemcpyDeviceToHost, s));
+        FCU_CHECK(cudaStreamSynchronize(s));
+        return FACETCU_OK;
+    });
+}
+
+int facetcu_mlp_forward_tensor(facetcu_context* ctx, const float* x, uint32_t n, float* y)
+{
+    return guarded(ctx, [&] {
+        require_initialized(ctx, "mlpForwardTensor()");
+        if (!ctx->net.ready) throw Error(FACETCU_LOGIC_ERROR, "the MLP has no parameters yet");
+        if (!x || !y || n == 0) throw Error(FACETCU_INVALID_ARGUMENT, "x, y and n are required");
+        cudaStream_t s = ctx->stream;
+        float* dx = static_cast<float*>(
+            ctx->mlp_io.reserve(size_t(n) * (mlp::kInputs + mlp::kOutputs) * 4));
+        float* dy = dx + size_t(n) * mlp::kInputs;
+        FCU_CHECK(cudaMemcpyAsync(dx, x, size_t(n) * mlp::kInputs * 4, cudaMemcpyHostToDevice, s));
+        mlp::infer_tensor(ctx->net, dx, n, ctx->mlp_tensor, dy, s);
+        if (mlp::tensor_error(ctx->mlp_tensor, s))
+            throw Error(FACETCU_DEVICE_TIMEOUT, "tensor-core MLP kernel timed out");
         FCU_CHECK(cudaMemcpyAsync(y, dy, size_t(n) * mlp::kOutputs * 4, cudaMemcpyDeviceToHost, s));
         FCU_CHECK(cudaStreamSynchronize(s));
         return FACETCU_OK;

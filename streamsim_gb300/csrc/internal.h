@@ -253,6 +253,14 @@ void hemisphere_sunlit(const facetcu_vertex* d_vertices, uint32_t facets, const 
 namespace mlp {
 constexpr int kInputs = 12, kOutputs = 64;
 constexpr int kParameterCount = 128 * 12 + 128 + 128 * 128 + 128 + 64 * 128 + 64;
+// Layer sizes and offsets in the parameter vector (W1[128x12], b1, W2, b2,
+// W3[64x128], b3; row-major W[out][in]).
+constexpr int kIn = 12, kH = 128, kOut = 64;
+constexpr int kW1 = kH * kIn, kB1 = kH, kW2 = kH * kH, kB2 = kH, kW3 = kOut * kH, kB3 = kOut;
+constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kW1, kOffW2 = kOffB1 + kB1, kOffB2 = kOffW2 + kW2,
+              kOffW3 = kOffB2 + kB2, kOffB3 = kOffW3 + kW3, kParams = kOffB3 + kB3;
+static_assert(kParams == kParameterCount, "parameter layout");
+
 struct Net {
     DeviceBuffer params, bf16, adam_m, adam_v, grad;
     bool ready = false;
@@ -261,6 +269,17 @@ struct Net {
 struct Scratch {
     DeviceBuffer z1, a1, z2, a2, y, dy, da, dz, part, lossp, idx, xb, tb;
 };
+// Buffers of the tensor-core inference (mlp_tc.cu).
+struct TensorScratch {
+    DeviceBuffer xb, a1, a2, w1p, error;
+};
+// Inference of n rows on the tensor cores (tcgen05, BF16 activations, FP32
+// accumulation): X[n][12] FP32 -> Y[n][64] FP32.  Asynchronous on s; a
+// wait that ran out inside a kernel is reported by tensor_error.
+void infer_tensor(Net& net, const float* X, size_t n, TensorScratch& ts, float* Y, cudaStream_t s);
+// Nonzero when a tensor-core kernel since the last infer_tensor timed out
+// (synchronises s).
+uint32_t tensor_error(TensorScratch& ts, cudaStream_t s);
 void init_params(Net& net, uint32_t seed, cudaStream_t s);
 void set_params(Net& net, const float* host, cudaStream_t s);
 // Rows per forward pass: kMaxRows keeps the GEMM grid (64 rows per CTA in

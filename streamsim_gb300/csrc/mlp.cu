@@ -23,10 +23,6 @@
 namespace facetcu {
 namespace mlp {
 
-constexpr int kIn = 12, kH = 128, kOut = 64;
-constexpr int kW1 = kH * kIn, kB1 = kH, kW2 = kH * kH, kB2 = kH, kW3 = kOut * kH, kB3 = kOut;
-constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kW1, kOffW2 = kOffB1 + kB1, kOffB2 = kOffW2 + kW2,
-              kOffW3 = kOffB2 + kB2, kOffB3 = kOffW3 + kW3, kParams = kOffB3 + kB3;
 
 namespace {
 

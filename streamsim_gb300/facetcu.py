@@ -26,6 +26,7 @@ NO_DEVICE = 6
 OUT_OF_MEMORY = 7
 DEVICE_CAPACITY = 8
 NOT_CONVERGED = 9
+DEVICE_TIMEOUT = 10
 
 PRECISION_FP32 = 0
 PRECISION_MIXED = 1
@@ -293,6 +294,7 @@ SIGNATURES.update({
     "facetcu_mlp_get_parameters": (C.c_int, [_ctx, _vp]),
     "facetcu_mlp_set_parameters": (C.c_int, [_ctx, _vp]),
     "facetcu_mlp_forward": (C.c_int, [_ctx, _vp, _u32, _vp]),
+    "facetcu_mlp_forward_tensor": (C.c_int, [_ctx, _vp, _u32, _vp]),
     "facetcu_mlp_loss_and_gradient": (C.c_int, [_ctx, _vp, _vp, _u32, C.POINTER(C.c_float), _vp]),
     "facetcu_mlp_train_device": (C.c_int, [_ctx, _vp, _vp, C.c_uint64, C.POINTER(MlpTrainConfig),
                                            C.POINTER(C.c_float)]),
@@ -1048,6 +1050,13 @@ class FacetrtCuda:
         x = _f32(x).reshape(-1, MLP_INPUTS)
         y = np.zeros((len(x), MLP_OUTPUTS), np.float32)
         self._check(self.lib.facetcu_mlp_forward(self.h, _ptr(x), len(x), _ptr(y)))
+        return y
+
+    def mlpForwardTensor(self, x):
+        """The forward pass on the tensor cores (BF16 activations)."""
+        x = _f32(x).reshape(-1, MLP_INPUTS)
+        y = np.zeros((len(x), MLP_OUTPUTS), np.float32)
+        self._check(self.lib.facetcu_mlp_forward_tensor(self.h, _ptr(x), len(x), _ptr(y)))
         return y
 
     def mlpLossAndGradient(self, x, target):

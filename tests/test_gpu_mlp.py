@@ -56,6 +56,29 @@ def test_forward_and_gradient_match_cpu_oracle(model, n):
         off += k
 
 
+@pytest.mark.parametrize("n", [5, 300, 4096, 100003])
+def test_tensor_core_forward(model, n):
+    """facetcu_mlp_forward_tensor (tcgen05.mma on 128-row tiles, BF16
+    operands from TMA, FP32 accumulation in tensor memory; partial last
+    tiles at 5, 300 and 100,003 rows): against the oracle with the same BF16
+    roundings of inputs and hidden activations (5e-3 of the output scale:
+    the FP32 accumulation order can move an activation across a BF16
+    rounding boundary), and against the FP32-activation path (3e-2, the
+    BF16 activations' own effect)."""
+    rng = np.random.default_rng(n + 1)
+    params = rng.normal(scale=0.15, size=M.COUNT).astype(np.float32)
+    model.mlpSetParameters(params)
+    x = rng.normal(size=(n, 12)).astype(np.float32)
+    y = model.mlpForwardTensor(x)
+    scale = max(1.0, float(np.abs(y).max()))
+    ref = M.forward_bf16_activations(params, x)
+    assert np.all(np.isfinite(y))
+    assert np.max(np.abs(y - ref)) <= 5e-3 * scale
+    assert np.max(np.abs(y - model.mlpForward(x))) <= 3e-2 * scale
+    # a second call reuses the buffers and gives the same bits
+    assert np.array_equal(model.mlpForwardTensor(x), y)
+
+
 def test_training_reduces_loss_on_a_learnable_map(model):
     """Adam on device data: fit y = tanh(x A) for a fixed A."""
     torch = pytest.importorskip("torch")

@@ -1004,9 +1004,13 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
 #ifndef FCU_ASYNC_EDGES
 #define FCU_ASYNC_EDGES 64
 #endif
+#ifndef FCU_ASYNC_WARPS
+#define FCU_ASYNC_WARPS 8
+#endif
+constexpr int kAsyncWarps = FCU_ASYNC_WARPS;  // warps per CTA of the pipelined step
 constexpr int kAsyncStages = FCU_ASYNC_STAGES;
 constexpr int kLookahead = FCU_ASYNC_LOOKAHEAD;
-constexpr int kStageEdges = FCU_ASYNC_EDGES;  // 32 or 64 edges per stage
+constexpr int kStageEdges = FCU_ASYNC_EDGES;  // 32, 64 or 128 edges per stage
 
 constexpr int pow2_at_least(int n) { return n <= 1 ? 1 : 2 * pow2_at_least((n + 1) / 2); }
 
@@ -1021,7 +1025,7 @@ struct AsyncLayout {
     static constexpr int kDesc = pow2_at_least(kAsyncStages + kLookahead);
     // per warp: the row ring, the counts of each ring stage, the descriptors
     static constexpr int kWarpBytes = kAsyncStages * (kStageBytes + kCountBytes) + kDesc * 16;
-    static constexpr int kBlockBytes = kWarps * kWarpBytes;
+    static constexpr int kBlockBytes = kAsyncWarps * kWarpBytes;
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p)
@@ -1048,7 +1052,7 @@ __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes)
 }
 
 template <int P, bool Scenes>
-__global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async(
+__global__ void __launch_bounds__(kAsyncWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async(
     GraphView g, PanelParams pp, const int8_t* __restrict__ Qin, int8_t* __restrict__ Qout,
     float* __restrict__ X, float* __restrict__ R, const float* __restrict__ sig_in,
     const float* __restrict__ sig_out, uint32_t* stats, uint32_t* counter, const uint32_t* done,
@@ -1065,7 +1069,8 @@ __global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async
     constexpr uint32_t C = Scenes ? kSceneChunk : kChunk;
     static_assert(2 * C + 1 <= 32, "a chunk's row offsets fit one warp");
     constexpr unsigned kAll = 0xffffffffu;
-    static_assert(SE == 32 || SE == 64, "32 or 64 edges per stage");
+    static_assert(SE == 32 || SE == 64 || SE == 128, "32, 64 or 128 edges per stage");
+    static_assert(Lay::kBlockBytes >= 3 * kAsyncWarps * P * 4, "the statistics reuse the rings");
     static_assert(EPL % 4 == 0 && G == 8, "4 x 4 transpose blocks, 8 edge groups");
     static_assert(NST >= 2 && D >= 1, "pipeline depths");
     extern __shared__ __align__(16) unsigned char dyn[];
@@ -1435,8 +1440,8 @@ __global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async
     // ---- statistics: CTA max per column, one atomic per column -------------
     __syncthreads();  // every warp is done with its ring
     float* s_md = reinterpret_cast<float*>(dyn);
-    float* s_mb = s_md + kWarps * P;
-    float* s_mr = s_mb + kWarps * P;
+    float* s_mb = s_md + kAsyncWarps * P;
+    float* s_mr = s_mb + kAsyncWarps * P;
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
         s_md[warp * P + col0 + k] = md[k];
@@ -1446,7 +1451,7 @@ __global__ void __launch_bounds__(kWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async
     __syncthreads();
     for (int c = threadIdx.x; c < P; c += blockDim.x) {
         float a = 0.0f, b = 0.0f, r = 0.0f;
-        for (int w = 0; w < kWarps; ++w) {
+        for (int w = 0; w < kAsyncWarps; ++w) {
             a = fmaxf(a, s_md[w * P + c]);
             b = fmaxf(b, s_mb[w * P + c]);
             r = fmaxf(r, s_mr[w * P + c]);
@@ -1963,7 +1968,7 @@ int async_step_grid()
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         FCU_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, k_step_i8_async<64, Scenes>, kWarps * 32, bytes));
+            &per_sm, k_step_i8_async<64, Scenes>, kAsyncWarps * 32, bytes));
         return std::max(1, sms) * std::max(1, per_sm);
     }();
     return grid;
@@ -1996,11 +2001,11 @@ void launch_step_i8(int P, const GraphView& g, const PanelParams& pp, const int8
         break;
     case 64:
         if (use_async_step(P, g) && sc)
-            k_step_i8_async<64, true><<<async_step_grid<true>(), kWarps * 32,
+            k_step_i8_async<64, true><<<async_step_grid<true>(), kAsyncWarps * 32,
                                         AsyncLayout<64>::kBlockBytes, s>>>(
                 g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
         else if (use_async_step(P, g))
-            k_step_i8_async<64, false><<<async_step_grid<false>(), kWarps * 32,
+            k_step_i8_async<64, false><<<async_step_grid<false>(), kAsyncWarps * 32,
                                          AsyncLayout<64>::kBlockBytes, s>>>(
                 g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
         else if (sc)

@@ -15,12 +15,17 @@
 //     BF16 activations (hidden) or FP32 outputs.
 // Every wait is bounded (1 s): a wait that runs out sets the error flag,
 // waits once more (bounded) for the work in flight and frees the tensor
-// memory before the CTA exits.
+// memory before the CTA exits.  With FACETCU_TEST_STALL_TENSOR_WAIT=1 in the
+// environment (read at each call; for tests of that path) the load barrier
+// expects 16 bytes more than the loads deliver, so its wait runs out and
+// the call reports FACETCU_DEVICE_TIMEOUT.
 //
 // The input rows are BF16 padded to 64 features (128 bytes); the first
 // layer's weight matrix is padded the same way.  Hidden activations are
 // BF16 (the SIMT path of mlp.cu keeps FP32 activations; the difference is a
 // BF16 rounding per layer, ~1e-2 of the output scale).
+#include <cstdlib>
+
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -121,7 +126,7 @@ __global__ void __launch_bounds__(128) k_mlp_tc(const __grid_constant__ CUtensor
                                                 const __grid_constant__ CUtensorMap bmap,
                                                 const float* __restrict__ bias,
                                                 OutT* __restrict__ out, uint32_t n,
-                                                uint32_t* error)
+                                                uint32_t* error, uint32_t extra_tx)
 {
     static_assert(N % 32 == 0 && N <= kTmemCols && N >= 32, "N");
     static_assert(KS >= 1 && KS <= 4 * KB, "K steps");
@@ -156,7 +161,7 @@ __global__ void __launch_bounds__(128) k_mlp_tc(const __grid_constant__ CUtensor
     bool issued = false;
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar_load)),
-                     "r"(uint32_t(Lay::kA + Lay::kB))
+                     "r"(uint32_t(Lay::kA + Lay::kB) + extra_tx)
                      : "memory");
 #pragma unroll
         for (int kb = 0; kb < KB; ++kb) {
@@ -307,7 +312,7 @@ CUtensorMap tensor_map(const void* base, uint64_t cols, uint64_t rows, uint32_t 
 
 template <int N, int KB, int KS, bool kGelu, typename OutT>
 void layer(const CUtensorMap& a, const CUtensorMap& b, const float* bias, OutT* out, size_t n,
-           uint32_t* error, cudaStream_t s)
+           uint32_t* error, uint32_t extra_tx, cudaStream_t s)
 {
     auto kern = k_mlp_tc<N, KB, KS, kGelu, OutT>;
     constexpr int bytes = TcLayout<N, KB>::kBytes;
@@ -317,7 +322,7 @@ void layer(const CUtensorMap& a, const CUtensorMap& b, const float* bias, OutT* 
     }();
     (void)attr;
     const unsigned grid = unsigned((n + kTileM - 1) / kTileM);
-    kern<<<grid, 128, bytes, s>>>(a, b, bias, out, uint32_t(n), error);
+    kern<<<grid, 128, bytes, s>>>(a, b, bias, out, uint32_t(n), error, extra_tx);
     FCU_LAUNCH("k_mlp_tc");
 }
 
@@ -345,12 +350,14 @@ void infer_tensor(Net& net, const float* X, size_t n, TensorScratch& ts, float* 
     const CUtensorMap mw1 = tensor_map(w1p, kPadIn, kH, kH);
     const CUtensorMap mw2 = tensor_map(w + kOffW2, kH, kH, kH);
     const CUtensorMap mw3 = tensor_map(w + kOffW3, kH, kOut, kOut);
+    const char* stall = std::getenv("FACETCU_TEST_STALL_TENSOR_WAIT");
+    const uint32_t extra = stall && stall[0] == '1' ? 16u : 0u;
     // A1 = gelu(X W1^T + b1): one K step (12 features + 4 zeros)
-    layer<kH, 1, 1, true, __nv_bfloat16>(mx, mw1, p + kOffB1, a1, n, err, s);
+    layer<kH, 1, 1, true, __nv_bfloat16>(mx, mw1, p + kOffB1, a1, n, err, extra, s);
     // A2 = gelu(A1 W2^T + b2)
-    layer<kH, 2, 8, true, __nv_bfloat16>(m1, mw2, p + kOffB2, a2, n, err, s);
+    layer<kH, 2, 8, true, __nv_bfloat16>(m1, mw2, p + kOffB2, a2, n, err, extra, s);
     // Y = A2 W3^T + b3
-    layer<kOut, 2, 8, false, float>(m2, mw3, p + kOffB3, Y, n, err, s);
+    layer<kOut, 2, 8, false, float>(m2, mw3, p + kOffB3, Y, n, err, extra, s);
 }
 
 uint32_t tensor_error(TensorScratch& ts, cudaStream_t s)

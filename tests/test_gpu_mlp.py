@@ -210,3 +210,22 @@ def test_trained_warm_start_on_an_unseen_forest():
     case["model"].close()
     assert row["cold"]["max_rel_err"] <= 1e-4 and row["mlp"]["max_rel_err"] <= 1e-4
     assert row["mlp"]["iterations"] <= row["cold"]["iterations"] + 1, row
+
+
+def test_tensor_core_wait_times_out_and_context_survives(model, monkeypatch):
+    """A bounded wait that runs out: with the test switch set, the tensor
+    kernels' load barrier expects more bytes than arrive, each CTA's wait
+    gives up after 1 s, frees its tensor memory and raises the error flag,
+    and the call returns FACETCU_DEVICE_TIMEOUT; the next call, without the
+    switch, computes the right answer in the same context."""
+    rng = np.random.default_rng(11)
+    params = rng.normal(scale=0.15, size=M.COUNT).astype(np.float32)
+    model.mlpSetParameters(params)
+    x = rng.normal(size=(5, 12)).astype(np.float32)  # one CTA per layer
+    monkeypatch.setenv("FACETCU_TEST_STALL_TENSOR_WAIT", "1")
+    with pytest.raises(facetcu.FacetcuError) as err:
+        model.mlpForwardTensor(x)
+    assert err.value.code == facetcu.DEVICE_TIMEOUT
+    monkeypatch.delenv("FACETCU_TEST_STALL_TENSOR_WAIT")
+    y = model.mlpForwardTensor(x)
+    assert np.max(np.abs(y - M.forward_bf16_activations(params, x))) <= 5e-3 * max(1.0, np.abs(y).max())

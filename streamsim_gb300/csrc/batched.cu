@@ -1743,37 +1743,66 @@ __global__ void k_check(uint32_t* stats, uint32_t* flag, int P, float tol, uint3
     }
 }
 
-__device__ __forceinline__ uint32_t old_side(const uint32_t* order, uint32_t s)
+__device__ __forceinline__ uint32_t new_side(const uint32_t* rank, uint32_t so)
 {
-    return order ? 2u * order[s >> 1] + (s & 1u) : s;
+    return rank ? 2u * rank[so >> 1] + (so & 1u) : so;
 }
 
-// Panel parameters for columns [c0, c0 + P) (column c = sun * bands + band),
-// rows in solver order (order maps solver facet -> caller facet).
-__global__ void k_prepare_panel(uint32_t S, uint32_t bands, uint32_t R, uint32_t c0, int P,
-                                const uint32_t* order, const float* rho, const float* tau,
-                                const float* emis, const float* beam, const float* dgeo,
-                                float* prho, float* ptau, float* pemis, float* pdir)
+// The panel kernels move [R][S] arrays (caller side order, band-major) to
+// [S][P] panels (solver order) and back.  A block takes 32 consecutive
+// caller sides and 32 columns at a time: the band-major side reads and
+// writes are 128-byte rows, the panel side is one 128-byte row segment per
+// side (rank maps caller facet -> solver facet), transposed through a
+// shared tile.  Reading in solver order instead (one 4-byte element of a
+// different band row per thread) moved 8x the bytes once the inputs
+// outgrew L2.
+constexpr int kPanelTile = 32;
+
+// Panel parameters for columns [c0, c0 + P) (column c = sun * bands + band).
+__global__ void __launch_bounds__(256) k_prepare_panel(
+    uint32_t S, uint32_t bands, uint32_t R, uint32_t c0, int P, const uint32_t* rank,
+    const float* __restrict__ rho, const float* __restrict__ tau, const float* __restrict__ emis,
+    const float* __restrict__ beam, const float* __restrict__ dgeo, float* __restrict__ prho,
+    float* __restrict__ ptau, float* __restrict__ pemis, float* __restrict__ pdir)
 {
-    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= size_t(S) * P) return;
-    const uint32_t s = uint32_t(i / P);
-    const uint32_t j = uint32_t(i % P);
-    const uint32_t c = c0 + j;
-    if (c >= R) {
-        prho[i] = 0.0f;
-        ptau[i] = 0.0f;
-        pemis[i] = 0.0f;
-        pdir[i] = 0.0f;
-        return;
+    __shared__ float tile[4][kPanelTile][kPanelTile + 1];
+    __shared__ uint32_t dest[kPanelTile];
+    const uint32_t so0 = blockIdx.x * kPanelTile;
+    if (threadIdx.x < kPanelTile) {
+        const uint32_t so = so0 + threadIdx.x;
+        dest[threadIdx.x] = so < S ? new_side(rank, so) : 0u;
     }
-    const uint32_t so = old_side(order, s);
-    const uint32_t b = c % bands, k = c / bands;
-    const size_t bi = size_t(b) * S + so;
-    prho[i] = rho[bi];
-    ptau[i] = tau[bi];
-    pemis[i] = emis ? emis[bi] : 0.0f;
-    pdir[i] = dgeo ? beam[b] * dgeo[size_t(k) * S + so] : 0.0f;
+    for (int j0 = 0; j0 < P; j0 += kPanelTile) {
+        const int w = min(P - j0, kPanelTile);
+        __syncthreads();
+        for (int k = threadIdx.x; k < kPanelTile * w; k += blockDim.x) {
+            const int j = k / kPanelTile, ls = k % kPanelTile;
+            const uint32_t so = so0 + ls, c = c0 + j0 + j;
+            float r = 0.0f, t = 0.0f, e = 0.0f, d = 0.0f;
+            if (so < S && c < R) {
+                const uint32_t b = c % bands, kk = c / bands;
+                const size_t bi = size_t(b) * S + so;
+                r = rho[bi];
+                t = tau[bi];
+                e = emis ? emis[bi] : 0.0f;
+                d = dgeo ? beam[b] * dgeo[size_t(kk) * S + so] : 0.0f;
+            }
+            tile[0][ls][j] = r;
+            tile[1][ls][j] = t;
+            tile[2][ls][j] = e;
+            tile[3][ls][j] = d;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < kPanelTile * w; k += blockDim.x) {
+            const int ls = k / w, j = k % w;
+            if (so0 + ls >= S) continue;
+            const size_t o = size_t(dest[ls]) * P + j0 + j;
+            prho[o] = tile[0][ls][j];
+            ptau[o] = tile[1][ls][j];
+            pemis[o] = tile[2][ls][j];
+            pdir[o] = tile[3][ls][j];
+        }
+    }
 }
 
 __global__ void k_panel_sky(uint32_t bands, uint32_t R, uint32_t c0, int P, const float* sky,
@@ -1785,34 +1814,61 @@ __global__ void k_panel_sky(uint32_t bands, uint32_t R, uint32_t c0, int P, cons
     }
 }
 
-// [R][S] (caller order) -> [S][P] (solver order)
+// [R][S] (caller order) -> [S][P] (solver order); src null: zeros
 template <typename T>
-__global__ void k_panel_in(const float* src, uint32_t S, uint32_t R, uint32_t c0, int P,
-                           const uint32_t* order, T* dst)
+__global__ void __launch_bounds__(256) k_panel_in(const float* __restrict__ src, uint32_t S,
+                                                  uint32_t R, uint32_t c0, int P,
+                                                  const uint32_t* rank, T* __restrict__ dst)
 {
-    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= size_t(S) * P) return;
-    const uint32_t s = uint32_t(i / P), j = uint32_t(i % P), c = c0 + j;
-    dst[i] = (src && c < R) ? T(src[size_t(c) * S + old_side(order, s)]) : T(0);
+    __shared__ float tile[kPanelTile][kPanelTile + 1];
+    __shared__ uint32_t dest[kPanelTile];
+    const uint32_t so0 = blockIdx.x * kPanelTile;
+    if (threadIdx.x < kPanelTile) {
+        const uint32_t so = so0 + threadIdx.x;
+        dest[threadIdx.x] = so < S ? new_side(rank, so) : 0u;
+    }
+    for (int j0 = 0; j0 < P; j0 += kPanelTile) {
+        const int w = min(P - j0, kPanelTile);
+        __syncthreads();
+        for (int k = threadIdx.x; k < kPanelTile * w; k += blockDim.x) {
+            const int j = k / kPanelTile, ls = k % kPanelTile;
+            const uint32_t so = so0 + ls, c = c0 + j0 + j;
+            tile[ls][j] = (src && so < S && c < R) ? src[size_t(c) * S + so] : 0.0f;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < kPanelTile * w; k += blockDim.x) {
+            const int ls = k / w, j = k % w;
+            if (so0 + ls < S) dst[size_t(dest[ls]) * P + j0 + j] = T(tile[ls][j]);
+        }
+    }
 }
 
-// [S][P] (solver order) -> [R][S] (caller order), through a shared tile
+// [S][P] (solver order) -> [R][S] (caller order)
 template <typename T>
-__global__ void k_panel_out(const T* src, uint32_t S, uint32_t R, uint32_t c0, int P,
-                            const uint32_t* order, float* dst)
+__global__ void __launch_bounds__(256) k_panel_out(const T* __restrict__ src, uint32_t S,
+                                                   uint32_t R, uint32_t c0, int P,
+                                                   const uint32_t* rank, float* __restrict__ dst)
 {
-    __shared__ float tile[32][kMaxP + 1];
-    const uint32_t sb = blockIdx.x * 32;
-    for (int k = threadIdx.x; k < 32 * P; k += blockDim.x) {
-        const int ls = k / P, j = k % P;
-        const uint32_t s = sb + ls;
-        tile[ls][j] = s < S ? float(src[size_t(s) * P + j]) : 0.0f;
+    __shared__ float tile[kPanelTile][kPanelTile + 1];
+    __shared__ uint32_t from[kPanelTile];
+    const uint32_t so0 = blockIdx.x * kPanelTile;
+    if (threadIdx.x < kPanelTile) {
+        const uint32_t so = so0 + threadIdx.x;
+        from[threadIdx.x] = so < S ? new_side(rank, so) : 0u;
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < 32 * P; k += blockDim.x) {
-        const int j = k / 32, ls = k % 32;
-        const uint32_t s = sb + ls, c = c0 + j;
-        if (s < S && c < R) dst[size_t(c) * S + old_side(order, s)] = tile[ls][j];
+    for (int j0 = 0; j0 < P; j0 += kPanelTile) {
+        const int w = min(P - j0, kPanelTile);
+        __syncthreads();
+        for (int k = threadIdx.x; k < kPanelTile * w; k += blockDim.x) {
+            const int ls = k / w, j = k % w;
+            tile[ls][j] = so0 + ls < S ? float(src[size_t(from[ls]) * P + j0 + j]) : 0.0f;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < kPanelTile * w; k += blockDim.x) {
+            const int j = k / kPanelTile, ls = k % kPanelTile;
+            const uint32_t so = so0 + ls, c = c0 + j0 + j;
+            if (so < S && c < R) dst[size_t(c) * S + so] = tile[ls][j];
+        }
     }
 }
 
@@ -2243,7 +2299,8 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
     const size_t elem = fp64 ? 8 : 4;
     ensure_permuted(gr, p, ws, s);
     const bool perm = gr.perm_valid;
-    const uint32_t* order = perm ? gr.order.as<uint32_t>() : nullptr;
+    // caller facet -> solver facet, for the panel transposes
+    const uint32_t* rank = perm ? gr.rank.as<uint32_t>() : nullptr;
     GraphView g;
     g.rows = perm ? gr.p_rows.as<uint32_t>() : gr.row_offsets.as<uint32_t>();
     g.packed = perm ? gr.p_packed.as<uint32_t>()
@@ -2358,7 +2415,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
             }
         };
         launches += 4;  // prepare, sky, panel in, panel out
-        k_prepare_panel<<<blocks_for(cells, 256), 256, 0, s>>>(S, p.bands, R, c0, P, order, p.rho,
+        k_prepare_panel<<<blocks_for(S, kPanelTile), 256, 0, s>>>(S, p.bands, R, c0, P, rank, p.rho,
                                                                 p.tau, p.emis, p.beam, p.dgeo,
                                                                 prho, ptau, pemis, pdir);
         FCU_LAUNCH("k_prepare_panel");
@@ -2367,11 +2424,11 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
         FCU_CHECK(cudaMemsetAsync(stats, 0, (4 * kMaxP + 16) * 4, s));  // stats, flags, colmax
         const float* init = cfg.warm_start == FACETCU_WARM_GIVEN ? d_initial : nullptr;
         if (fp64)
-            k_panel_in<double><<<blocks_for(cells, 256), 256, 0, s>>>(
-                init, S, R, c0, P, order, reinterpret_cast<double*>(x0));
+            k_panel_in<double><<<blocks_for(S, kPanelTile), 256, 0, s>>>(
+                init, S, R, c0, P, rank, reinterpret_cast<double*>(x0));
         else
-            k_panel_in<float><<<blocks_for(cells, 256), 256, 0, s>>>(
-                init, S, R, c0, P, order, reinterpret_cast<float*>(x0));
+            k_panel_in<float><<<blocks_for(S, kPanelTile), 256, 0, s>>>(
+                init, S, R, c0, P, rank, reinterpret_cast<float*>(x0));
         FCU_LAUNCH("k_panel_in");
         // A solve from zero: its first sweep gathers nothing (null input).
         const bool zero_start = init == nullptr;
@@ -2594,11 +2651,11 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
         }
         const char* final_buf = cur ? x1 : x0;
         if (fp64)
-            k_panel_out<double><<<blocks_for(S, 32), 256, 0, s>>>(
-                reinterpret_cast<const double*>(final_buf), S, R, c0, P, order, d_out);
+            k_panel_out<double><<<blocks_for(S, kPanelTile), 256, 0, s>>>(
+                reinterpret_cast<const double*>(final_buf), S, R, c0, P, rank, d_out);
         else
-            k_panel_out<float><<<blocks_for(S, 32), 256, 0, s>>>(
-                reinterpret_cast<const float*>(final_buf), S, R, c0, P, order, d_out);
+            k_panel_out<float><<<blocks_for(S, kPanelTile), 256, 0, s>>>(
+                reinterpret_cast<const float*>(final_buf), S, R, c0, P, rank, d_out);
         FCU_LAUNCH("k_panel_out");
         worst_iterations = std::max(worst_iterations, host_flag[1]);
         float change;

@@ -196,6 +196,85 @@ __device__ __forceinline__ Acc gather_narrow(const GraphView& g, uint32_t s, con
     return acc;
 }
 
+// ---- 1- and 2-column panels: a group of 8P lanes per side -----------------
+// 8 edge lanes x P columns per side, so a warp holds 4/P sides (2/P facets)
+// at once: a row of 100-200 edges keeps each lane's U loads busy, and the
+// chain of dependent loads of a side (row offsets, edge words, neighbour
+// values, parameters) is paid once for several sides.  (One side per warp
+// left most of the 32 x U load slots empty and took ~7 dependent round
+// trips per facet.)
+// Warps take facet pairs round robin (pair w, w + W, ...): every warp sees
+// every part of the graph, so scenes with longer rows in a batch do not
+// load single warps (a contiguous range per warp did), and no counter.
+template <int P> struct NarrowGroup {
+    static_assert(P == 1 || P == 2, "1 or 2 columns");
+    static constexpr int kLanes = 8 * P;        // lanes per side
+    static constexpr int kFacets = 16 / kLanes;  // facets per warp pass
+};
+__device__ __forceinline__ void warp_pairs(uint32_t& first, uint32_t& stride)
+{
+    first = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    stride = gridDim.x * kWarps;
+}
+
+// An edge read once per sweep: a streaming load, so that the graph passing
+// through L2 does not evict the neighbour values the gathers hit there.
+__device__ __forceinline__ void edge_stream(const GraphView& g, uint32_t e, uint32_t& nb, float& c)
+{
+    if (g.packed) {
+        const uint32_t p = __ldcs(g.packed + e);
+        nb = p & ((1u << g.nb_bits) - 1u);
+        c = float(p >> g.nb_bits);
+    } else {
+        edge_at(g, e, nb, c);
+    }
+}
+
+template <int P, typename T, typename Acc>
+__device__ __forceinline__ Acc gather_group(const GraphView& g, uint32_t s, bool valid, const T* X,
+                                            int eg, int col)
+{
+    constexpr int U = FCU_NARROW_U;
+    Acc acc = 0;
+    if (valid) {
+        const uint32_t start = __ldg(g.rows + s), end = __ldg(g.rows + s + 1);
+        for (uint32_t e = start + uint32_t(eg); e < end; e += uint32_t(8 * U)) {
+            Acc v[U];
+            float c[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t idx = e + uint32_t(u * 8);
+                v[u] = 0;
+                c[u] = 0.0f;
+                if (idx < end) {
+                    uint32_t nb;
+                    edge_stream(g, idx, nb, c[u]);
+                    if constexpr (sizeof(Acc) == 8)
+                        v[u] = Acc(X[size_t(nb) * P + col]);
+                    else
+                        v[u] = Acc(load_as_float<T>(X + size_t(nb) * P + col));
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) acc += Acc(c[u]) * v[u];
+        }
+    }
+    // the sum over the side's 8 edge lanes (lanes eg * P + col of the group)
+#pragma unroll
+    for (int o = P; o < 8 * P; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    return acc;
+}
+
+// Fold the statistics of every lane of column c into lane c.
+__device__ __forceinline__ void fold_narrow_stats(float* md, float* mb, float* mr, int P)
+{
+    for (int o = P; o < 32; o <<= 1) {
+        md[0] = fmaxf(md[0], __shfl_xor_sync(0xffffffffu, md[0], o));
+        mb[0] = fmaxf(mb[0], __shfl_xor_sync(0xffffffffu, mb[0], o));
+        mr[0] = fmaxf(mr[0], __shfl_xor_sync(0xffffffffu, mr[0], o));
+    }
+}
+
 // ---- wide panels (P = 32, 64, 128) ---------------------------------------
 // Each lane moves 16 bytes of a neighbour row per load: CPL = 4 FP32 or 8
 // BF16 columns.  L = P / CPL lanes cover one row, so a warp gathers
@@ -242,11 +321,11 @@ __device__ __forceinline__ void edge_word(const uint32_t* __restrict__ packed,
                                           uint32_t nb_bits, uint32_t& nb, float& c)
 {
     if (packed) {
-        const uint32_t p = __ldg(packed + e);
+        const uint32_t p = __ldcs(packed + e);  // read once per sweep: evict first
         nb = p & ((1u << nb_bits) - 1u);
         c = float(p >> nb_bits);
     } else {
-        const uint2 w = __ldg(reinterpret_cast<const uint2*>(edges) + e);
+        const uint2 w = __ldcs(reinterpret_cast<const uint2*>(edges) + e);
         nb = w.x;
         c = float(w.y);
     }
@@ -1570,6 +1649,47 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep(GraphView g, PanelParams 
     const float fl = kSideFloor * pp.colmax[col];
     uint32_t fb, fe;
     warp_range(g.facets, fb, fe);
+    if constexpr (P <= 2) {
+        using NG = NarrowGroup<P>;
+        const int grp = lane / NG::kLanes, eg = (lane % NG::kLanes) / P;
+        uint32_t pair, stride;
+        warp_pairs(pair, stride);
+        for (; 2u * pair < g.facets; pair += stride)
+#pragma unroll
+        for (int q = 0; q < 2 / NG::kFacets; ++q) {
+            const uint32_t f = 2u * pair + uint32_t(q) + uint32_t(grp >> 1);
+            const bool valid = f < g.facets;
+            const uint32_t s = 2u * f + uint32_t(grp & 1);
+            const size_t i = size_t(s) * P + col;
+            // the side's own loads first, so that they overlap the gather
+            uint32_t d = 0u, sk = 0u;
+            Acc dir = 0, em = 0, rh = 0, ta = 0, o = 0;
+            if (valid) {
+                d = __ldcs(g.denom + s);
+                sk = __ldcs(g.skyc + s);
+                dir = Acc(__ldcs(pp.direct + i));
+                if (eg == 0) {
+                    em = Acc(__ldcs(pp.emis + i));
+                    rh = Acc(__ldcs(pp.rho + i));
+                    ta = Acc(__ldcs(pp.tau + i));
+                    o = Bin ? Bin[i] : Acc(0);
+                }
+            }
+            const Acc acc = Bin ? gather_group<P, T, Acc>(g, s, valid, Bin, eg, col) : Acc(0);
+            const Acc h = valid ? (d == 0u ? L : (Acc(sk) * L + acc) / Acc(d)) + dir : Acc(0);
+            const Acc ho = __shfl_xor_sync(0xffffffffu, h, NG::kLanes);  // the facet's other side
+            if (valid && eg == 0) {
+                const Acc b = em + rh * h + ta * ho;
+                Bout[i] = b;
+                md[0] = fmaxf(md[0], absf(b - o));
+                mb[0] = fmaxf(mb[0], absf(b));
+                mr[0] = fmaxf(mr[0], rel_change(float(b - o), float(b), fl));
+            }
+        }
+        fold_narrow_stats(md, mb, mr, P);
+        publish_stats<1>(md, mb, mr, lane, P, stats);
+        return;
+    }
     for (uint32_t f = fb; f < fe; ++f) {
         const uint32_t s0 = 2u * f, s1 = s0 + 1u;
         Acc h[2];
@@ -1611,6 +1731,46 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep_defect(GraphView g, Panel
     float md[1] = {0.0f}, mb[1] = {0.0f};
     uint32_t fb, fe;
     warp_range(g.facets, fb, fe);
+    if constexpr (P <= 2) {
+        using NG = NarrowGroup<P>;
+        const int grp = lane / NG::kLanes, eg = (lane % NG::kLanes) / P;
+        uint32_t pair, stride;
+        warp_pairs(pair, stride);
+        for (; 2u * pair < g.facets; pair += stride)
+#pragma unroll
+        for (int q = 0; q < 2 / NG::kFacets; ++q) {
+            const uint32_t f = 2u * pair + uint32_t(q) + uint32_t(grp >> 1);
+            const bool valid = f < g.facets;
+            const uint32_t s = 2u * f + uint32_t(grp & 1);
+            const size_t i = size_t(s) * P + col;
+            // the side's own loads first, so that they overlap the gather
+            uint32_t d = 0u;
+            float rh = 0.0f, ta = 0.0f, xo = 0.0f;
+            if (valid) {
+                d = __ldg(g.denom + s);
+                if (eg == 0) {
+                    rh = pp.rho[i];
+                    ta = pp.tau[i];
+                    xo = X[i];
+                }
+            }
+            const float acc = gather_group<P, __nv_bfloat16, float>(g, s, valid, Din, eg, col);
+            const float h = valid && d != 0u ? acc / float(d) : 0.0f;
+            const float ho = __shfl_xor_sync(0xffffffffu, h, NG::kLanes);
+            if (valid && eg == 0) {
+                const float dd = rh * h + ta * ho;
+                Dout[i] = __float2bfloat16_rn(dd);
+                const float x = xo + dd;
+                X[i] = x;
+                md[0] = fmaxf(md[0], fabsf(dd));
+                mb[0] = fmaxf(mb[0], fabsf(x));
+            }
+        }
+        float mr[1] = {0.0f};
+        fold_narrow_stats(md, mb, mr, P);
+        publish_stats<1>(md, mb, mr, lane, P, stats);
+        return;
+    }
     for (uint32_t f = fb; f < fe; ++f) {
         const uint32_t s0 = 2u * f, s1 = s0 + 1u;
         float h[2];

@@ -75,6 +75,27 @@ def block_stats(rows, neighbors, facet_rank, block=128, panel=64):
         "block_over_csr_hbm_bytes": blk_bytes / csr_bytes,
         "block_tensor_flops_per_sweep": float(blocks) * 2 * block * block * panel,
         "useful_flop_fraction": nnz / float(blocks * block * block),
+        # the hybrid layout: blocks above a fill threshold as dense BF16
+        # tiles on the tensor cores, the rest as the int8 CSR gather
+        "hybrid": {f"{t:g}": hybrid_split(counts, fill, t, block, panel, nnz)
+                   for t in (0.01, 0.05, 0.10)},
+    }
+
+
+def hybrid_split(counts, fill, threshold, block, panel, nnz):
+    """The blocks above `threshold` fill: how many, their share of the
+    nonzeros, the HBM bytes of their dense BF16 tiles against the 4-byte
+    CSR words of the same edges, and their tensor flops at `panel`
+    columns."""
+    sel = fill > threshold
+    n = int(sel.sum())
+    e = int(counts[sel].sum())
+    return {
+        "blocks": n,
+        "nonzero_share": e / float(nnz),
+        "tile_hbm_bytes": n * block * block * 2,
+        "csr_hbm_bytes_of_same_edges": e * 4,
+        "tensor_flops": float(n) * 2 * block * block * panel,
     }
 
 

@@ -89,6 +89,7 @@ struct GraphView {
     float* scene_cheb;                 // [scenes][4 kMaxP] Chebyshev state (weights at 2 kMaxP)
     uint32_t* scene_done;              // [scenes]
     uint32_t legacy_step;              // 1: 64-column int8 steps on the register-gather kernel
+    uint32_t counts8;                  // 1: every count is at most 255 (the solver's copy)
 };
 
 __device__ __forceinline__ void edge_at(const GraphView& g, uint32_t e, uint32_t& nb, float& c)
@@ -1050,7 +1051,8 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
 //   issue   — kAsyncStages - 1 stages ahead of consume: 16-byte cp.async
 //             copies (LDGSTS, L2 only) of the stage's neighbour rows into a
 //             ring of kAsyncStages stages in shared memory, and its counts
-//             (low bytes packed per dp4a word);
+//             (one byte each, packed per dp4a word: the kernel runs on the
+//             solver's graph copy, whose counts are split at 255);
 //   consume — 4 x 4 byte transposes and dp4a from shared memory; at a
 //             side's last stage the reduction and (odd side) the facet's
 //             epilogue.
@@ -1071,7 +1073,9 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
 // kernel 0.619 ms): 64-edge stages, 2 ring stages, 1 stage of lookahead
 // 0.527 ms; 2 of lookahead 0.608; 3 ring stages on 2 CTAs per SM 0.636;
 // 32-edge stages with 4 ring stages 0.622 (their per-stage bookkeeping
-// doubled the instructions per edge).
+// doubled the instructions per edge); 64-edge stages with 4 warps per CTA
+// (6 CTAs per SM) 0.529; 128-edge stages with 4 or 2 warps 0.588-0.590
+// (a 183-edge mean row fills 72 % of two 128-edge stages).
 #ifndef FCU_ASYNC_STAGES
 #define FCU_ASYNC_STAGES 2
 #endif
@@ -1097,10 +1101,9 @@ constexpr int pow2_at_least(int n) { return n <= 1 ? 1 : 2 * pow2_at_least((n + 
 template <int P>
 struct AsyncLayout {
     static constexpr int kStageBytes = kStageEdges * P;  // int8 rows of one stage
-    // a stage's counts: the low bytes packed for the dp4a (one byte per
-    // edge), a flag word (any count above 255) and the full counts for that
-    // case
-    static constexpr int kCountBytes = kStageEdges + 16 + kStageEdges * 4;
+    // a stage's counts, one byte per edge packed for the dp4a (the solver's
+    // graph copy holds no count above 255)
+    static constexpr int kCountBytes = kStageEdges;
     // descriptor slots (a power of two, at least stages + lookahead)
     static constexpr int kDesc = pow2_at_least(kAsyncStages + kLookahead);
     // per warp: the row ring, the counts of each ring stage, the descriptors
@@ -1335,24 +1338,13 @@ __global__ void __launch_bounds__(kAsyncWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_
         if (issued < requested) {
             const int slot = int(issued % NST);
             const uint32_t n = nf[0];
-            uint32_t nb[WPL], c[WPL];
-            uint32_t cmax = 0u;
+            uint32_t nb[WPL];
+            unsigned char* cs = cnt_s + slot * Lay::kCountBytes;
 #pragma unroll
             for (int j = 0; j < WPL; ++j) {
                 nb[j] = wf[0][j] & nb_mask;
-                c[j] = wf[0][j] >> g.nb_bits;
-                cmax |= c[j];
+                cs[j * 32 + cnt_byte] = static_cast<unsigned char>(wf[0][j] >> g.nb_bits);
             }
-            unsigned char* cs = cnt_s + slot * Lay::kCountBytes;
-#pragma unroll
-            for (int j = 0; j < WPL; ++j) cs[j * 32 + cnt_byte] = static_cast<unsigned char>(c[j] & 255u);
-            const bool high = __any_sync(kAll, cmax > 255u);
-            if (high) {
-#pragma unroll
-                for (int j = 0; j < WPL; ++j)
-                    reinterpret_cast<uint32_t*>(cs + SE + 16)[j * 32 + lane] = c[j];
-            }
-            if (lane == 0) reinterpret_cast<uint32_t*>(cs + SE)[0] = high ? 1u : 0u;
             unsigned char* dst = ring + slot * Lay::kStageBytes + sub * 16;
 #pragma unroll
             for (int k = 0; k < CPL; ++k) {
@@ -1378,50 +1370,24 @@ __global__ void __launch_bounds__(kAsyncWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_
         const uint4 mt = meta[consumed & (NQ - 1)];
         const unsigned char* cs = cnt_s + slot * Lay::kCountBytes;
         const uint4* rows = reinterpret_cast<const uint4*>(ring + slot * Lay::kStageBytes);
-        // The stage's products; a stage holding a count above 255 (about
-        // 1 in 10^4 on the forests) takes a second copy of the loop that adds
-        // the counts' higher bytes.  (Testing the flag inside the loop, per
-        // 4 x 4 block, cost 6 % of the step.)
-        auto products = [&](auto high_tag) {
-            constexpr bool kHigh = decltype(high_tag)::value;
 #pragma unroll
-            for (int blk = 0; blk < EPL / 4; ++blk) {
-                uint4 q[4];
+        for (int blk = 0; blk < EPL / 4; ++blk) {
+            uint4 q[4];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) q[k] = rows[((blk * 4 + k) * G + grp) * L + sub];
-                const uint32_t lo = reinterpret_cast<const uint32_t*>(cs)[blk * G + grp];
-                const uint32_t e0[4] = {q[0].x, q[0].y, q[0].z, q[0].w};
-                const uint32_t e1[4] = {q[1].x, q[1].y, q[1].z, q[1].w};
-                const uint32_t e2[4] = {q[2].x, q[2].y, q[2].z, q[2].w};
-                const uint32_t e3[4] = {q[3].x, q[3].y, q[3].z, q[3].w};
+            for (int k = 0; k < 4; ++k) q[k] = rows[((blk * 4 + k) * G + grp) * L + sub];
+            const uint32_t lo = reinterpret_cast<const uint32_t*>(cs)[blk * G + grp];
+            const uint32_t e0[4] = {q[0].x, q[0].y, q[0].z, q[0].w};
+            const uint32_t e1[4] = {q[1].x, q[1].y, q[1].z, q[1].w};
+            const uint32_t e2[4] = {q[2].x, q[2].y, q[2].z, q[2].w};
+            const uint32_t e3[4] = {q[3].x, q[3].y, q[3].z, q[3].w};
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    uint32_t t[4];
-                    transpose4(e0[i], e1[i], e2[i], e3[i], t);
+            for (int i = 0; i < 4; ++i) {
+                uint32_t t[4];
+                transpose4(e0[i], e1[i], e2[i], e3[i], t);
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        acc[4 * i + k] = dp4a_su(t[k], lo, acc[4 * i + k]);
-                    if constexpr (kHigh) {
-                        const uint32_t* cf = reinterpret_cast<const uint32_t*>(cs + SE + 16);
-                        const int c0 = int(cf[(blk * 4) * G + grp]),
-                                  c1 = int(cf[(blk * 4 + 1) * G + grp]),
-                                  c2 = int(cf[(blk * 4 + 2) * G + grp]),
-                                  c3 = int(cf[(blk * 4 + 3) * G + grp]);
-#pragma unroll 1
-                        for (int sh = 8; sh < 32; sh += 8) {
-                            const uint32_t cb = pack_bytes(c0, c1, c2, c3, sh);
-#pragma unroll
-                            for (int k = 0; k < 4; ++k)
-                                acc[4 * i + k] += int(uint32_t(dp4a_su(t[k], cb, 0)) << sh);
-                        }
-                    }
-                }
+                for (int k = 0; k < 4; ++k) acc[4 * i + k] = dp4a_su(t[k], lo, acc[4 * i + k]);
             }
-        };
-        if (reinterpret_cast<const uint32_t*>(cs + SE)[0] != 0u)
-            products(std::true_type{});
-        else
-            products(std::false_type{});
+        }
         ++consumed;
         if (!mt.y) return;
         // the side's last stage: sums, then (odd side) the facet's update
@@ -2053,16 +2019,33 @@ __global__ void k_rank(const uint32_t* order, uint32_t facets, uint32_t* rank)
     if (i < facets) rank[order[i]] = i;
 }
 
+// The solver's copy of the graph splits every edge whose count is above 255
+// into edges of at most 255 to the same neighbour (255, 255, ..., the rest),
+// adjacent in the row: the int8 step's dp4a then takes every count as one
+// byte.  Its integer sums are the same; the FP32 and FP64 sweeps add the
+// pieces one by one.  (The forests hold about one such edge in 10^6.)
+__device__ __forceinline__ uint32_t count_pieces(uint32_t c) { return c > 255u ? (c + 254u) / 255u : 1u; }
+
+// One warp per renumbered side: its row length in pieces, denominator and
+// sky count.
 __global__ void k_perm_lengths(const uint32_t* order, uint32_t S, const uint32_t* rows,
-                               const uint32_t* denom, const uint32_t* sky, uint32_t* len,
-                               uint32_t* pden, uint32_t* psky)
+                               const uint32_t* packed, uint32_t nb_bits, const uint32_t* denom,
+                               const uint32_t* sky, uint32_t* len, uint32_t* pden, uint32_t* psky)
 {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (s >= S) return;
     const uint32_t so = 2u * order[s >> 1] + (s & 1u);
-    len[s] = rows[so + 1] - rows[so];
-    pden[s] = denom[so];
-    psky[s] = sky[so];
+    const uint32_t b = rows[so], n = rows[so + 1] - b;
+    uint32_t k = 0;
+    for (uint32_t i = lane; i < n; i += 32) k += count_pieces(packed[b + i] >> nb_bits);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+    if (lane == 0) {
+        len[s] = k;
+        pden[s] = denom[so];
+        psky[s] = sky[so];
+    }
 }
 
 // The scene of each renumbered facet.
@@ -2073,6 +2056,8 @@ __global__ void k_perm_scene(const uint32_t* __restrict__ order, const uint16_t*
     if (f < F) out[f] = scene[order[f]];
 }
 
+// One warp per renumbered side: its edges with neighbours renumbered and
+// counts above 255 split (the pieces' places from a scan over the lanes).
 __global__ void k_perm_copy(const uint32_t* order, const uint32_t* rank, uint32_t S,
                             const uint32_t* rows, const uint32_t* packed, const uint32_t* prows,
                             uint32_t* ppacked, uint32_t nb_bits)
@@ -2082,12 +2067,30 @@ __global__ void k_perm_copy(const uint32_t* order, const uint32_t* rank, uint32_
     const int lane = threadIdx.x & 31;
     if (s >= S) return;
     const uint32_t so = 2u * order[s >> 1] + (s & 1u);
-    const uint32_t b = rows[so], n = rows[so + 1] - b, pb = prows[s];
-    for (uint32_t i = lane; i < n; i += 32) {
-        const uint32_t p = packed[b + i];
-        const uint32_t nb = p & mask;
-        const uint32_t nn = 2u * rank[nb >> 1] + (nb & 1u);
-        ppacked[pb + i] = nn | (p & ~mask);
+    const uint32_t b = rows[so], n = rows[so + 1] - b;
+    uint32_t out = prows[s];
+    for (uint32_t i0 = 0; i0 < n; i0 += 32) {
+        const uint32_t i = i0 + uint32_t(lane);
+        uint32_t nn = 0u, c = 0u, k = 0u;
+        if (i < n) {
+            const uint32_t p = packed[b + i];
+            const uint32_t nb = p & mask;
+            nn = 2u * rank[nb >> 1] + (nb & 1u);
+            c = p >> nb_bits;
+            k = count_pieces(c);
+        }
+        uint32_t incl = k;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const uint32_t first = out + incl - k;
+        for (uint32_t j = 0; j < k; ++j) {
+            const uint32_t cj = j + 1u < k ? 255u : c - 255u * (k - 1u);
+            ppacked[first + j] = nn | (cj << nb_bits);
+        }
+        out += __shfl_sync(0xffffffffu, incl, 31);
     }
 }
 
@@ -2206,7 +2209,8 @@ int async_step_grid()
 
 bool use_async_step(int P, const GraphView& g)
 {
-    return FCU_STEP_ASYNC && P == 64 && g.packed != nullptr && g.legacy_step == 0u;
+    return FCU_STEP_ASYNC && P == 64 && g.packed != nullptr && g.counts8 != 0u &&
+           g.legacy_step == 0u;
 }
 
 // parity: the step's index modulo 2 (its input scales are slot `parity`,
@@ -2374,15 +2378,21 @@ void ensure_permuted(DeviceGraph& gr, const BatchProblem& p, Workspace& ws, cuda
     uint32_t* prows = static_cast<uint32_t*>(gr.p_rows.reserve((size_t(S) + 1) * 4));
     uint32_t* pden = static_cast<uint32_t*>(gr.p_denom.reserve(size_t(S) * 4));
     uint32_t* psky = static_cast<uint32_t*>(gr.p_sky.reserve(size_t(S) * 4));
-    uint32_t* ppk = static_cast<uint32_t*>(gr.p_packed.reserve(gr.nnz * 4 + 4));
-    k_perm_lengths<<<blocks_for(S, 256), 256, 0, s>>>(order, S, gr.row_offsets.as<uint32_t>(),
-                                                       gr.denominators.as<uint32_t>(),
-                                                       gr.sky.as<uint32_t>(), prows, pden, psky);
+    k_perm_lengths<<<blocks_for(size_t(S) * 32, 256), 256, 0, s>>>(
+        order, S, gr.row_offsets.as<uint32_t>(), gr.packed.as<uint32_t>(), gr.nb_bits,
+        gr.denominators.as<uint32_t>(), gr.sky.as<uint32_t>(), prows, pden, psky);
     FCU_LAUNCH("k_perm_lengths");
     unsigned long long* total = static_cast<unsigned long long*>(ws.e.reserve(64));
     exclusive_scan_u32(prows, prows, S, total, ws, s);
     k_set_last<<<1, 1, 0, s>>>(prows, S, total);
     FCU_LAUNCH("k_set_last");
+    unsigned long long split_nnz = 0;
+    FCU_CHECK(cudaMemcpyAsync(&split_nnz, total, 8, cudaMemcpyDeviceToHost, s));
+    FCU_CHECK(cudaStreamSynchronize(s));
+    if (split_nnz > 0xffffffffull)
+        throw Error(FACETCU_OVERFLOW_ERROR, "the solver's graph copy exceeds 2^32 edges");
+    gr.p_nnz = size_t(split_nnz);
+    uint32_t* ppk = static_cast<uint32_t*>(gr.p_packed.reserve(gr.p_nnz * 4 + 4));
     k_perm_copy<<<blocks_for(size_t(S) * 32, 256), 256, 0, s>>>(
         order, rank, S, gr.row_offsets.as<uint32_t>(), gr.packed.as<uint32_t>(), prows, ppk,
         gr.nb_bits);
@@ -2492,6 +2502,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
     g.scene_cheb = nullptr;
     g.scene_done = nullptr;
     g.legacy_step = (cfg.flags & FACETCU_BATCH_LEGACY_STEP) != 0u ? 1u : 0u;
+    g.counts8 = perm ? 1u : 0u;
     if (FCU_SCENE_SKIP && perm && mixed && gr.p_scene.ptr && gr.p_scene.bytes >= size_t(S / 2u) * 2 &&
         gr.scene_facets.size() >= 3) {
         // scene batch: converged scenes leave the int8 steps

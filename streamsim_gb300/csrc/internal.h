@@ -148,6 +148,7 @@ struct DeviceGraph {
     DeviceBuffer order;         // new facet -> old facet
     DeviceBuffer rank;          // old facet -> new facet
     DeviceBuffer p_rows, p_packed, p_denom, p_sky;
+    size_t p_nnz = 0;           // edges of the copy (counts above 255 split)
     // Scene batches: the first facet of every scene and the total (empty for
     // one scene); with the Morton copy, the scene of each renumbered facet.
     std::vector<uint32_t> scene_facets;

@@ -312,7 +312,10 @@ def test_pipelined_int8_step_bit_identical(kind):
     radiosity must be the same bits and the sweep counts the same; the
     result meets the 1e-4 bar against FP64.  Both graphs have empty rows
     (downward soil sides); the coarse soil (2.5 m quads under low leaves)
-    has counts above 255, the high-byte path of the dp4a sums."""
+    has counts above 255, which the solver's copy of the graph splits into
+    edges of at most 255 (the pipelined step takes every count as one
+    byte; the register-gather kernel, run on the same copy, adds high bytes
+    when a count has them)."""
     if kind == "forest":
         sc = scenes.forest(6, 20.0, 2000, 3, name="step")
     else:

@@ -891,7 +891,7 @@ def run_c3(args, rank, world, local):
         "speedup_vs_batched_fp32": fp32_s / step_s,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None,
-                     "kernel": "k_step_i8_async<64>" if args.panel_width == 64 else "k_step_i8<128>",
+                     "kernel": f"k_step_i8_async<{args.panel_width if args.panel_width in (64, 128) else 128}>",
                      "launches_timed": rt["timed_sweeps"],
                      "avg_launch_ms": rt["sweep_seconds"] / max(rt["timed_sweeps"], 1) * 1e3},
         "e2e": None, "gpu_launches": int(res["kernel_launches"]), "clocks": clocks,

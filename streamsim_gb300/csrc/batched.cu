@@ -1091,7 +1091,15 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
 #ifndef FCU_ASYNC_WARPS
 #define FCU_ASYNC_WARPS 8
 #endif
-constexpr int kAsyncWarps = FCU_ASYNC_WARPS;  // warps per CTA of the pipelined step
+constexpr int kAsyncWarps = FCU_ASYNC_WARPS;  // warps per CTA of the pipelined step (64 columns)
+// At 128 columns a stage holds 8 KB of rows: 4 warps per CTA keep the
+// shared memory per SM (3 CTAs) at the 64-column kernel's.
+#ifndef FCU_ASYNC_WARPS_128
+#define FCU_ASYNC_WARPS_128 4
+#endif
+template <int P> struct AsyncWarps {
+    static constexpr int value = P == 128 ? FCU_ASYNC_WARPS_128 : kAsyncWarps;
+};
 constexpr int kAsyncStages = FCU_ASYNC_STAGES;
 constexpr int kLookahead = FCU_ASYNC_LOOKAHEAD;
 constexpr int kStageEdges = FCU_ASYNC_EDGES;  // 32, 64 or 128 edges per stage
@@ -1108,7 +1116,7 @@ struct AsyncLayout {
     static constexpr int kDesc = pow2_at_least(kAsyncStages + kLookahead);
     // per warp: the row ring, the counts of each ring stage, the descriptors
     static constexpr int kWarpBytes = kAsyncStages * (kStageBytes + kCountBytes) + kDesc * 16;
-    static constexpr int kBlockBytes = kAsyncWarps * kWarpBytes;
+    static constexpr int kBlockBytes = AsyncWarps<P>::value * kWarpBytes;
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p)
@@ -1135,13 +1143,14 @@ __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes)
 }
 
 template <int P, bool Scenes>
-__global__ void __launch_bounds__(kAsyncWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_async(
+__global__ void __launch_bounds__(AsyncWarps<P>::value * 32, FCU_ASYNC_BLOCKS) k_step_i8_async(
     GraphView g, PanelParams pp, const int8_t* __restrict__ Qin, int8_t* __restrict__ Qout,
     float* __restrict__ X, float* __restrict__ R, const float* __restrict__ sig_in,
     const float* __restrict__ sig_out, uint32_t* stats, uint32_t* counter, const uint32_t* done,
     const float* __restrict__ scene_sig_in, const float* __restrict__ scene_sig_out)
 {
-    static_assert(P == 64, "the pipelined step covers 64-column panels");
+    static_assert(P == 64 || P == 128, "the pipelined step covers 64- and 128-column panels");
+    constexpr int W = AsyncWarps<P>::value;
     using Lay = AsyncLayout<P>;
     constexpr int L = P / 16, G = 32 / L, NC = P / 32;
     constexpr int SE = kStageEdges;
@@ -1153,8 +1162,8 @@ __global__ void __launch_bounds__(kAsyncWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_
     static_assert(2 * C + 1 <= 32, "a chunk's row offsets fit one warp");
     constexpr unsigned kAll = 0xffffffffu;
     static_assert(SE == 32 || SE == 64 || SE == 128, "32, 64 or 128 edges per stage");
-    static_assert(Lay::kBlockBytes >= 3 * kAsyncWarps * P * 4, "the statistics reuse the rings");
-    static_assert(EPL % 4 == 0 && G == 8, "4 x 4 transpose blocks, 8 edge groups");
+    static_assert(Lay::kBlockBytes >= 3 * W * P * 4, "the statistics reuse the rings");
+    static_assert(EPL % 4 == 0 && (G == 8 || G == 4), "4 x 4 transpose blocks, 8 or 4 edge groups");
     static_assert(NST >= 2 && D >= 1, "pipeline depths");
     extern __shared__ __align__(16) unsigned char dyn[];
     if (*done) return;
@@ -1329,10 +1338,10 @@ __global__ void __launch_bounds__(kAsyncWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_
     // Issue the oldest requested stage (front of the queue): its counts and
     // row copies into ring slot issued % NST, as one copy group.
     // Edge e = k * G + grp of a stage is the k-th edge of lane group grp:
-    // its count's low byte goes to byte k % 4 of word (k / 4) * G + grp, the
-    // word one dp4a of that group uses.  Lane l holds edges j * 32 + l, so
-    // k = 4 j + l / G.
-    const int cnt_byte = (lane % G) * 4 + lane / G;
+    // its count goes to byte k % 4 of word (k / 4) * G + grp, the word one
+    // dp4a of that group uses.  Lane l holds edges j * 32 + l, so
+    // k = (32 / G) j + l / G and the byte is 32 j + cnt_byte (G = 8 or 4).
+    const int cnt_byte = 4 * G * ((lane / G) / 4) + 4 * (lane % G) + (lane / G) % 4;
     const unsigned char* qsrc = reinterpret_cast<const unsigned char*>(Qin) + sub * 16;
     auto issue = [&]() {
         if (issued < requested) {
@@ -1348,8 +1357,8 @@ __global__ void __launch_bounds__(kAsyncWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_
             unsigned char* dst = ring + slot * Lay::kStageBytes + sub * 16;
 #pragma unroll
             for (int k = 0; k < CPL; ++k) {
-                const int row = k * G + grp;  // row / 32 == k / 4
-                const uint32_t rn = __shfl_sync(kAll, nb[k / 4], row & 31);
+                const int row = k * G + grp;  // row / 32 == k G / 32
+                const uint32_t rn = __shfl_sync(kAll, nb[(k * G) / 32], row & 31);
                 if (uint32_t(row) < n) cp_async16(dst + row * P, qsrc + size_t(rn) * P);
             }
             ++issued;
@@ -1499,8 +1508,8 @@ __global__ void __launch_bounds__(kAsyncWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_
     // ---- statistics: CTA max per column, one atomic per column -------------
     __syncthreads();  // every warp is done with its ring
     float* s_md = reinterpret_cast<float*>(dyn);
-    float* s_mb = s_md + kAsyncWarps * P;
-    float* s_mr = s_mb + kAsyncWarps * P;
+    float* s_mb = s_md + W * P;
+    float* s_mr = s_mb + W * P;
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
         s_md[warp * P + col0 + k] = md[k];
@@ -1510,7 +1519,7 @@ __global__ void __launch_bounds__(kAsyncWarps * 32, FCU_ASYNC_BLOCKS) k_step_i8_
     __syncthreads();
     for (int c = threadIdx.x; c < P; c += blockDim.x) {
         float a = 0.0f, b = 0.0f, r = 0.0f;
-        for (int w = 0; w < kAsyncWarps; ++w) {
+        for (int w = 0; w < W; ++w) {
             a = fmaxf(a, s_md[w * P + c]);
             b = fmaxf(b, s_mb[w * P + c]);
             r = fmaxf(r, s_mr[w * P + c]);
@@ -2188,29 +2197,43 @@ int step_grid()
     return grid;
 }
 
-// The pipelined 64-column step: its dynamic shared memory is opted in once
-// (before any graph capture) and the grid sized for it.
-template <bool Scenes>
+// The pipelined step: its dynamic shared memory is opted in once (before
+// any graph capture) and the grid sized for it.
+template <int P, bool Scenes>
 int async_step_grid()
 {
     static const int grid = [] {
-        constexpr int bytes = AsyncLayout<64>::kBlockBytes;
-        FCU_CHECK(cudaFuncSetAttribute(k_step_i8_async<64, Scenes>,
+        constexpr int bytes = AsyncLayout<P>::kBlockBytes;
+        FCU_CHECK(cudaFuncSetAttribute(k_step_i8_async<P, Scenes>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         FCU_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, k_step_i8_async<64, Scenes>, kAsyncWarps * 32, bytes));
+            &per_sm, k_step_i8_async<P, Scenes>, AsyncWarps<P>::value * 32, bytes));
         return std::max(1, sms) * std::max(1, per_sm);
     }();
     return grid;
 }
 
+template <int P, bool Scenes>
+void launch_async_step(const GraphView& g, const PanelParams& pp, const int8_t* qin, int8_t* qout,
+                       float* X, float* R, const float* sin, const float* sout, uint32_t* stats,
+                       uint32_t* counter, const uint32_t* done, const float* ssin,
+                       const float* ssout, cudaStream_t s)
+{
+    k_step_i8_async<P, Scenes><<<async_step_grid<P, Scenes>(), AsyncWarps<P>::value * 32,
+                                 AsyncLayout<P>::kBlockBytes, s>>>(
+        g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
+}
+
+#ifndef FCU_STEP_ASYNC_128
+#define FCU_STEP_ASYNC_128 1
+#endif
 bool use_async_step(int P, const GraphView& g)
 {
-    return FCU_STEP_ASYNC && P == 64 && g.packed != nullptr && g.counts8 != 0u &&
-           g.legacy_step == 0u;
+    return FCU_STEP_ASYNC && (P == 64 || (P == 128 && FCU_STEP_ASYNC_128)) &&
+           g.packed != nullptr && g.counts8 != 0u && g.legacy_step == 0u;
 }
 
 // parity: the step's index modulo 2 (its input scales are slot `parity`,
@@ -2235,13 +2258,11 @@ void launch_step_i8(int P, const GraphView& g, const PanelParams& pp, const int8
         break;
     case 64:
         if (use_async_step(P, g) && sc)
-            k_step_i8_async<64, true><<<async_step_grid<true>(), kAsyncWarps * 32,
-                                        AsyncLayout<64>::kBlockBytes, s>>>(
-                g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
+            launch_async_step<64, true>(g, pp, qin, qout, X, R, sin, sout, stats, counter, done,
+                                        ssin, ssout, s);
         else if (use_async_step(P, g))
-            k_step_i8_async<64, false><<<async_step_grid<false>(), kAsyncWarps * 32,
-                                         AsyncLayout<64>::kBlockBytes, s>>>(
-                g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
+            launch_async_step<64, false>(g, pp, qin, qout, X, R, sin, sout, stats, counter, done,
+                                         ssin, ssout, s);
         else if (sc)
             k_step_i8<64, true><<<step_grid<64, true>(), kWarps * 32, 0, s>>>(
                 g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
@@ -2250,7 +2271,13 @@ void launch_step_i8(int P, const GraphView& g, const PanelParams& pp, const int8
                 g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
         break;
     default:
-        if (sc)
+        if (use_async_step(128, g) && sc)
+            launch_async_step<128, true>(g, pp, qin, qout, X, R, sin, sout, stats, counter, done,
+                                         ssin, ssout, s);
+        else if (use_async_step(128, g))
+            launch_async_step<128, false>(g, pp, qin, qout, X, R, sin, sout, stats, counter,
+                                          done, ssin, ssout, s);
+        else if (sc)
             k_step_i8<128, true><<<step_grid<128, true>(), kWarps * 32, 0, s>>>(
                 g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
         else
@@ -2324,10 +2351,15 @@ cudaGraphExec_t step_graph(BatchState& st, const StepGraphKey& key)
     case 64:
         step_grid<64, false>();
         step_grid<64, true>();
-        async_step_grid<false>();
-        async_step_grid<true>();
+        async_step_grid<64, false>();
+        async_step_grid<64, true>();
         break;
-    default: step_grid<128, false>(); step_grid<128, true>(); break;
+    default:
+        step_grid<128, false>();
+        step_grid<128, true>();
+        async_step_grid<128, false>();
+        async_step_grid<128, true>();
+        break;
     }
     cudaGraph_t graph = nullptr;
     FCU_CHECK(cudaStreamBeginCapture(key.stream, cudaStreamCaptureModeThreadLocal));

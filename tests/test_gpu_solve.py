@@ -304,13 +304,16 @@ def test_autotune_panel_width_and_cache(c1, tmp_path):
     fresh.close()
 
 
-@pytest.mark.parametrize("kind", ["forest", "coarse_soil"])
-def test_pipelined_int8_step_bit_identical(kind):
+@pytest.mark.parametrize("kind,suns", [("forest", 1), ("coarse_soil", 1), ("forest", 2),
+                                       ("coarse_soil", 2)])
+def test_pipelined_int8_step_bit_identical(kind, suns):
     """The 64-column int8 step runs as an asynchronous-copy pipeline (rows
     staged in shared memory by cp.async); FACETCU_BATCH_LEGACY_STEP runs the
     register-gather kernel instead.  Both sum exactly in int32, so the
     radiosity must be the same bits and the sweep counts the same; the
-    result meets the 1e-4 bar against FP64.  Both graphs have empty rows
+    result meets the 1e-4 bar against FP64.  With two suns the 128 columns
+    run as one 128-column panel (the pipelined kernel's 4-group layout).
+    Both graphs have empty rows
     (downward soil sides); the coarse soil (2.5 m quads under low leaves)
     has counts above 255, which the solver's copy of the graph splits into
     edges of at most 255 (the pipelined step takes every count as one
@@ -333,6 +336,10 @@ def test_pipelined_int8_step_bit_identical(kind):
     if kind == "coarse_soil":
         assert 255 < counts.max() < 1024  # packed graph, counts above one byte
     rho, tau, dgeo, sky, beam = _bands(sc, lit, sun, 64)
+    if suns == 2:
+        sun2 = scenes.sun_direction(55.0, 250.0)
+        lit2 = m.hemisphereSunlit(sun2, suv, 256, 32)
+        dgeo = np.vstack([dgeo, scenes.direct_geometry(sc, lit2, sun2)[None, :]])
     a, ra = m.solveBatched(rho, tau, sky, beam, dgeo, precision=facetcu.PRECISION_MIXED,
                            tolerance=1e-6)
     b, rb = m.solveBatched(rho, tau, sky, beam, dgeo, precision=facetcu.PRECISION_MIXED,
@@ -344,3 +351,42 @@ def test_pipelined_int8_step_bit_identical(kind):
                               tolerance=1e-12, maximum_iterations=4000)
     assert rel_err(a, truth) < 1e-4
     m.close()
+
+
+def test_pipelined_scene_step_128_columns_bit_identical():
+    """A scene batch solved on 128-column panels (64 bands x 2 suns): the
+    pipelined step with per-scene scales and stops gives the same bits as
+    the register-gather kernel, and meets the 1e-4 bar against FP64."""
+    parts = [scenes.row_crops(5000, 7), scenes.urban(8000, 8), scenes.config1(9, 600, 10)]
+    uv, dirs = scenes.hemisphere_samples(128, 8, seed=7)
+    suv, _ = scenes.hemisphere_samples(64, 8, seed=8)
+    models, rho, tau, dgeo = [], [], [], []
+    for i, sc in enumerate(parts):
+        m = model_for(sc.vertices, 256, 64)
+        m.buildHemisphereGraph(uv, dirs, 128, 64, 8)
+        rows = []
+        for sun in (scenes.sun_direction(25.0 + 10 * i, 30.0 * i),
+                    scenes.sun_direction(50.0, 200.0 + 20 * i)):
+            rows.append(scenes.direct_geometry(sc, m.hemisphereSunlit(sun, suv, 64, 8), sun))
+        dgeo.append(np.stack(rows))
+        r, t = scenes.band_optics(sc, 64)
+        rho.append(r)
+        tau.append(t)
+        models.append(m)
+    batch = facetcu.FacetrtCuda()
+    batch.initialize(16, 16, 8)
+    batch.sceneBatch(models)
+    cat = lambda xs: np.ascontiguousarray(np.concatenate(xs, axis=-1))
+    args = (cat(rho), cat(tau), np.full(64, 100.0, np.float32), np.full(64, 800.0, np.float32),
+            cat(dgeo))
+    out, res = batch.solveBatched(*args, precision=facetcu.PRECISION_MIXED, tolerance=1e-6,
+                                  panel_width=128)
+    reg, rres = batch.solveBatched(*args, precision=facetcu.PRECISION_MIXED, tolerance=1e-6,
+                                   panel_width=128, flags=facetcu.BATCH_LEGACY_STEP)
+    assert res["converged"] and res["iterations"] == rres["iterations"]
+    assert np.array_equal(out, reg)
+    truth, _ = batch.solveBatched(*args, precision=facetcu.PRECISION_FP64, tolerance=1e-12,
+                                  maximum_iterations=4000)
+    assert rel_err(out, truth) < 1e-4
+    for m in models + [batch]:
+        m.close()

@@ -650,6 +650,56 @@ __global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_sweep_wide(GraphVie
     publish_cols<CPL>(md, mb, mr, col0, owner, P, stats);
 }
 
+// The first sweep of a solve from zero, B = T(0): no gather, so one thread
+// per facet and column, facets round robin over the grid (a thread keeps
+// its column, its statistics stay in registers), the same arithmetic as
+// k_sweep_wide with a zero gather.  (Run through k_sweep_wide's warp-per-
+// facet loop it took 0.35 ms at the bench's 64 columns.)
+template <int P>
+__global__ void __launch_bounds__(256) k_sweep_zero(GraphView g, PanelParams pp,
+                                                    float* __restrict__ Bout, uint32_t* stats,
+                                                    const uint32_t* done)
+{
+    static_assert(256 % P == 0, "whole facets per block");
+    constexpr int FPB = 256 / P;  // facets per block pass
+    if (*done) return;
+    const int c = threadIdx.x % P;
+    const float L = pp.skyL[c], fl = kSideFloor * pp.colmax[c];
+    float md = 0.0f, mb = 0.0f, mr = 0.0f;
+    const uint32_t stride = gridDim.x * FPB;
+    for (uint32_t f = blockIdx.x * FPB + threadIdx.x / P; f < g.facets; f += stride) {
+        const uint32_t s0 = 2u * f, s1 = s0 + 1u;
+        const uint32_t d0 = __ldg(g.denom + s0), d1 = __ldg(g.denom + s1);
+        const float k0 = float(__ldg(g.skyc + s0)), k1 = float(__ldg(g.skyc + s1));
+        const size_t i0 = size_t(s0) * P + c, i1 = i0 + P;
+        const float h0 = (d0 != 0u ? (k0 * L) / float(d0) : L) + __ldcs(pp.direct + i0);
+        const float h1 = (d1 != 0u ? (k1 * L) / float(d1) : L) + __ldcs(pp.direct + i1);
+        const float b0 = __ldcs(pp.emis + i0) + __ldcs(pp.rho + i0) * h0 + __ldcs(pp.tau + i0) * h1;
+        const float b1 = __ldcs(pp.emis + i1) + __ldcs(pp.rho + i1) * h1 + __ldcs(pp.tau + i1) * h0;
+        Bout[i0] = b0;
+        Bout[i1] = b1;
+        md = fmaxf(md, fmaxf(fabsf(b0), fabsf(b1)));
+        mr = fmaxf(mr, fmaxf(rel_change(b0, b0, fl), rel_change(b1, b1, fl)));
+    }
+    mb = md;  // the change from zero is the value
+    __shared__ float s_st[3][256];
+    s_st[0][threadIdx.x] = md;
+    s_st[1][threadIdx.x] = mb;
+    s_st[2][threadIdx.x] = mr;
+    __syncthreads();
+    for (int col = threadIdx.x; col < P; col += blockDim.x) {
+        float a = 0.0f, b = 0.0f, r = 0.0f;
+        for (int t = col; t < 256; t += P) {
+            a = fmaxf(a, s_st[0][t]);
+            b = fmaxf(b, s_st[1][t]);
+            r = fmaxf(r, s_st[2][t]);
+        }
+        atomicMax(stats + col, __float_as_uint(a));
+        atomicMax(stats + kMaxP + col, __float_as_uint(b));
+        atomicMax(stats + 2 * kMaxP + col, __float_as_uint(r));
+    }
+}
+
 // ---- residual-tracked int8 steps (MIXED, wide panels) --------------------
 // State per cell: X (FP32 iterate), R = T(X) - X (FP32, its Jacobi
 // residual) and Q = round(R / sigma) (int8, one scale sigma per column, not
@@ -2125,6 +2175,24 @@ void launch_sweep(int P, const GraphView& g, const PanelParams& pp, const T* in,
                   uint32_t* stats, uint32_t* counter, const uint32_t* done, cudaStream_t s)
 {
     if constexpr (sizeof(T) == 4) {
+        if (in == nullptr && P >= 8) {
+            // a solve from zero: its first sweep has nothing to gather
+            static const int grid = [] {
+                int dev = 0, sms = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                return std::max(1, sms) * 8;
+            }();
+            switch (P) {
+            case 8: k_sweep_zero<8><<<grid, 256, 0, s>>>(g, pp, out, stats, done); break;
+            case 16: k_sweep_zero<16><<<grid, 256, 0, s>>>(g, pp, out, stats, done); break;
+            case 32: k_sweep_zero<32><<<grid, 256, 0, s>>>(g, pp, out, stats, done); break;
+            case 64: k_sweep_zero<64><<<grid, 256, 0, s>>>(g, pp, out, stats, done); break;
+            default: k_sweep_zero<128><<<grid, 256, 0, s>>>(g, pp, out, stats, done); break;
+            }
+            FCU_LAUNCH("k_sweep_zero");
+            return;
+        }
         if (P == 8 || P == 16) {
             // 16-byte row vectors in rounds of 8 loads per lane
             if (P == 8) {

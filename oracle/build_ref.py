@@ -34,6 +34,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "facetrt_ref.cpp")
 LIB = os.path.join(OUT, "libfacetrt_ref.so")
+# The reference tree this recipe compiles from: the one place its path is
+# named (tests and the fixture script import it); FACETRT_REFERENCE_ROOT
+# overrides it.  Where it is absent the backend is compiled from the extract
+# an earlier run generated into oracle/_ref (it travels with the repository
+# snapshot), and the tree-only checkers are skipped.
 REFERENCE = os.environ.get("FACETRT_REFERENCE_ROOT", "/root/reference")
 FACETRT = os.path.join(REFERENCE, "models", "histream", "src", "facetrt")
 BASE = os.path.join(REFERENCE, "models", "histream", "src", "base")

@@ -10,6 +10,8 @@ graph diagnostics as a compressed .npz, so the tests can run where the
 reference tree is absent.
 
 Usage: python tests/golden/make_golden.py [reference_root]
+(default: the tree the oracle recipe reads, oracle/build_ref.py REFERENCE,
+which FACETRT_REFERENCE_ROOT overrides)
 """
 import json
 import os
@@ -19,11 +21,14 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle.build_ref import REFERENCE  # noqa: E402
+
 SCENES = ["urban_tree_building", "urban_dem_building"]
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else REFERENCE
     for scene in SCENES:
         out_dir = os.path.join(root, "validation", scene, "output")
         with open(os.path.join(out_dir, "radiosity_gpu.json"), encoding="utf-8") as f:

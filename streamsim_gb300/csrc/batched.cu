@@ -2369,12 +2369,21 @@ void launch_scene_check(const GraphView& g, int P, uint32_t parity, float tol, c
     FCU_LAUNCH("k_scene_check");
 }
 
-// One batch of kStepBatch int8 steps, each followed by its check, as a CUDA
-// graph: the batches of a solve repeat the same launches (the q panels and
-// scales alternate with the step's parity and every batch starts on an even
-// step; the check takes its sweep index from the device counter k_init_i8
-// seeds), so the batch is captured once per panel configuration and replayed.
-constexpr uint32_t kStepBatch = 8;
+// The int8 phase of a solve as one CUDA graph launch: a conditional WHILE
+// node whose body is two steps (the q panels and scales alternate with the
+// step's parity), each followed by its check (the sweep index comes from the
+// device counter k_init_i8 seeds), and k_steps_continue, which keeps the loop
+// going while the phase's done flag is clear and two more steps fit under
+// the iteration limit.  The device decides when the phase ends; the host
+// reads the flags once, after the launch.  The graph is captured once per
+// panel configuration and replayed.
+constexpr uint32_t kStepBatch = 2;  // steps per loop body
+
+__global__ void k_steps_continue(cudaGraphConditionalHandle loop, const uint32_t* done,
+                                 const uint32_t* it_dev, uint32_t limit)
+{
+    cudaGraphSetConditional(loop, (*done == 0u && *it_dev + kStepBatch <= limit) ? 1u : 0u);
+}
 
 struct StepGraphKey {
     int P;
@@ -2389,6 +2398,7 @@ struct StepGraphKey {
     uint32_t* stats;
     uint32_t* flag;
     float tol;
+    uint32_t limit;  // iteration limit of the solve
     cudaStream_t stream;
 };
 
@@ -2397,7 +2407,7 @@ void record_steps(const StepGraphKey& k, cudaStream_t s)
     int8_t* qb[2] = {const_cast<int8_t*>(k.q0), const_cast<int8_t*>(k.q1)};
     float* slot[2] = {k.slot0, k.slot1};
     uint32_t* counter = k.flag + 8;
-    for (uint32_t j = 0; j < kStepBatch; ++j) {
+    for (uint32_t j = 0; j < kStepBatch; ++j) {  // kStepBatch is even: the parity repeats
         launch_step_i8(k.P, k.g, k.pp, qb[j & 1u], qb[(j + 1) & 1u], k.X, k.R, slot[j & 1u],
                        slot[(j + 1) & 1u], k.stats, counter, k.flag + 3, j & 1u, s);
         float* colmax = reinterpret_cast<float*>(k.flag + 16);
@@ -2430,19 +2440,39 @@ cudaGraphExec_t step_graph(BatchState& st, const StepGraphKey& key)
         break;
     }
     cudaGraph_t graph = nullptr;
-    FCU_CHECK(cudaStreamBeginCapture(key.stream, cudaStreamCaptureModeThreadLocal));
+    FCU_CHECK(cudaGraphCreate(&graph, 0));
+    cudaGraphExec_t exec = nullptr;
     try {
-        record_steps(key, key.stream);
+        cudaGraphConditionalHandle loop;
+        FCU_CHECK(cudaGraphConditionalHandleCreate(&loop, graph, 1u, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = loop;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        FCU_CHECK(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        FCU_CHECK(cudaStreamBeginCaptureToGraph(key.stream, body, nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal));
+        try {
+            record_steps(key, key.stream);
+            k_steps_continue<<<1, 1, 0, key.stream>>>(loop, key.flag + 3, key.flag + 12,
+                                                      key.limit);
+            FCU_LAUNCH("k_steps_continue");
+        } catch (...) {
+            cudaGraph_t dummy = nullptr;
+            cudaStreamEndCapture(key.stream, &dummy);
+            throw;
+        }
+        cudaGraph_t captured = nullptr;
+        FCU_CHECK(cudaStreamEndCapture(key.stream, &captured));
+        FCU_CHECK(cudaGraphInstantiate(&exec, graph, 0));
     } catch (...) {
-        cudaStreamEndCapture(key.stream, &graph);
-        if (graph) cudaGraphDestroy(graph);
+        cudaGraphDestroy(graph);
         throw;
     }
-    FCU_CHECK(cudaStreamEndCapture(key.stream, &graph));
-    cudaGraphExec_t exec = nullptr;
-    const cudaError_t rc = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
-    FCU_CHECK(rc);
     st.step_graph = exec;
     static_assert(sizeof(StepGraphKey) <= sizeof(st.step_graph_key), "graph key size");
     std::memcpy(st.step_graph_key, &key, sizeof(key));
@@ -2815,8 +2845,9 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                 bool steps_done = false;
                 while (!steps_done && it < max_it) {
                     const uint32_t batch = std::min(timed ? 1u : check_every, max_it - it);
-                    if (!timed && batch == kStepBatch) {
-                        // j is even here: the captured parity pattern applies
+                    if (!timed && max_it - it >= kStepBatch && (j & 1u) == 0u) {
+                        // the rest of the phase as one launch (j even: the
+                        // captured parity pattern applies)
                         StepGraphKey key;
                         std::memset(&key, 0, sizeof(key));  // padding takes part in the compare
                         key.P = P;
@@ -2831,12 +2862,25 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                         key.stats = stats;
                         key.flag = flag;
                         key.tol = step_tol;
+                        key.limit = max_it;
                         key.stream = s;
                         FCU_CHECK(cudaGraphLaunch(step_graph(st, key), s));
-                        launches += (g.scene ? 3 : 2) * kStepBatch;
-                        sweeps += kStepBatch;
                         ++graph_launches;
-                        j += kStepBatch;
+                        uint32_t fl[10];  // flag[3 .. 12]: the phase's flags, the device counter
+                        FCU_CHECK(cudaMemcpyAsync(fl, flag + 3, sizeof(fl), cudaMemcpyDeviceToHost, s));
+                        FCU_CHECK(cudaStreamSynchronize(s));
+                        const uint32_t ran = fl[9] - it;  // steps launched (each one checked)
+                        launches += (g.scene ? 3 : 2) * ran + ran / kStepBatch;
+                        sweeps += ran;
+                        j += ran;
+                        it += ran;
+                        if (fl[0]) {
+                            steps_done = true;
+                            sweeps -= it - fl[1];  // launched after the target: no work
+                            it = fl[1];
+                            FCU_CHECK(cudaMemsetAsync(flag + 3, 0, 12, s));
+                        }
+                        continue;
                     } else
                     for (uint32_t k = 0; k < batch; ++k, ++j) {
                         const float* sin = slot[j & 1u];

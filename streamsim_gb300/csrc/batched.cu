@@ -157,10 +157,7 @@ __device__ __forceinline__ Acc gather_narrow(const GraphView& g, uint32_t s, con
 #pragma unroll
             for (int u = 0; u < U; ++u) acc += Acc(c[u]) * v[u];
         }
-#pragma unroll
-        for (int o = P; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        return acc;
-    }
+    } else {
     for (uint32_t base = start; base < end; base += 32) {
         const uint32_t n = min(32u, end - base);
         uint32_t pk = 0;
@@ -192,6 +189,7 @@ __device__ __forceinline__ Acc gather_narrow(const GraphView& g, uint32_t s, con
 #pragma unroll
             for (int u = 0; u < U; ++u) acc += Acc(c[u]) * v[u];
         }
+    }
     }
 #pragma unroll
     for (int o = P; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -1727,8 +1725,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep(GraphView g, PanelParams 
         }
         fold_narrow_stats(md, mb, mr, P);
         publish_stats<1>(md, mb, mr, lane, P, stats);
-        return;
-    }
+    } else {
     for (uint32_t f = fb; f < fe; ++f) {
         const uint32_t s0 = 2u * f, s1 = s0 + 1u;
         Acc h[2];
@@ -1755,6 +1752,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep(GraphView g, PanelParams 
     }
     // lanes >= P hold zeros; column c of the stats is lane c (one column each)
     publish_stats<1>(md, mb, mr, lane, P, stats);
+    }
 }
 
 template <int P>
@@ -1808,8 +1806,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep_defect(GraphView g, Panel
         float mr[1] = {0.0f};
         fold_narrow_stats(md, mb, mr, P);
         publish_stats<1>(md, mb, mr, lane, P, stats);
-        return;
-    }
+    } else {
     for (uint32_t f = fb; f < fe; ++f) {
         const uint32_t s0 = 2u * f, s1 = s0 + 1u;
         float h[2];
@@ -1835,6 +1832,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_sweep_defect(GraphView g, Panel
     }
     const float mr[1] = {0.0f};  // defect cycles stop on the absolute test
     publish_stats<1>(md, mb, mr, lane, P, stats);
+    }
 }
 
 // d = Bnew - Bold (FP32) -> BF16.

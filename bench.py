@@ -1091,9 +1091,9 @@ def run_eb(args, rank, world, local):
     T0 = np.full(S, meteo["air_temperature"] + 273.15, np.float32)
     lit = w["lit"]
 
-    def node(tolerance):
+    def node(tolerance, precision=fc.PRECISION_FP32):
         p, keep = fc.energy_parameters(sc.leaf_count, materials, mi, None, 0.0, bands,
-                                       solver_tolerance=tolerance)
+                                       solver_tolerance=tolerance, precision=precision)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         out, res = m.facetebNode(p, meteo, sun, lit, windows, T0, bd, bf)
@@ -1109,6 +1109,12 @@ def run_eb(args, rank, world, local):
     node_s = float(np.mean(times))
     fixed, fres, fixed_s = node(0.0)
     fixed, fres, fixed_s = node(0.0)
+    # the same node with its window and band solves in MIXED precision
+    mixed_times = []
+    for _ in range(max(2, args.steps)):
+        mixed, mres, dt = node(1e-6, fc.PRECISION_MIXED)
+        mixed_times.append(dt)
+    mixed_s = float(np.mean(mixed_times[1:]))
     units = F * res["solves"]
     h2d = 4 * (2 * S + 2 * F) + 12 * len(win)
     d2h = 4 * S * (12 + len(bands))
@@ -1148,6 +1154,10 @@ def run_eb(args, rank, world, local):
         "node": {k: res[k] for k in ("coupling_iterations", "converged", "max_temperature_delta",
                                      "max_energy_residual_equivalent", "shortwave_sweeps",
                                      "longwave_sweeps", "band_sweeps", "solves")},
+        "mixed_precision": {"value": F * mres["solves"] / mixed_s, "ms_per_step": mixed_s * 1e3,
+                            "coupling_iterations": mres["coupling_iterations"],
+                            "max_abs_temperature_difference_K": float(
+                                np.max(np.abs(mixed["temperature"] - out["temperature"])))},
         "fixed_sweeps": {"value": units / fixed_s, "ms_per_step": fixed_s * 1e3,
                          "coupling_iterations": fres["coupling_iterations"],
                          "max_abs_temperature_difference_K": float(

@@ -260,14 +260,17 @@ int facetcu_solve_batched_device(facetcu_context *ctx, const facetcu_batch_confi
                                  float *radiosity, facetcu_batch_result *result);
 
 /* Autotuning of the batched solve: times the candidate panel widths (32, 64
- * and 128 columns, those not wider than the columns; 32 in FP64) on short
- * solves (6 sweeps of every panel) of the given inputs (device pointers, as
+ * and 128 columns, those not wider than the columns; 32 in FP64) and, for
+ * the widths whose MIXED int8 step runs on the pipelined kernel (64 and
+ * 128), that kernel's CTAs per SM (as many as fit, 2 or 1) on short solves
+ * (6 sweeps of every panel) of the given inputs (device pointers, as
  * facetcu_solve_batched_device; `radiosity` is scratch here) and keeps the
  * fastest for this GPU, graph size, column count and precision: later
- * batched solves with panel_width = 0 use it.  cache_path (may be NULL)
- * names a JSON-lines file the choices are read from first and written back
- * to; a cached choice returns without timing.  No counterpart in the
- * reference. */
+ * batched solves with panel_width = 0 use it (the results do not depend on
+ * the choice, only the time).  *panel_width receives the width.  cache_path
+ * (may be NULL) names a JSON-lines file the choices are read from first and
+ * written back to; a cached choice returns without timing.  No counterpart
+ * in the reference. */
 int facetcu_autotune_batched(facetcu_context *ctx, const facetcu_batch_config *config,
                              const float *reflectance, const float *transmittance,
                              const float *emission, const float *sky, const float *beam,

@@ -61,7 +61,12 @@ struct facetcu_context {
     DeviceBuffer spec_io;
     DeviceBuffer eb_io, eb_tab;  // FacetEB node fields and per-material tables
     DeviceBuffer img_io;         // sensor image scratch and outputs
-    std::map<std::string, uint32_t> tuned;  // autotuned panel widths by problem key
+    // autotuned settings by problem key: the panel width and the pipelined
+    // int8 step's CTAs per SM (0: as many as fit)
+    struct Tuned {
+        uint32_t panel_width = 0, step_ctas = 0;
+    };
+    std::map<std::string, Tuned> tuned;
     std::string gpu_name;                   // for the autotuner's key
 };
 
@@ -977,15 +982,20 @@ std::string tune_key(facetcu_context* ctx, const facetcu_batch_config* cfg)
 
 int run_batched(facetcu_context* ctx, const facetcu_batch_config* cfg_in, const float* rho,
                 const float* tau, const float* emis, const float* sky, const float* beam,
-                const float* dgeo, const float* initial, float* out, facetcu_batch_result* result)
+                const float* dgeo, const float* initial, float* out, facetcu_batch_result* result,
+                uint32_t step_ctas = 0)
 {
     facetcu_batch_config tuned_cfg = *cfg_in;
     if (tuned_cfg.panel_width == 0 && !ctx->tuned.empty()) {
         const auto it = ctx->tuned.find(tune_key(ctx, cfg_in));
-        if (it != ctx->tuned.end()) tuned_cfg.panel_width = it->second;
+        if (it != ctx->tuned.end()) {
+            tuned_cfg.panel_width = it->second.panel_width;
+            step_ctas = it->second.step_ctas;
+        }
     }
     const facetcu_batch_config* cfg = &tuned_cfg;
     BatchProblem p{};
+    p.step_ctas_per_sm = step_ctas;
     p.vertices = ctx->vertices.as<facetcu_vertex>();
     for (int a = 0; a < 3; ++a) {
         p.lo[a] = ctx->bmin[a];
@@ -1595,7 +1605,9 @@ int facetcu_scene_batch(facetcu_context* ctx, facetcu_context* const* scenes,
 namespace {
 
 // JSON-lines cache: {"key": "...", "panel_width": N} per line.
-void read_tune_cache(const char* path, std::map<std::string, uint32_t>& out)
+// One JSON object per line: key, panel width and (optional, 0 when absent)
+// the pipelined step's CTAs per SM.
+void read_tune_cache(const char* path, std::map<std::string, facetcu_context::Tuned>& out)
 {
     std::ifstream in(path);
     std::string line;
@@ -1605,18 +1617,24 @@ void read_tune_cache(const char* path, std::map<std::string, uint32_t>& out)
         if (k0 == std::string::npos || p0 == std::string::npos) continue;
         const size_t ks = k0 + 8, ke = line.find('"', ks);
         if (ke == std::string::npos) continue;
-        out[line.substr(ks, ke - ks)] = uint32_t(std::strtoul(line.c_str() + p0 + 15, nullptr, 10));
+        facetcu_context::Tuned t;
+        t.panel_width = uint32_t(std::strtoul(line.c_str() + p0 + 15, nullptr, 10));
+        const size_t c0 = line.find("\"step_ctas_per_sm\": ");
+        if (c0 != std::string::npos)
+            t.step_ctas = uint32_t(std::strtoul(line.c_str() + c0 + 20, nullptr, 10));
+        out[line.substr(ks, ke - ks)] = t;
     }
 }
 
-void write_tune_cache(const char* path, const std::map<std::string, uint32_t>& m)
+void write_tune_cache(const char* path, const std::map<std::string, facetcu_context::Tuned>& m)
 {
     const std::string tmp = std::string(path) + ".tmp";
     {
         std::ofstream out(tmp);
         if (!out) throw Error(FACETCU_RUNTIME_ERROR, std::string("cannot write ") + tmp);
         for (const auto& kv : m)
-            out << "{\"key\": \"" << kv.first << "\", \"panel_width\": " << kv.second << "}\n";
+            out << "{\"key\": \"" << kv.first << "\", \"panel_width\": " << kv.second.panel_width
+                << ", \"step_ctas_per_sm\": " << kv.second.step_ctas << "}\n";
     }
     if (std::rename(tmp.c_str(), path) != 0)
         throw Error(FACETCU_RUNTIME_ERROR, std::string("cannot replace ") + path);
@@ -1642,7 +1660,7 @@ int facetcu_autotune_batched(facetcu_context* ctx, const facetcu_batch_config* c
         if (cache_path) read_tune_cache(cache_path, ctx->tuned);
         auto hit = ctx->tuned.find(key);
         if (hit != ctx->tuned.end()) {
-            *panel_width = hit->second;
+            *panel_width = hit->second.panel_width;
             return FACETCU_OK;
         }
         check_batch_inputs(ctx, reflectance, transmittance, emission,
@@ -1650,29 +1668,37 @@ int facetcu_autotune_batched(facetcu_context* ctx, const facetcu_batch_config* c
                            config->band_count);
         const uint64_t R = uint64_t(config->band_count) * config->sun_count;
         const uint32_t cap = config->precision == FACETCU_PRECISION_FP64 ? 32u : 128u;
-        uint32_t best = 0;
+        // panel width x (for the widths whose int8 step is the pipelined
+        // kernel, MIXED at 64 and 128 columns) its CTAs per SM
+        facetcu_context::Tuned best;
         double best_t = 0.0;
         for (uint32_t P = 32; P <= cap; P *= 2) {
             if (P > R && P != 32) break;  // wider than the columns: only padding
-            facetcu_batch_config c = *config;
-            c.panel_width = P;
-            c.warm_start = FACETCU_WARM_NONE;
-            c.maximum_iterations = 6;  // a few sweeps of every panel
-            c.tolerance = 0.0f;
-            c.flags = 0;
-            facetcu_batch_result r{};
-            run_batched(ctx, &c, reflectance, transmittance, emission, sky, beam,
-                        direct_geometry, nullptr, radiosity, &r);  // warms the graph copies
-            run_batched(ctx, &c, reflectance, transmittance, emission, sky, beam,
-                        direct_geometry, nullptr, radiosity, &r);
-            if (best == 0 || r.seconds < best_t) {
-                best = P;
-                best_t = r.seconds;
+            const bool pipelined =
+                config->precision == FACETCU_PRECISION_MIXED && (P == 64 || P == 128);
+            for (uint32_t ctas : {0u, 2u, 1u}) {
+                if (ctas && !pipelined) break;
+                facetcu_batch_config c = *config;
+                c.panel_width = P;
+                c.warm_start = FACETCU_WARM_NONE;
+                c.maximum_iterations = 6;  // a few sweeps of every panel
+                c.tolerance = 0.0f;
+                c.flags = 0;
+                facetcu_batch_result r{};
+                run_batched(ctx, &c, reflectance, transmittance, emission, sky, beam,
+                            direct_geometry, nullptr, radiosity, &r, ctas);  // warms the graph copies
+                run_batched(ctx, &c, reflectance, transmittance, emission, sky, beam,
+                            direct_geometry, nullptr, radiosity, &r, ctas);
+                if (best.panel_width == 0 || r.seconds < best_t) {
+                    best.panel_width = P;
+                    best.step_ctas = ctas;
+                    best_t = r.seconds;
+                }
             }
         }
         ctx->tuned[key] = best;
         if (cache_path) write_tune_cache(cache_path, ctx->tuned);
-        *panel_width = best;
+        *panel_width = best.panel_width;
         return FACETCU_OK;
     });
 }

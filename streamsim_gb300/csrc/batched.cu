@@ -90,6 +90,7 @@ struct GraphView {
     uint32_t* scene_done;              // [scenes]
     uint32_t legacy_step;              // 1: 64-column int8 steps on the register-gather kernel
     uint32_t counts8;                  // 1: every count is at most 255 (the solver's copy)
+    uint32_t step_ctas;                // pipelined step: CTAs per SM (0: as many as fit)
 };
 
 __device__ __forceinline__ void edge_at(const GraphView& g, uint32_t e, uint32_t& nb, float& c)
@@ -2264,11 +2265,15 @@ int step_grid()
 }
 
 // The pipelined step: its dynamic shared memory is opted in once (before
-// any graph capture) and the grid sized for it.
+// any graph capture); the grid is the SM count times the CTAs per SM that
+// fit, or fewer when the autotuner asks for fewer (`ctas`).
 template <int P, bool Scenes>
-int async_step_grid()
+int async_step_grid(uint32_t ctas = 0)
 {
-    static const int grid = [] {
+    struct Fit {
+        int sms, per_sm;
+    };
+    static const Fit fit = [] {
         constexpr int bytes = AsyncLayout<P>::kBlockBytes;
         FCU_CHECK(cudaFuncSetAttribute(k_step_i8_async<P, Scenes>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
@@ -2277,9 +2282,10 @@ int async_step_grid()
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         FCU_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &per_sm, k_step_i8_async<P, Scenes>, AsyncWarps<P>::value * 32, bytes));
-        return std::max(1, sms) * std::max(1, per_sm);
+        return Fit{std::max(1, sms), std::max(1, per_sm)};
     }();
-    return grid;
+    const int per_sm = ctas ? std::min(fit.per_sm, int(ctas)) : fit.per_sm;
+    return fit.sms * per_sm;
 }
 
 template <int P, bool Scenes>
@@ -2288,8 +2294,8 @@ void launch_async_step(const GraphView& g, const PanelParams& pp, const int8_t* 
                        uint32_t* counter, const uint32_t* done, const float* ssin,
                        const float* ssout, cudaStream_t s)
 {
-    k_step_i8_async<P, Scenes><<<async_step_grid<P, Scenes>(), AsyncWarps<P>::value * 32,
-                                 AsyncLayout<P>::kBlockBytes, s>>>(
+    k_step_i8_async<P, Scenes><<<async_step_grid<P, Scenes>(g.step_ctas),
+                                 AsyncWarps<P>::value * 32, AsyncLayout<P>::kBlockBytes, s>>>(
         g, pp, qin, qout, X, R, sin, sout, stats, counter, done, ssin, ssout);
 }
 
@@ -2631,6 +2637,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
     g.scene_done = nullptr;
     g.legacy_step = (cfg.flags & FACETCU_BATCH_LEGACY_STEP) != 0u ? 1u : 0u;
     g.counts8 = perm ? 1u : 0u;
+    g.step_ctas = p.step_ctas_per_sm;
     if (FCU_SCENE_SKIP && perm && mixed && gr.p_scene.ptr && gr.p_scene.bytes >= size_t(S / 2u) * 2 &&
         gr.scene_facets.size() >= 3) {
         // scene batch: converged scenes leave the int8 steps

@@ -192,6 +192,7 @@ struct BatchProblem {
     const float* sky;      // bands
     const float* beam;     // bands
     const float* dgeo;     // suns * S or null
+    uint32_t step_ctas_per_sm = 0;  // pipelined int8 step: CTAs per SM (0: as many as fit)
 };
 struct BatchState {
     DeviceBuffer x0, x1;        // panels, side-major [S][P]
@@ -202,7 +203,7 @@ struct BatchState {
     DeviceBuffer i8;            // int8 step panels (two)
     DeviceBuffer scene_state;   // scene batches: [scenes][kMaxP] step records + [scenes] done
     cudaGraphExec_t step_graph = nullptr;  // captured batch of int8 steps
-    alignas(8) unsigned char step_graph_key[256] = {};
+    alignas(8) unsigned char step_graph_key[384] = {};
 };
 void release_graphs(BatchState& st);
 // Device-side checks of the batched solve's inputs; returns the error bits

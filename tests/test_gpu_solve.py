@@ -264,8 +264,9 @@ def test_batched_input_checks_on_host_and_device_paths(c1):
 
 
 def test_autotune_panel_width_and_cache(c1, tmp_path):
-    """facetcu_autotune_batched times the panel widths on short solves, keeps
-    the fastest (one of 32/64/128 not wider than the columns), writes it to
+    """facetcu_autotune_batched times the panel widths (and the pipelined
+    step's CTAs per SM) on short solves, keeps the fastest (one of 32/64/128
+    not wider than the columns), writes it to
     the JSON-lines cache, and later solves with panel_width = 0 use it: the
     same bits as a solve with that width given explicitly, also in a fresh
     context that only reads the cache."""
@@ -302,6 +303,19 @@ def test_autotune_panel_width_and_cache(c1, tmp_path):
     assert fresh.autotuneBatched(cfg, *ptrs, out.data_ptr(), str(cache)) == best  # from the cache
     assert np.array_equal(solve(fresh, 0), tuned)
     fresh.close()
+    # the pipelined step's CTAs per SM (the tuner's second parameter) change
+    # the time, not the bits: a cached choice of 64 columns at 1 CTA per SM
+    # equals the explicit 64-column solve at the occupancy limit
+    import json
+    key = json.loads(text.splitlines()[0])["key"]
+    assert '"step_ctas_per_sm": ' in text
+    one = tmp_path / "tune_one_cta.jsonl"
+    one.write_text(json.dumps({"key": key, "panel_width": 64, "step_ctas_per_sm": 1}) + "\n")
+    slow = model_for(sc.vertices, 512, 64)
+    slow.setGraph(*m.graph())
+    assert slow.autotuneBatched(cfg, *ptrs, out.data_ptr(), str(one)) == 64
+    assert np.array_equal(solve(slow, 0), solve(slow, 64))
+    slow.close()
 
 
 @pytest.mark.parametrize("kind,suns", [("forest", 1), ("coarse_soil", 1), ("forest", 2),

@@ -2448,14 +2448,25 @@ cudaGraphExec_t step_graph(BatchState& st, const StepGraphKey& key)
     cudaGraphExec_t exec = nullptr;
     try {
         cudaGraphConditionalHandle loop;
-        FCU_CHECK(cudaGraphConditionalHandleCreate(&loop, graph, 1u, cudaGraphCondAssignDefault));
         cudaGraphNodeParams cp = {};
-        cp.type = cudaGraphNodeTypeConditional;
-        cp.conditional.handle = loop;
-        cp.conditional.type = cudaGraphCondTypeWhile;
-        cp.conditional.size = 1;
         cudaGraphNode_t node = nullptr;
-        FCU_CHECK(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+        cudaError_t e = cudaGraphConditionalHandleCreate(&loop, graph, 1u, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess) {
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = loop;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp);
+        }
+        if (e == cudaErrorNotSupported || e == cudaErrorInvalidValue) {
+            // no conditional nodes with this driver: the caller launches
+            // the steps one by one (the same bits)
+            cudaGetLastError();
+            cudaGraphDestroy(graph);
+            st.no_loop_graph = true;
+            return nullptr;
+        }
+        FCU_CHECK(e);
         cudaGraph_t body = cp.conditional.phGraph_out[0];
         FCU_CHECK(cudaStreamBeginCaptureToGraph(key.stream, body, nullptr, nullptr, 0,
                                                 cudaStreamCaptureModeThreadLocal));
@@ -2850,7 +2861,7 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                 bool steps_done = false;
                 while (!steps_done && it < max_it) {
                     const uint32_t batch = std::min(timed ? 1u : check_every, max_it - it);
-                    if (!timed && max_it - it >= kStepBatch && (j & 1u) == 0u) {
+                    if (!timed && !st.no_loop_graph && max_it - it >= kStepBatch && (j & 1u) == 0u) {
                         // the rest of the phase as one launch (j even: the
                         // captured parity pattern applies)
                         StepGraphKey key;
@@ -2869,7 +2880,9 @@ int batched_solve(const DeviceGraph& gr_in, const BatchProblem& p, const facetcu
                         key.tol = step_tol;
                         key.limit = max_it;
                         key.stream = s;
-                        FCU_CHECK(cudaGraphLaunch(step_graph(st, key), s));
+                        const cudaGraphExec_t loop_graph = step_graph(st, key);
+                        if (!loop_graph) continue;  // launch the steps one by one
+                        FCU_CHECK(cudaGraphLaunch(loop_graph, s));
                         ++graph_launches;
                         uint32_t fl[10];  // flag[3 .. 12]: the phase's flags, the device counter
                         FCU_CHECK(cudaMemcpyAsync(fl, flag + 3, sizeof(fl), cudaMemcpyDeviceToHost, s));

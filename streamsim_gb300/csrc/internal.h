@@ -202,7 +202,8 @@ struct BatchState {
     DeviceBuffer corr;          // residual / correction panel
     DeviceBuffer i8;            // int8 step panels (two)
     DeviceBuffer scene_state;   // scene batches: [scenes][kMaxP] step records + [scenes] done
-    cudaGraphExec_t step_graph = nullptr;  // captured batch of int8 steps
+    cudaGraphExec_t step_graph = nullptr;  // the int8 phase's loop graph
+    bool no_loop_graph = false;            // conditional graph nodes unavailable
     alignas(8) unsigned char step_graph_key[384] = {};
 };
 void release_graphs(BatchState& st);

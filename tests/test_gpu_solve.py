@@ -161,9 +161,10 @@ def test_batched_warm_start_given(c1):
 
 
 def test_mixed_graph_replay_matches_per_sweep_launches(c1):
-    """The int8 step batches replayed from a captured CUDA graph give the
-    same bits as launching every step and check one by one (the sweep-timing
-    mode), on a wide panel and on two panels of different widths."""
+    """The int8 phase run as one graph launch (a conditional WHILE node the
+    device ends) gives the same bits as launching every step and check one
+    by one (the sweep-timing mode), on a wide panel and on two panels of
+    different widths."""
     sc = c1["scene"]
     for bands, suns in ((64, 1), (32, 3)):
         rho, tau, _, sky, beam = _bands(sc, c1["lit"], c1["sun"], bands)
@@ -177,6 +178,31 @@ def test_mixed_graph_replay_matches_per_sweep_launches(c1):
         assert ra["graph_launches"] > 0 and rb["graph_launches"] == 0
         assert ra["iterations"] == rb["iterations"]
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("limit", [4, 5, 9])
+def test_mixed_loop_graph_stops_at_the_iteration_limit(c1, monkeypatch, limit):
+    """A MIXED solve that cannot converge within maximum_iterations: the
+    device loop stops at the limit (an odd budget leaves one step for the
+    host to launch alone), reports it, and gives the same bits as launching
+    every step one by one and as the steps launched without the loop graph
+    (the path taken where conditional graph nodes are unavailable)."""
+    sc = c1["scene"]
+    rho, tau, dgeo, sky, beam = _bands(sc, c1["lit"], c1["sun"], 64)
+    kw = dict(precision=facetcu.PRECISION_MIXED, tolerance=1e-9, maximum_iterations=limit,
+              raise_on_nonconvergence=False)
+    a, ra = c1["model"].solveBatched(rho, tau, sky, beam, dgeo, **kw)
+    assert ra["converged"] == 0 and ra["iterations"] == limit
+    b, rb = c1["model"].solveBatched(rho, tau, sky, beam, dgeo,
+                                     flags=facetcu.BATCH_TIME_SWEEPS, **kw)
+    assert rb["iterations"] == limit and np.array_equal(a, b)
+    fresh = model_for(sc.vertices, 512, 64)
+    fresh.setGraph(*c1["model"].graph())
+    monkeypatch.setenv("FACETCU_TEST_NO_LOOP_GRAPH", "1")
+    c, rc = fresh.solveBatched(rho, tau, sky, beam, dgeo, **kw)
+    fresh.close()
+    assert rc["graph_launches"] == 0 and rc["iterations"] == limit
+    assert np.array_equal(a, c)
 
 
 def test_scene_batch_matches_scenes_solved_alone():

@@ -1108,7 +1108,7 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
 //             epilogue.
 // In-flight rows cost shared memory instead of registers, and the edge
 // words are requested before their rows are, so neither the dp4a work nor
-// the epilogue's loads stop the gather.  Facets come in chunks of kChunk
+// the epilogue's loads stop the gather.  Facets come in chunks of kAsyncChunk
 // from the step's counter; the request cursor takes its next chunk (and
 // that chunk's row offsets and denominators) one chunk ahead, and asks L2
 // for the next chunk's edge words and each chunk's per-cell planes
@@ -1153,6 +1153,15 @@ template <int P> struct AsyncWarps {
 constexpr int kAsyncStages = FCU_ASYNC_STAGES;
 constexpr int kLookahead = FCU_ASYNC_LOOKAHEAD;
 constexpr int kStageEdges = FCU_ASYNC_EDGES;  // 32, 64 or 128 edges per stage
+// Facets per hand-out of the pipelined step (single scenes): the request
+// cursor takes chunks one ahead, so a chunk's row offsets and the L2
+// prefetches of its planes serve its C facets.  Measured on the config-2
+// forest: 1 facet 0.512 ms, 2 0.497, 3 0.488, 4 0.501, 5 0.497, 6 0.505,
+// 8 0.535.
+#ifndef FCU_ASYNC_CHUNK
+#define FCU_ASYNC_CHUNK 3
+#endif
+constexpr uint32_t kAsyncChunk = FCU_ASYNC_CHUNK;
 
 constexpr int pow2_at_least(int n) { return n <= 1 ? 1 : 2 * pow2_at_least((n + 1) / 2); }
 
@@ -1208,7 +1217,7 @@ __global__ void __launch_bounds__(AsyncWarps<P>::value * 32, FCU_ASYNC_BLOCKS) k
     constexpr int EPL = SE / G;        // edges per lane per stage
     constexpr int CPL = SE * L / 32;   // 16-byte copies per lane per stage
     constexpr int NST = kAsyncStages, D = kLookahead, NQ = Lay::kDesc;
-    constexpr uint32_t C = Scenes ? kSceneChunk : kChunk;
+    constexpr uint32_t C = Scenes ? kSceneChunk : kAsyncChunk;
     static_assert(2 * C + 1 <= 32, "a chunk's row offsets fit one warp");
     constexpr unsigned kAll = 0xffffffffu;
     static_assert(SE == 32 || SE == 64 || SE == 128, "32, 64 or 128 edges per stage");

@@ -1125,7 +1125,13 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
 // 32-edge stages with 4 ring stages 0.622 (their per-stage bookkeeping
 // doubled the instructions per edge); 64-edge stages with 4 warps per CTA
 // (6 CTAs per SM) 0.529; 128-edge stages with 4 or 2 warps 0.588-0.590
-// (a 183-edge mean row fills 72 % of two 128-edge stages).
+// (a 183-edge mean row fills 72 % of two 128-edge stages).  With three
+// facets per chunk, CTA shapes (warps x CTAs per SM, registers per thread):
+// 8 x 3 (80, spills) 0.488 ms; 8 x 2 (128) 0.474; 4 x 6 0.486; 12 x 2 0.496;
+// 12 x 1 0.518; 16 x 1 (118) 0.466; 20 x 1 (96) 0.452; 22 x 1 (80, spills)
+// 0.479; 24 x 1 0.494; 26 x 1 0.503; 16 x 1 with 3 ring stages 0.471, with 3
+// stages and 2 of lookahead 0.478.  One CTA of 20 warps per SM: the most
+// warps whose registers (96) hold the step without spills.
 #ifndef FCU_ASYNC_STAGES
 #define FCU_ASYNC_STAGES 2
 #endif
@@ -1133,22 +1139,27 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
 #define FCU_ASYNC_LOOKAHEAD 1
 #endif
 #ifndef FCU_ASYNC_BLOCKS
-#define FCU_ASYNC_BLOCKS 3
+#define FCU_ASYNC_BLOCKS 1
 #endif
 #ifndef FCU_ASYNC_EDGES
 #define FCU_ASYNC_EDGES 64
 #endif
 #ifndef FCU_ASYNC_WARPS
-#define FCU_ASYNC_WARPS 8
+#define FCU_ASYNC_WARPS 20
 #endif
 constexpr int kAsyncWarps = FCU_ASYNC_WARPS;  // warps per CTA of the pipelined step (64 columns)
-// At 128 columns a stage holds 8 KB of rows: 4 warps per CTA keep the
-// shared memory per SM (3 CTAs) at the 64-column kernel's.
+// At 128 columns a stage holds 8 KB of rows: 4 warps per CTA, 3 CTAs per SM
+// (measured on the config-2 forest with two suns: 0.788 ms; 6 x 2 0.790,
+// 12 x 1 0.793, 10 x 1 0.835, 8 x 1 0.901).
 #ifndef FCU_ASYNC_WARPS_128
 #define FCU_ASYNC_WARPS_128 4
 #endif
+#ifndef FCU_ASYNC_BLOCKS_128
+#define FCU_ASYNC_BLOCKS_128 3
+#endif
 template <int P> struct AsyncWarps {
     static constexpr int value = P == 128 ? FCU_ASYNC_WARPS_128 : kAsyncWarps;
+    static constexpr int blocks = P == 128 ? FCU_ASYNC_BLOCKS_128 : FCU_ASYNC_BLOCKS;  // min CTAs per SM
 };
 constexpr int kAsyncStages = FCU_ASYNC_STAGES;
 constexpr int kLookahead = FCU_ASYNC_LOOKAHEAD;
@@ -1202,7 +1213,7 @@ __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes)
 }
 
 template <int P, bool Scenes>
-__global__ void __launch_bounds__(AsyncWarps<P>::value * 32, FCU_ASYNC_BLOCKS) k_step_i8_async(
+__global__ void __launch_bounds__(AsyncWarps<P>::value * 32, AsyncWarps<P>::blocks) k_step_i8_async(
     GraphView g, PanelParams pp, const int8_t* __restrict__ Qin, int8_t* __restrict__ Qout,
     float* __restrict__ X, float* __restrict__ R, const float* __restrict__ sig_in,
     const float* __restrict__ sig_out, uint32_t* stats, uint32_t* counter, const uint32_t* done,

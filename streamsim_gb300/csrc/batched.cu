@@ -304,6 +304,12 @@ template <bool kBF16> constexpr int kVecCols = kBF16 ? 8 : 4;
 #ifndef FCU_STEP64_MIN_BLOCKS
 #define FCU_STEP64_MIN_BLOCKS 4
 #endif
+// Resident CTAs per SM of the FP32 wide sweep (64 registers at 4): the
+// config-2 forest's 64-column sweep 1.096 ms at 4 against 1.146 at 3 and
+// 1.458 at 2 (latency hidden by warps, not by registers).
+#ifndef FCU_SWEEP_MIN_BLOCKS
+#define FCU_SWEEP_MIN_BLOCKS 4
+#endif
 #ifndef FCU_SCENE_SKIP
 #define FCU_SCENE_SKIP 1
 #endif
@@ -571,7 +577,7 @@ __device__ __forceinline__ void publish_stats(const float* md, const float* mb, 
 // stands for B_in = 0 (the first sweep of a solve that starts from zero):
 // the gather is skipped, which gives the same bits as gathering zeros.
 template <int P>
-__global__ void __launch_bounds__(kWarps * 32, kMinBlocks) k_sweep_wide(GraphView g, PanelParams pp,
+__global__ void __launch_bounds__(kWarps * 32, FCU_SWEEP_MIN_BLOCKS) k_sweep_wide(GraphView g, PanelParams pp,
                                                             const float* __restrict__ Bin,
                                                             float* __restrict__ Bout,
                                                             uint32_t* stats, uint32_t* counter,

@@ -306,10 +306,15 @@ template <bool kBF16> constexpr int kVecCols = kBF16 ? 8 : 4;
 #endif
 // Resident CTAs per SM of the FP32 wide sweep (64 registers at 4): the
 // config-2 forest's 64-column sweep 1.096 ms at 4 against 1.146 at 3 and
-// 1.458 at 2 (latency hidden by warps, not by registers).
+// 1.458 at 2 (latency hidden by warps, not by registers); at 128 columns
+// the spills at 64 registers cost more (C3's batched FP32 solve 11.5 s at 3,
+// 12.3 s at 4), so that width keeps 3.
 #ifndef FCU_SWEEP_MIN_BLOCKS
 #define FCU_SWEEP_MIN_BLOCKS 4
 #endif
+template <int P> struct SweepBlocks {
+    static constexpr int value = P == 128 ? 3 : FCU_SWEEP_MIN_BLOCKS;
+};
 #ifndef FCU_SCENE_SKIP
 #define FCU_SCENE_SKIP 1
 #endif
@@ -577,7 +582,7 @@ __device__ __forceinline__ void publish_stats(const float* md, const float* mb, 
 // stands for B_in = 0 (the first sweep of a solve that starts from zero):
 // the gather is skipped, which gives the same bits as gathering zeros.
 template <int P>
-__global__ void __launch_bounds__(kWarps * 32, FCU_SWEEP_MIN_BLOCKS) k_sweep_wide(GraphView g, PanelParams pp,
+__global__ void __launch_bounds__(kWarps * 32, SweepBlocks<P>::value) k_sweep_wide(GraphView g, PanelParams pp,
                                                             const float* __restrict__ Bin,
                                                             float* __restrict__ Bout,
                                                             uint32_t* stats, uint32_t* counter,

@@ -46,7 +46,9 @@ namespace {
 constexpr int kWarps = 8;  // warps per CTA
 constexpr int kMaxP = 128;
 #ifndef FCU_NARROW_U
-#define FCU_NARROW_U 8  // loads in flight per lane for 1-4 column panels (12 ties, 16 is slower)
+// loads in flight per lane for 1-4 column panels (the C5 batch, whose
+// thermal band is a 1-column panel: 172.0 ms at 8, 172.6 at 4, 192 at 12 or 16)
+#define FCU_NARROW_U 8
 #endif
 
 struct PanelParams {
@@ -490,7 +492,9 @@ __device__ __forceinline__ void gather_rounds(const uint32_t* __restrict__ rows,
 // solve 11.80 -> 11.35 ms), finer chunks evening out the warps' rows.
 // Scene batches hand out 8: a warp that moves into another scene publishes
 // its per-scene statistics (atomics per column), and small chunks scatter a
-// warp over many scenes (C5: 235 ms at 8 facets, 252 at 2, 236 at 32).
+// warp over many scenes (C5: 235 ms at 8 facets, 252 at 2, 236 at 32 with
+// the register-gather step; 172.8 ms at 8, 176.8 at 4, 174.1 at 6, 172.7 at
+// 12 with the pipelined one).
 #ifndef FCU_CHUNK
 #define FCU_CHUNK 2
 #endif

@@ -46,8 +46,9 @@ namespace {
 constexpr int kWarps = 8;  // warps per CTA
 constexpr int kMaxP = 128;
 #ifndef FCU_NARROW_U
-// loads in flight per lane for 1-4 column panels (the C5 batch, whose
-// thermal band is a 1-column panel: 172.0 ms at 8, 172.6 at 4, 192 at 12 or 16)
+// loads in flight per lane for 1-4 column panels (the 32-scene batch of
+// 4.7 M facets, whose thermal band is a 1-column panel: 172.0 ms at 8, 172.6
+// at 4, 192 at 12 or 16)
 #define FCU_NARROW_U 8
 #endif
 
@@ -309,8 +310,8 @@ template <bool kBF16> constexpr int kVecCols = kBF16 ? 8 : 4;
 // Resident CTAs per SM of the FP32 wide sweep (64 registers at 4): the
 // config-2 forest's 64-column sweep 1.096 ms at 4 against 1.146 at 3 and
 // 1.458 at 2 (latency hidden by warps, not by registers); at 128 columns
-// the spills at 64 registers cost more (C3's batched FP32 solve 11.5 s at 3,
-// 12.3 s at 4), so that width keeps 3.
+// the spills at 64 registers cost more (the batched FP32 solve of 479,600
+// facets x 16,384 columns: 11.5 s at 3, 12.3 s at 4), so that width keeps 3.
 #ifndef FCU_SWEEP_MIN_BLOCKS
 #define FCU_SWEEP_MIN_BLOCKS 4
 #endif
@@ -492,9 +493,9 @@ __device__ __forceinline__ void gather_rounds(const uint32_t* __restrict__ rows,
 // solve 11.80 -> 11.35 ms), finer chunks evening out the warps' rows.
 // Scene batches hand out 8: a warp that moves into another scene publishes
 // its per-scene statistics (atomics per column), and small chunks scatter a
-// warp over many scenes (C5: 235 ms at 8 facets, 252 at 2, 236 at 32 with
-// the register-gather step; 172.8 ms at 8, 176.8 at 4, 174.1 at 6, 172.7 at
-// 12 with the pipelined one).
+// warp over many scenes (the 32-scene batch of 4.7 M facets: 235 ms at 8
+// facets, 252 at 2, 236 at 32 with the register-gather step; 172.8 ms at 8,
+// 176.8 at 4, 174.1 at 6, 172.7 at 12 with the pipelined one).
 #ifndef FCU_CHUNK
 #define FCU_CHUNK 2
 #endif
@@ -1134,7 +1135,7 @@ __global__ void __launch_bounds__(kWarps * 32, StepBlocks<P>::value) k_step_i8(
 #ifndef FCU_STEP_ASYNC
 #define FCU_STEP_ASYNC 1
 #endif
-// Measured on the config-2 forest (C2 graph, 64 columns; the register-gather
+// Measured on the config-2 forest (203,840 facets, 64 columns; the register-gather
 // kernel 0.619 ms): 64-edge stages, 2 ring stages, 1 stage of lookahead
 // 0.527 ms; 2 of lookahead 0.608; 3 ring stages on 2 CTAs per SM 0.636;
 // 32-edge stages with 4 ring stages 0.622 (their per-stage bookkeeping
